@@ -1,0 +1,366 @@
+"""Acquisition throughput benchmark (cells/s; one cell = PRN x Doppler x code phase).
+
+Default workload: batched multi-constellation acquisition of one 40 ms
+capture of int16 I/Q at 50 MHz (synthetic, seeded):
+  GPS L1 C/A   32 PRNs,  1 ms coherent (50,000-point FFT) x 40 blocks, +-5 kHz / 250 Hz (41 bins)
+  GLONASS L1OF 14 FDMA channels k = -7..+6 (562.5 kHz spacing), same grid
+  Galileo E1B  36 PRNs,  4 ms coherent (200,000-point FFT) x 10 blocks, +-5 kHz / 62.5 Hz (161 bins)
+= 1.254e9 cells per step; one step = the 16 jobs of one capture through
+ugsdr_acquire_batch.  `--config gps_l1_4mhz` runs the 4 MHz / 4000-point
+GPS L1 C/A search instead.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the CPU restatement of the reference path
+(oracle/, the reference's ProcessBpsk loop with per-call FFTs) on the host
+cores, on a bounded sample of the same workload, and prints the same line.
+Multi-GPU: one process per GPU, each running its own replica of the
+workload (jobs are independent; no collective), `scaling` = weak.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+FS = 50e6
+CENTER = 1590e6
+SIGMA = 20.0
+
+
+def log2(x):
+    return math.log(x, 2)
+
+
+# ------------------------------------------------------------------ workload
+def galileo_chips():
+    z = np.load(ROOT / "tests" / "golden" / "codes.npz")
+    n = int(z["galileo_e1b_len"])
+    bits = np.unpackbits(z["galileo_e1b"], axis=1)[:, :n]
+    return (1.0 - 2.0 * bits).astype(np.float32)
+
+
+def multi_workload(seed: int = 2):
+    """Jobs (as plain dicts) and the synthetic int16 capture."""
+    from ugsdr_gb300 import _lib as L
+    from ugsdr_gb300 import api, signals
+    rng = np.random.default_rng(seed)
+    gps = {p: api.prn_code(L.GPS_L1CA, p) for p in range(32)}
+    glo = api.prn_code(L.GLONASS_L1OF, 0)
+    e1b = galileo_chips()
+    if_gps = 1575.42e6 - CENTER
+    ems = []
+    for p in rng.choice(32, 8, replace=False):
+        ems.append(signals.Emitter(gps[int(p)], 1.023e6, rng.uniform(0, 1023), if_gps + rng.uniform(-4500, 4500),
+                                   rng.uniform(38, 48), 50.0, rng.uniform(0, 6.28)))
+    for k in rng.choice(np.arange(-7, 7), 8, replace=False):
+        f_if = 1602e6 + int(k) * 0.5625e6 - CENTER
+        ems.append(signals.Emitter(glo, 0.511e6, rng.uniform(0, 511), f_if + rng.uniform(-4500, 4500),
+                                   rng.uniform(38, 48), 50.0, rng.uniform(0, 6.28)))
+    for p in rng.choice(36, 8, replace=False):
+        ems.append(signals.Emitter(e1b[int(p)], 2.046e6,
+                                   rng.uniform(0, 8184), if_gps + rng.uniform(-4500, 4500), rng.uniform(38, 48), 250.0,
+                                   rng.uniform(0, 6.28)))
+    raw = signals.synthesize(ems, FS, int(FS * 0.040), SIGMA, "ci16", seed + 100)
+    jobs = [dict(system="gps", codes=[gps[p] for p in range(32)], n=50000, k=40, step=250.0, fe=-if_gps, if_=if_gps)]
+    for k in range(-7, 7):
+        f_if = 1602e6 + k * 0.5625e6 - CENTER
+        jobs.append(dict(system="glo", codes=[glo], n=50000, k=40, step=250.0, fe=-f_if, if_=f_if))
+    jobs.append(dict(system="gal", codes=[e1b[p] for p in range(36)], n=200000, k=10, step=62.5, fe=-if_gps, if_=if_gps))
+    return jobs, raw
+
+
+def gps_4mhz_workload(seed: int = 1):
+    from ugsdr_gb300 import _lib as L
+    from ugsdr_gb300 import api, signals
+    gps = {p: api.prn_code(L.GPS_L1CA, p) for p in range(32)}
+    raw, _ = signals.gps_l1_config(seed=seed, codes=gps)
+    jobs = [dict(system="gps", codes=[gps[p] for p in range(32)], n=4000, k=10, step=500.0, fe=0.0, if_=0.0, fs=4e6)]
+    return jobs, raw
+
+
+def n_doppler(step, rng=5000.0):
+    n, d = 0, -rng
+    while d <= rng:
+        n += 1
+        d += step
+    return n
+
+
+def job_cells(j):
+    return len(j["codes"]) * n_doppler(j["step"]) * j["n"]
+
+
+def inverse_flops(j):
+    """Algorithmic flops of the inverse stage: per (code, Doppler, block) one
+    N-point IFFT (5 N log2 N) + conj-multiply and |.| accumulate (10 N)."""
+    n = j["n"]
+    return len(j["codes"]) * n_doppler(j["step"]) * j["k"] * (5 * n * log2(n) + 10 * n)
+
+
+def inverse_bytes(j):
+    """Algorithmic HBM bytes of the inverse stage: one-sided spectra read once
+    per (Doppler, block) row, code spectra once, 16 B per cell record."""
+    n, nd = j["n"], n_doppler(j["step"])
+    return nd * j["k"] * (n // 2 + 1) * 8 + len(j["codes"]) * (n // 2 + 1) * 8 + len(j["codes"]) * nd * 16
+
+
+# ------------------------------------------------------------------- clocks
+class ClockSampler:
+    def __init__(self):
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200", "-i", str(int(os.environ.get("LOCAL_RANK", 0)))],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if len(r) > 8 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 8 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows if len(r) > 8 for i in range(4) if r[5 + i] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+# ------------------------------------------------------------------ ours arm
+def run_ours(args, world, rank):
+    import torch
+    from ugsdr_gb300 import _lib as L
+    from ugsdr_gb300 import api
+
+    dev = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(dev)
+    jobs, raw = (multi_workload() if args.config == "multi" else gps_4mhz_workload())
+    fs = jobs[0].get("fs", FS)
+    stype = L.SAMPLES_CI16 if raw.dtype == np.int16 else L.SAMPLES_CI8
+    ctx = api.Context(dev)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    handles = []
+    for j in jobs:
+        hs = [ctx.code_put(c, j["n"], repeats=1) for c in j["codes"]]
+        handles.append(hs)
+    # inputs resident in HBM for `value`; pinned host copy for `e2e`
+    d_raw = torch.from_numpy(raw.copy()).cuda(dev)
+    h_raw = torch.empty(raw.shape, dtype=d_raw.dtype, pin_memory=True)
+    h_raw.copy_(torch.from_numpy(raw))
+    h_np = h_raw.numpy()
+    n_samples = raw.shape[0]
+
+    def mk(on_device):
+        out = []
+        for j, hs in zip(jobs, handles):
+            src = d_raw.data_ptr() if on_device else h_np
+            out.append(ctx.make_job(src, stype, fs, j["n"], j["k"], hs, 5000.0, j["step"], n_samples=n_samples,
+                                    on_device=on_device, frontend_frequency=j["fe"], intermediate_frequency=j["if_"]))
+        return out
+
+    dev_jobs, host_jobs = mk(True), mk(False)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{dev}")  # > L2 (129 MB)
+    cells = sum(job_cells(j) for j in jobs)
+
+    for _ in range(args.warmup):
+        ctx.acquire_batch(dev_jobs)
+    torch.cuda.synchronize()
+
+    def timed(job_list, k, with_timing):
+        times = []
+        launches0 = ctx.launch_count()
+        if with_timing:
+            ctx.reset_timing()
+            ctx.enable_timing(True)
+        for _ in range(k):
+            with torch.cuda.stream(stream):
+                flush.zero_()  # L2 flush between steps, outside the events
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            stream.synchronize()
+            s.record(stream)
+            t0 = time.perf_counter()
+            ctx.acquire_batch(job_list)
+            e.record(stream)
+            e.synchronize()
+            wall = time.perf_counter() - t0
+            times.append(max(s.elapsed_time(e) / 1e3, wall))
+        ctx.enable_timing(False)
+        return times, (ctx.launch_count() - launches0) / k
+
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler() as clk:
+        times, launches = timed(dev_jobs, args.steps, True)
+    torch.cuda.synchronize()
+    t_step = float(np.mean(times))
+    if world > 1:
+        t = torch.tensor([t_step], device=f"cuda:{dev}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_step = float(t.item())
+    inv_name = "acq_inverse_large" if jobs[0]["n"] > 12000 else "acq_inverse"
+    n_inv, ms_inv = ctx.kernel_time(inv_name)
+    n_fwd, ms_fwd = ctx.kernel_time(inv_name.replace("inverse", "forward"))
+    flops_inv = sum(inverse_flops(j) for j in jobs) * args.steps
+    bytes_inv = sum(inverse_bytes(j) for j in jobs) * args.steps
+
+    # end to end through the C ABI with pinned host samples
+    e2e_times, _ = timed(host_jobs, max(2, args.steps // 2), False)
+    t_e2e = float(np.mean(e2e_times))
+    h2d = raw.nbytes  # one upload per step (jobs share the capture)
+    n_cells_rec = sum(len(j["codes"]) * n_doppler(j["step"]) for j in jobs)
+    d2h = n_cells_rec * 16
+
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    sm_max = peaks.get("sm_max_mhz", 2070.0)
+    n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
+    fp32_peak = n_sm * 128 * 2 * sm_max * 1e6 / 1e12  # TFLOP/s: SMs x 128 FP32 lanes x FMA x clock
+    achieved = flops_inv / (ms_inv / 1e3) / 1e12 if ms_inv > 0 else None
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    hbm_ach = bytes_inv / (ms_inv / 1e3) / 1e9 if ms_inv > 0 else None
+    clocks = clk.summary()
+    line = {
+        "metric": "acq cells/s (PRN x Doppler x code-phase)",
+        "value": world * cells / t_step,
+        "unit": "cells/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": t_step * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded int16/int8 I/Q captures; Galileo E1B chips from the reference's code tables)",
+        "config": {"workload": "multi-constellation batch: int16 I/Q 50 MHz 40 ms; GPS L1 C/A 32x41x50000x40, "
+                               "GLONASS L1OF 14ch x41x50000x40, Galileo E1B 36x161x200000x10"
+                   if args.config == "multi" else "GPS L1 C/A int8 4 MHz 10 ms; 32 PRN x 21 Doppler x 4000 x 10",
+                   "cells_per_step": cells, "jobs_per_step": len(jobs), "parallelism": f"replicas x{world}",
+                   "l2": "flushed between steps (256 MB write); working set > L2"},
+        "e2e": {"value": world * cells / t_e2e, "unit": "cells/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": t_e2e * 1e3},
+        "gpu_launches": launches,
+        "roofline": {"bound": "fp32", "kernel": inv_name, "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                     "frac": achieved / fp32_peak if achieved else None, "traffic": None,
+                     "peak_source": f"{n_sm} SMs x 128 FP32 lanes x 2 x sm_max_mhz {sm_max} (MEASURED_PEAKS.json)",
+                     "launches": n_inv, "avg_launch_ms": ms_inv / max(n_inv, 1),
+                     "hbm": {"achieved": hbm_ach, "peak": hbm_peak, "unit": "GB/s",
+                             "frac": hbm_ach / hbm_peak if hbm_ach else None},
+                     "forward_ms_share": ms_fwd / (ms_fwd + ms_inv) if ms_inv else None},
+        "clocks": clocks,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(args, jobs, raw, fs)
+    return line
+
+
+# ------------------------------------------------------------ CPU reference
+def cpu_baseline(args, jobs, raw, fs, budget_s: float = 20.0):
+    """Bounded sample of the same workload on the host cores through the CPU
+    restatement of the reference loop (oracle/): for each system, as many
+    codes as threads, 1 Doppler bin, the full K blocks; per-cell time scaled
+    to the whole step."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import pyoracle
+    threads = os.cpu_count() or 1
+    x = raw.astype(np.float32)
+    x = (x[:, 0] + 1j * x[:, 1]).astype(np.complex64) if raw.ndim == 2 else x.astype(np.complex64)
+    total_t, sample_desc = 0.0, []
+    seen = {}
+    for j in jobs:
+        key = (j["system"], j["n"], j["k"])
+        if key not in seen:
+            ncodes = min(len(j["codes"]), threads)
+            codes = np.stack([pyoracle.upsample(c, j["n"]) for c in j["codes"][:ncodes]])
+            xx = pyoracle.table_mix(x[: j["n"] * j["k"]], fs, j["fe"]) if j["fe"] else x[: j["n"] * j["k"]]
+            t0 = time.perf_counter()
+            pyoracle.acquire_many(xx, j["n"], j["k"], codes, fs, 0.0, 1.0, threads=threads)
+            dt = time.perf_counter() - t0
+            seen[key] = dt / (ncodes * j["n"])  # seconds per cell
+            sample_desc.append(f"{j['system']}: {ncodes} codes x 1 Doppler x {j['n']} x {j['k']} blocks in {dt:.2f}s")
+        total_t += seen[key] * job_cells(j)
+    cells = sum(job_cells(j) for j in jobs)
+    return {"value": cells / total_t, "unit": "cells/s", "cores": threads, "kind": "port",
+            "sample": "; ".join(sample_desc) + " -> per-cell time x cells of the full step (project FFT, not FFTW)",
+            "ms_per_step_extrapolated": total_t * 1e3}
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return None
+    jobs, raw = (multi_workload() if args.config == "multi" else gps_4mhz_workload())
+    fs = jobs[0].get("fs", FS)
+    vals = []
+    for _ in range(args.warmup + args.steps):
+        vals.append(cpu_baseline(args, jobs, raw, fs))
+    vals = vals[args.warmup:]
+    v = float(np.mean([b["value"] for b in vals]))
+    cells = sum(job_cells(j) for j in jobs)
+    b = vals[-1]
+    return {
+        "metric": "acq cells/s (PRN x Doppler x code-phase)", "value": v, "unit": "cells/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": cells / v * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
+        "config": {"workload": "same as --impl ours", "cells_per_step": cells},
+        "cpu_baseline": {"value": v, "unit": "cells/s", "cores": b["cores"], "kind": "port", "sample": b["sample"]},
+        "e2e": {"value": v, "unit": "cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--config", choices=["multi", "gps_l1_4mhz"], default="multi")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    rank = int(os.environ.get("RANK", 0))
+    if world > 1 and args.impl == "ours":
+        import torch
+        torch.distributed.init_process_group("nccl")
+    line = run_ours(args, world, rank) if args.impl == "ours" else run_reference(args, world, rank)
+    if rank == 0 and line is not None:
+        print(json.dumps(line), flush=True)
+    if world > 1 and args.impl == "ours":
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,293 @@
+/*
+ * ugsdr_cuda.h - C ABI of the GB300 (sm_103a) acquisition-and-correlation
+ * backend for ugsdr.
+ *
+ * Plain pointers and sizes only.  Every function returns an int status:
+ * UGSDR_OK (0) or a negative UGSDR_E_* code; the message of the last failure
+ * on a context is available from ugsdr_last_error().  No C++ exception
+ * crosses this boundary; the C++ policy adapters (ugsdr_cuda_policies.hpp)
+ * turn a failure into std::runtime_error the way the reference's CPU policies
+ * throw (e.g. src/math/reshape_and_sum.hpp:17, src/correlator/correlator.hpp:31).
+ *
+ * Pointers: unless a function says otherwise, buffers are HOST memory owned
+ * by the caller (the reference policies work on std::vector); the context
+ * owns all device memory (code-spectrum cache, FFT twiddles, scratch).  The
+ * batched acquisition job also accepts device-resident samples.
+ *
+ * Threading: a context serialises its own calls on its stream; use one
+ * context per host thread for concurrency (the reference calls its policies
+ * from std::execution::par_unseq lambdas, src/acquisition/fse.hpp:294).
+ */
+#ifndef UGSDR_CUDA_H
+#define UGSDR_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define UGSDR_CUDA_ABI_VERSION 1
+
+enum ugsdr_status {
+	UGSDR_OK = 0,
+	UGSDR_E_INVALID = -1,      /* bad argument (size, range, null pointer) */
+	UGSDR_E_CUDA = -2,         /* CUDA runtime error */
+	UGSDR_E_NOMEM = -3,        /* device allocation or admission refused */
+	UGSDR_E_UNSUPPORTED = -4,  /* size/radix/signal not handled */
+	UGSDR_E_NOT_FOUND = -5,    /* unknown handle */
+	UGSDR_E_QUEUE_FULL = -6,   /* serving queue has no free slot */
+	UGSDR_E_TIMEOUT = -7       /* a bounded device-side wait gave up */
+};
+
+/* Signal ids: the values of ugsdr::Signal (src/common.hpp:40-66). */
+enum ugsdr_signal {
+	UGSDR_GPS_L1CA = 0,
+	UGSDR_GPS_L2CM = 1,
+	UGSDR_GPS_L5I = 2,
+	UGSDR_GPS_L5Q = 3,
+	UGSDR_GLONASS_L1OF = 4,
+	UGSDR_GLONASS_L2OF = 5,
+	UGSDR_GALILEO_E1B = 6,
+	UGSDR_GALILEO_E1C = 7
+};
+
+/* Sample formats at the front-end boundary (src/signal_parameters.hpp:150-183). */
+enum ugsdr_sample_type {
+	UGSDR_SAMPLES_CF32 = 0, /* interleaved float I/Q (std::complex<float>) */
+	UGSDR_SAMPLES_CI8 = 1,  /* interleaved int8 I/Q  (FileType::Iq_8_plus_8) */
+	UGSDR_SAMPLES_CI16 = 2, /* interleaved int16 I/Q (FileType::Iq_16_plus_16) */
+	UGSDR_SAMPLES_RI8 = 3   /* real int8, imag = 0   (FileType::Real_8) */
+};
+
+/* Matched-filter spectrum convention. */
+enum ugsdr_spectrum_mode {
+	/* reference FFTW path: code spectrum from an r2c transform, bins
+	 * N/2+1..N-1 zero, inverse scaled by 2/N (src/math/dft.hpp:37-46, 124-129) */
+	UGSDR_SPECTRUM_ONE_SIDED = 0,
+	/* IPP / ArrayFire paths: full conj spectrum, inverse scaled by 1/N */
+	UGSDR_SPECTRUM_TWO_SIDED = 1
+};
+
+enum ugsdr_statistic {
+	UGSDR_STAT_ABS = 0,  /* |y|   (SequentialAbs, src/math/abs.hpp:24-32) */
+	UGSDR_STAT_ABS2 = 1  /* |y|^2 */
+};
+
+typedef struct ugsdr_ctx ugsdr_ctx;
+
+/* ---------------------------------------------------------------- context */
+int ugsdr_ctx_create(int device, ugsdr_ctx** out);
+int ugsdr_ctx_destroy(ugsdr_ctx* ctx);
+/* Run subsequent work on a caller-owned cudaStream_t (NULL = context's own). */
+int ugsdr_ctx_set_stream(ugsdr_ctx* ctx, void* cuda_stream);
+int ugsdr_ctx_synchronize(ugsdr_ctx* ctx);
+const char* ugsdr_last_error(const ugsdr_ctx* ctx);
+/* Number of kernels this context has launched so far. */
+int ugsdr_ctx_launch_count(const ugsdr_ctx* ctx, uint64_t* count);
+int ugsdr_abi_version(void);
+/* CUDA-event timing of the engine's kernels on the stream they are launched
+ * on (off by default; a pair of events per launch while on). */
+int ugsdr_ctx_enable_timing(ugsdr_ctx* ctx, int on);
+/* Launch count and summed device time (ms) of the kernels named `kernel`
+ * ("acq_forward", "acq_inverse", "acq_forward_large", "acq_inverse_large",
+ * "track_bank", ...) since timing was enabled or last reset.  Synchronises. */
+int ugsdr_ctx_kernel_time(ugsdr_ctx* ctx, const char* kernel, uint64_t* launches, double* total_ms);
+int ugsdr_ctx_reset_timing(ugsdr_ctx* ctx);
+
+/* ------------------------------------------------------------- PRN codes */
+/* Replaces ugsdr::Codegen<Impl>::Get<T>(sv) / PrnGenerator<signal>
+ * (src/prn_codes/codegen.hpp:23-36, codegen_wrapper.hpp:32-61): writes the
+ * +-1 chips of `sv` (0-based id, as the reference) into out[0..cap).  *len
+ * receives the code length even when cap is too small (then UGSDR_E_INVALID).
+ * LFSR codes (GPS L1 C/A PRN 1-37, L5I/L5Q PRN 1-32, GLONASS L1OF/L2OF) are
+ * generated here; memory codes (Galileo E1B/E1C) return UGSDR_E_UNSUPPORTED:
+ * pass their chips to ugsdr_code_put directly. */
+int ugsdr_prn_code(int signal, int sv, float* out, size_t cap, size_t* len);
+
+/* RepeatCodeNTimes + Upsampler::Transform (src/common.hpp:78-85,
+ * src/resample/upsampler.hpp:30-37): dst[i] = src[(i*L/S) % L], L = len*repeats. */
+int ugsdr_repeat_upsample(const float* chips, size_t len, size_t repeats, float* dst, size_t samples);
+
+/* ------------------------------------------------- code-spectrum cache */
+/* Builds conj(FFT(code)) on the device for a code of `samples` samples made
+ * from `chips` by RepeatCodeNTimes(repeats) + upsampling, optionally with the
+ * sign of segment s (length sign_segment samples) flipped where bit s of
+ * sign_mask is set (the per-ms sign permutations of ProcessGalileo,
+ * src/acquisition/fse.hpp:374-388).  Replaces MatchedFilter::PrepareCodeSpectrum
+ * (src/matched_filter/matched_filter.hpp:27-30) for the batched engine; the
+ * spectrum stays resident until released or the context is destroyed. */
+int ugsdr_code_put(ugsdr_ctx* ctx, const float* chips, size_t n_chips, size_t repeats, size_t samples,
+	uint32_t sign_mask, size_t sign_segment, int spectrum_mode, int* handle);
+int ugsdr_code_release(ugsdr_ctx* ctx, int handle);
+
+/* ---------------------------------------------------- batched acquisition */
+/* One search = FastSearchEngineBase::ProcessBpsk (src/acquisition/fse.hpp:
+ * 242-276) for every code in `codes`, over K = n_blocks consecutive coherent
+ * blocks of block_samples samples whose GetOneMsPeak outputs (fse.hpp:201-220)
+ * are summed non-coherently (K = 1 is the reference as written).
+ * Doppler grid: d = -range; d <= range; d += step (fse.hpp:250-252), each
+ * applied with the TableMixer NCO (src/mixer/table_mixer.hpp:78-101). */
+typedef struct ugsdr_acq_job {
+	const void* samples;       /* n_samples samples of sample_type */
+	int sample_type;           /* ugsdr_sample_type */
+	int samples_on_device;     /* 1: `samples` is a device pointer */
+	size_t n_samples;          /* >= block_samples * n_blocks */
+	double sampling_rate;      /* Hz (the acquisition rate, new_sampling_rate) */
+	double intermediate_frequency; /* added to the reported Doppler (fse.hpp:263) */
+	/* Front-end translation applied before the Doppler mix, as
+	 * Mixer::Translate(signal, fs, frontend_frequency) (fse.hpp:289, 348);
+	 * 0 = none.  For a signal at IF f_if the reference passes -f_if. */
+	double frontend_frequency;
+	double code_offset_ratio;  /* signal_fs / acquisition_fs (fse.hpp:247, 262) */
+	size_t block_samples;      /* N: coherent block = FFT size */
+	size_t n_blocks;           /* K */
+	size_t fold_samples;       /* 0: no reshape; else samples per ms (fse.hpp:203) */
+	int fold_coherent;         /* 1: |.| then fold; 0: fold complex then |.| (fse.hpp:209-218) */
+	double doppler_range;
+	double doppler_step;
+	const int* codes;          /* n_codes handles from ugsdr_code_put (same N, mode) */
+	int n_codes;
+	int statistic;             /* ugsdr_statistic */
+	int spectrum_mode;         /* ugsdr_spectrum_mode, must match the codes */
+} ugsdr_acq_job;
+
+/* Per-code result: the AcquisitionResult<T> fields (src/acquisition/acquisition_result.hpp:11-19). */
+typedef struct ugsdr_acq_result {
+	int code;            /* handle */
+	int doppler_bin;     /* index into the Doppler grid of the kept maximum */
+	uint32_t index;      /* peak sample index in the (folded) output */
+	uint32_t n_doppler;  /* Doppler bins searched */
+	double doppler;      /* grid Doppler + intermediate_frequency */
+	double code_offset;  /* code_offset_ratio * index */
+	double level;        /* peak value */
+	double sigma;        /* std + mean, as AcquisitionResult::sigma (fse.hpp:261) */
+	double mean;
+	double std;
+	double snr;          /* level / sigma (GetSnr) */
+} ugsdr_acq_result;
+
+/* Per (code, Doppler) cell record, optional output. */
+typedef struct ugsdr_acq_cell {
+	float level;
+	uint32_t index;
+	float mean;
+	float std;
+} ugsdr_acq_cell;
+
+/* Runs one job; results[n_codes]; cells (optional, may be NULL) receives
+ * n_codes x n_doppler records, code-major. */
+int ugsdr_acquire(ugsdr_ctx* ctx, const ugsdr_acq_job* job, ugsdr_acq_result* results, ugsdr_acq_cell* cells);
+/* Runs several jobs back to back on the context's stream (one persistent set
+ * of launches per job, no host synchronisation in between). */
+int ugsdr_acquire_batch(ugsdr_ctx* ctx, const ugsdr_acq_job* jobs, int n_jobs, ugsdr_acq_result* const* results);
+/* Number of Doppler bins the reference loop visits for (range, step). */
+int ugsdr_doppler_bins(double range, double step, uint32_t* n);
+
+/* ---------------------------------------------- per-op policy entries */
+/* Each replaces one reference policy implementation; host buffers. */
+
+/* Mixer<Impl>::Translate(T& src_dst, fs, f, phase) with TableMixer arithmetic
+ * (src/mixer/mixer.hpp:33-42, src/mixer/table_mixer.hpp:78-101). In place. */
+int ugsdr_mix(ugsdr_ctx* ctx, float* iq, size_t n, double fs, double frequency, double phase);
+/* SequentialDft::Transform on complex data (src/math/dft.hpp:114-135, 211-220):
+ * forward unnormalised, inverse scaled 2/N (FFTW path). */
+int ugsdr_dft(ugsdr_ctx* ctx, const float* in_iq, float* out_iq, size_t n, int inverse);
+/* MatchedFilter::PrepareCodeSpectrum (src/matched_filter/matched_filter.hpp:27-30, 49-54). */
+int ugsdr_matched_filter_prepare(ugsdr_ctx* ctx, const float* code, size_t n, int spectrum_mode, float* spectrum_iq);
+/* MatchedFilter::FilterOptimized (matched_filter.hpp:32-35, 56-61), in place. */
+int ugsdr_matched_filter(ugsdr_ctx* ctx, float* iq, size_t n, const float* spectrum_iq, int spectrum_mode);
+/* Abs::Transform (src/math/abs.hpp:13-17). */
+int ugsdr_abs(ugsdr_ctx* ctx, const float* iq, size_t n, float* out);
+/* ReshapeAndSum::Transform (src/math/reshape_and_sum.hpp:20-30): real (is_complex=0)
+ * or complex data folded to `block` values; UGSDR_E_INVALID when n % block != 0. */
+int ugsdr_reshape_sum(ugsdr_ctx* ctx, const float* in, size_t n, size_t block, int is_complex, float* out);
+/* MaxIndex::Transform (src/math/max_index.hpp:15-24): first maximum. */
+int ugsdr_max_index(ugsdr_ctx* ctx, const float* in, size_t n, float* value, size_t* index);
+/* MeanStdDev::Calculate (src/math/mean_stddev.hpp:13-22): mean, unbiased sigma. */
+int ugsdr_mean_stddev(ugsdr_ctx* ctx, const float* in, size_t n, float* mean, float* sigma);
+/* Upsampler::Transform (src/resample/upsampler.hpp:13-23), real or complex. */
+int ugsdr_upsample(ugsdr_ctx* ctx, const float* in, size_t n, int is_complex, float* out, size_t samples);
+/* Resampler::Transform (src/resample/resampler.hpp:15-25; ZOH to the lcm then
+ * boxcar mean, decimator.hpp:144-160), complex samples.  *n_out receives the
+ * output length; pass out = NULL to query it. */
+int ugsdr_resample(ugsdr_ctx* ctx, const float* in_iq, size_t n, uint64_t new_fs, uint64_t old_fs,
+	float* out_iq, size_t cap, size_t* n_out);
+/* Correlator::Correlate (src/correlator/correlator.hpp:16-20, 27-34). */
+int ugsdr_correlate(ugsdr_ctx* ctx, const float* iq, const float* code, size_t n, float* out_iq);
+/* SignalParametersBase::GetPartialSignal int -> complex<float> conversion
+ * (src/signal_parameters.hpp:150-183). */
+int ugsdr_convert_samples(ugsdr_ctx* ctx, const void* in, int sample_type, size_t n, float* out_iq);
+
+/* ------------------------------------------------------ tracking bank */
+/* Correlator bank for many channels per 1 ms epoch: carrier wipe-off and
+ * VE/E/P/L/VL taps (Tracker::GetEpl / TrackingParameters::CorrelateSplit,
+ * src/tracking/tracker.hpp:119-139, src/tracking/tracking_parameters.hpp:472-493)
+ * followed by the PLL/FLL and DLL updates (tracking_parameters.hpp:495-528). */
+typedef struct ugsdr_track_channel {
+	int code;                 /* index into the bank's code table */
+	double sampling_rate;     /* Hz */
+	double code_frequency;    /* chips/s (base) */
+	double code_length;       /* chips per code period */
+	double code_phase;        /* chips at the first sample of the first epoch */
+	double carrier_frequency; /* Hz (initial Doppler + IF) */
+	double carrier_phase;     /* rad */
+	int boc;                  /* 1: very-early/very-late taps are meaningful */
+} ugsdr_track_channel;
+
+typedef struct ugsdr_track_config {
+	double early_late_spacing;      /* chips (0.5 in the spec; reference 0.25 each side) */
+	double very_early_late_spacing; /* chips (0.15) */
+	double pll_bandwidth;           /* Hz (15) */
+	double dll_bandwidth;           /* Hz (1) */
+	double fll_bandwidth;           /* Hz (0 = off) */
+	double integration_time;        /* s (0.001) */
+} ugsdr_track_config;
+
+/* Per channel per epoch output: taps VE, E, P, L, VL as I/Q and loop state. */
+typedef struct ugsdr_track_output {
+	float taps[5][2];
+	double carrier_frequency;
+	double carrier_phase;       /* rad, wrapped */
+	double code_phase;          /* chips */
+	double code_frequency;
+	double phase_error;         /* PLL discriminator, cycles */
+	double code_error;          /* DLL discriminator */
+} ugsdr_track_output;
+
+typedef struct ugsdr_track_bank ugsdr_track_bank;
+
+/* codes: n_codes x code_len_max chips (+-1), code_lens[n_codes]. */
+int ugsdr_track_create(ugsdr_ctx* ctx, const ugsdr_track_config* cfg, const ugsdr_track_channel* channels, int n_channels,
+	const float* codes, const int* code_lens, int n_codes, int code_len_max, ugsdr_track_bank** bank);
+/* Advances every channel by n_epochs epochs of samples (n_epochs * samples_per_epoch,
+ * one shared sampling rate), writing n_epochs x n_channels outputs (host or NULL). */
+int ugsdr_track_run(ugsdr_track_bank* bank, const void* samples, int sample_type, int samples_on_device,
+	size_t samples_per_epoch, int n_epochs, ugsdr_track_output* outputs);
+int ugsdr_track_destroy(ugsdr_track_bank* bank);
+
+/* ------------------------------------------------------------ serving */
+/* Continuous-batching acquisition server: jobs are admitted while others run,
+ * as slots and device memory allow; code spectra stay cached across requests. */
+typedef struct ugsdr_server ugsdr_server;
+typedef struct ugsdr_server_config {
+	int max_inflight;          /* concurrent jobs on the device */
+	size_t memory_budget;      /* bytes of device memory admission may use (0 = free memory) */
+	int queue_capacity;        /* pending requests before UGSDR_E_QUEUE_FULL */
+} ugsdr_server_config;
+
+int ugsdr_server_create(ugsdr_ctx* ctx, const ugsdr_server_config* cfg, ugsdr_server** server);
+/* Copies the job description (and the host samples) and returns a ticket. */
+int ugsdr_server_submit(ugsdr_server* server, const ugsdr_acq_job* job, uint64_t* ticket);
+/* Non-blocking: 1 + results when done, 0 while pending. results[n_codes]. */
+int ugsdr_server_poll(ugsdr_server* server, uint64_t ticket, ugsdr_acq_result* results, int* done);
+/* Blocks until every submitted job finished. */
+int ugsdr_server_drain(ugsdr_server* server);
+int ugsdr_server_destroy(ugsdr_server* server);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

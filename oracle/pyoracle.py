@@ -1,0 +1,136 @@
+"""ctypes binding of the CPU oracle (oracle/liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: used by tests/, __graft_entry__.smoke() (as the
+checker) and bench.py's cpu_baseline / --impl reference arm.  The product
+path never imports this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "liboracle.so"
+_lib = None
+
+
+def load() -> C.CDLL:
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB.exists():
+        subprocess.run(["make", "-s", "-C", str(HERE), "all"], check=True)
+    lib = C.CDLL(str(LIB))
+    vp, sz, d, i = C.c_void_p, C.c_size_t, C.c_double, C.c_int
+    sigs = {
+        "orc_table_mixer_f32": [vp, sz, d, d, d],
+        "orc_table_mixer_f64": [vp, sz, d, d, d],
+        "orc_dft_c2c_f32": [vp, vp, sz, i],
+        "orc_dft_c2c_f64": [vp, vp, sz, i],
+        "orc_dft_r2c_f32": [vp, vp, sz],
+        "orc_prepare_code_spectrum_f32": [vp, sz, i, vp],
+        "orc_prepare_code_spectrum_f64": [vp, sz, i, vp],
+        "orc_filter_optimized_f32": [vp, sz, vp, i],
+        "orc_filter_optimized_f64": [vp, sz, vp, i],
+        "orc_abs_f32": [vp, sz, vp],
+        "orc_reshape_sum_f32": [vp, sz, sz],
+        "orc_reshape_sum_c32": [vp, sz, sz],
+        "orc_max_index_f32": [vp, sz],
+        "orc_mean_std_f32": [vp, sz, vp, vp],
+        "orc_mean_std_f64": [vp, sz, vp, vp],
+        "orc_upsample_f32": [vp, sz, vp, sz],
+        "orc_resample_c32": [vp, sz, vp, sz, sz],
+        "orc_correlate_f32": [vp, vp, sz, vp],
+        "orc_correlate_split_f32": [vp, vp, sz, d, d, vp],
+        "orc_acquire_f32": [vp, sz, sz, sz, vp, d, d, d, d, d, i, i, i, i, vp, vp, vp],
+        "orc_acquire_f64": [vp, sz, sz, sz, vp, d, d, d, d, d, i, i, i, i, vp, vp, vp],
+        "orc_acquire_many_f32": [vp, sz, sz, sz, vp, sz, d, d, d, d, d, i, i, i, i, i, vp],
+    }
+    for name, args in sigs.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = None
+    lib.orc_reshape_sum_f32.restype = i
+    lib.orc_reshape_sum_c32.restype = i
+    lib.orc_max_index_f32.restype = sz
+    lib.orc_resample_c32.restype = sz
+    _lib = lib
+    return lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+REC_FIELDS = ("level", "sigma", "code_offset", "doppler", "index", "doppler_bin", "snr", "mean", "std")
+
+
+def table_mix(x: np.ndarray, fs: float, f: float, phase: float = 0.0) -> np.ndarray:
+    y = np.array(x, copy=True)
+    fn = load().orc_table_mixer_f64 if y.dtype == np.complex128 else load().orc_table_mixer_f32
+    fn(_p(y), y.size, fs, f, phase)
+    return y
+
+
+def acquire(iq_complex: np.ndarray, n: int, k_blocks: int, code: np.ndarray, fs: float, range_hz: float, step_hz: float,
+            if_freq: float = 0.0, ratio: float = 1.0, reshape: bool = False, coherent: bool = True, stat: int = 0,
+            spectrum_mode: int = 0, double: bool = False, grid: bool = False):
+    """ProcessBpsk restated (oracle.cpp Acquire).  iq_complex: complex samples."""
+    lib = load()
+    if double:
+        x = np.ascontiguousarray(iq_complex, np.complex128)
+        c = np.ascontiguousarray(code, np.float64)
+        fn = lib.orc_acquire_f64
+    else:
+        x = np.ascontiguousarray(iq_complex, np.complex64)
+        c = np.ascontiguousarray(code, np.float32)
+        fn = lib.orc_acquire_f32
+    rec = np.zeros(9)
+    nbins = len(doppler_grid(range_hz, step_hz))
+    g = np.zeros((nbins, 4)) if grid else None
+    fn(_p(x), x.size, n, k_blocks, _p(c), fs, range_hz, step_hz, if_freq, ratio, 1 if reshape else 0, 1 if coherent else 0,
+       stat, spectrum_mode, _p(rec), _p(g), None)
+    out = dict(zip(REC_FIELDS, rec))
+    if grid:
+        return out, g
+    return out
+
+
+def acquire_many(iq_complex: np.ndarray, n: int, k_blocks: int, codes: np.ndarray, fs: float, range_hz: float,
+                 step_hz: float, threads: int = 1, reshape: bool = False, coherent: bool = True, stat: int = 0,
+                 spectrum_mode: int = 0) -> np.ndarray:
+    lib = load()
+    x = np.ascontiguousarray(iq_complex, np.complex64)
+    c = np.ascontiguousarray(codes, np.float32)
+    recs = np.zeros((c.shape[0], 9))
+    lib.orc_acquire_many_f32(_p(x), x.size, n, k_blocks, _p(c), c.shape[0], fs, range_hz, step_hz, 0.0, 1.0,
+                             1 if reshape else 0, 1 if coherent else 0, stat, spectrum_mode, threads, _p(recs))
+    return recs
+
+
+def doppler_grid(range_hz: float, step_hz: float) -> list[float]:
+    out, d = [], -range_hz
+    while d <= range_hz:
+        out.append(d)
+        d += step_hz
+    return out
+
+
+def upsample(code: np.ndarray, samples: int) -> np.ndarray:
+    code = np.ascontiguousarray(code, np.float32)
+    out = np.empty(samples, np.float32)
+    load().orc_upsample_f32(_p(code), code.size, _p(out), samples)
+    return out
+
+
+def resample(x: np.ndarray, new_fs: int, old_fs: int) -> np.ndarray:
+    import math
+    x = np.ascontiguousarray(x, np.complex64)
+    lcm = new_fs * old_fs // math.gcd(new_fs, old_fs)
+    up = lcm * x.size // old_fs
+    out = np.empty(up // (lcm // new_fs) + 2, np.complex64)
+    n = load().orc_resample_c32(_p(x), x.size, _p(out), new_fs, old_fs)
+    return out[:n].copy()

@@ -1,0 +1,219 @@
+"""Generate the golden fixtures in tests/golden/ from the reference itself.
+
+Runs the reference's own CPU primitives, compiled from the reference sources
+by `make -C oracle ref REF_DIR=...` into oracle/_ref/libugsdr_ref.so
+(oracle/ref_harness.cpp + project FFTW-API shim), and stores their outputs as
+small .npz fixtures.  Only this script needs the reference tree; the tests
+read the committed fixtures.
+
+    python tests/golden/make_golden.py [REF_DIR]
+"""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parents[1]
+sys.path.insert(0, str(ROOT))
+
+from ugsdr_gb300 import signals  # noqa: E402
+
+SIGNALS = {  # ugsdr::Signal value -> (name, count of ids)
+    0: ("gps_l1ca", 37),
+    2: ("gps_l5i", 32),
+    3: ("gps_l5q", 32),
+    4: ("glonass_l1of", 1),
+    6: ("galileo_e1b", 50),
+    7: ("galileo_e1c", 50),
+}
+
+
+def ref_lib(ref_dir: str) -> C.CDLL:
+    subprocess.run(["make", "-s", "-C", str(ROOT / "oracle"), "ref", f"REF_DIR={ref_dir}"], check=True)
+    lib = C.CDLL(str(ROOT / "oracle" / "_ref" / "libugsdr_ref.so"))
+    vp, sz, d, i = C.c_void_p, C.c_size_t, C.c_double, C.c_int
+    lib.ref_prn_code.argtypes = [i, i, vp, i]
+    lib.ref_repeat_upsample.argtypes = [vp, i, i, vp, sz]
+    lib.ref_table_mixer_f32.argtypes = [vp, sz, d, d, d]
+    lib.ref_table_mixer_f64.argtypes = [vp, sz, d, d, d]
+    lib.ref_dft_c2c_f32.argtypes = [vp, vp, sz, i]
+    lib.ref_dft_r2c_f32.argtypes = [vp, vp, sz]
+    lib.ref_prepare_code_spectrum_f32.argtypes = [vp, sz, vp]
+    lib.ref_filter_optimized_f32.argtypes = [vp, sz, vp]
+    lib.ref_abs_f32.argtypes = [vp, sz, vp]
+    lib.ref_reshape_sum_f32.argtypes = [vp, sz, sz, vp]
+    lib.ref_reshape_sum_f32.restype = i
+    lib.ref_max_index_f32.argtypes = [vp, sz, vp, vp]
+    lib.ref_mean_std_f32.argtypes = [vp, sz, vp, vp]
+    lib.ref_resample_c32.argtypes = [vp, sz, vp, sz, sz, sz]
+    lib.ref_resample_c32.restype = sz
+    lib.ref_correlate_f32.argtypes = [vp, vp, sz, vp]
+    lib.ref_acquire_f32.argtypes = [vp, sz, sz, sz, vp, d, d, d, d, d, i, i, vp, vp]
+    lib.ref_acquire_f64.argtypes = [vp, sz, sz, sz, vp, d, d, d, d, d, i, i, vp, vp]
+    return lib
+
+
+def p(a: np.ndarray) -> int:
+    return a.ctypes.data
+
+
+def codes(lib) -> dict[str, np.ndarray]:
+    out = {}
+    buf = np.zeros(20000, np.float32)
+    for sig, (name, count) in SIGNALS.items():
+        rows = []
+        for sv in range(count):
+            n = lib.ref_prn_code(sig, sv, p(buf), buf.size)
+            rows.append(buf[:n].copy())
+        arr = np.stack(rows)
+        assert set(np.unique(arr)) <= {-1.0, 1.0}
+        out[name] = np.packbits(arr < 0, axis=1)
+        out[name + "_len"] = np.array(arr.shape[1])
+    return out
+
+
+def unpack(fix, name: str) -> np.ndarray:
+    n = int(fix[name + "_len"])
+    bits = np.unpackbits(fix[name], axis=1)[:, :n]
+    return (1.0 - 2.0 * bits).astype(np.float32)
+
+
+def kats(lib, code_fix) -> dict[str, np.ndarray]:
+    rng = np.random.default_rng(7)
+    out = {}
+    ca = unpack(code_fix, "gps_l1ca")
+    glo = unpack(code_fix, "glonass_l1of")[0]
+    # mixer: several (fs, f, phase), float and double, n = 3000
+    x = (rng.normal(size=3000) + 1j * rng.normal(size=3000)).astype(np.complex64)
+    out["mix_in"] = x
+    mixes = [(4e6, 1234.5, 0.0), (4e6, -4500.0, 0.0), (4e6, 1.5e6, 1.0), (1e6, 0.5e6, 0.0), (50e6, -14.58e6, -2.5),
+             (4e6, 0.0, 0.3)]
+    out["mix_params"] = np.array(mixes)
+    for k, (fs, f, ph) in enumerate(mixes):
+        y = x.copy()
+        lib.ref_table_mixer_f32(p(y), y.size, fs, f, ph)
+        out[f"mix_out_{k}"] = y
+        y64 = x.astype(np.complex128)
+        lib.ref_table_mixer_f64(p(y64), y64.size, fs, f, ph)
+        out[f"mix_out64_{k}"] = y64
+    # ones mixed at fs/2 (basic_tests.cpp:321-357)
+    ones = np.ones(1000, np.complex64)
+    lib.ref_table_mixer_f32(p(ones), ones.size, 1e6, 0.5e6, 0.0)
+    out["mix_half"] = ones
+    # DFT KAT tone (basic_tests.cpp:482-505) and random c2c both directions
+    for n in (1000, 4000, 2046, 511):
+        v = (rng.normal(size=n) + 1j * rng.normal(size=n)).astype(np.complex64)
+        fwd = np.empty_like(v)
+        inv = np.empty_like(v)
+        lib.ref_dft_c2c_f32(p(v), p(fwd), n, 0)
+        lib.ref_dft_c2c_f32(p(v), p(inv), n, 1)
+        out[f"dft_in_{n}"] = v
+        out[f"dft_fwd_{n}"] = fwd
+        out[f"dft_inv_{n}"] = inv
+    # code spectra and matched filter: GLONASS KAT (basic_tests.cpp:368-383), C/A at 4000 samples
+    for name, code in (("glo", glo), ("ca4000", None)):
+        if code is None:
+            code = np.empty(4000, np.float32)
+            lib.ref_repeat_upsample(p(ca[0]), 1023, 1, p(code), 4000)
+        code = np.ascontiguousarray(code, np.float32)
+        spec = np.empty(code.size, np.complex64)
+        lib.ref_prepare_code_spectrum_f32(p(code), code.size, p(spec))
+        sig = code.astype(np.complex64)
+        lib.ref_filter_optimized_f32(p(sig), sig.size, p(spec))
+        out[f"mf_code_{name}"] = code
+        out[f"mf_spec_{name}"] = spec
+        out[f"mf_out_{name}"] = sig
+    # abs / reshape / max / mean-std / correlator
+    a = (rng.normal(size=10000) + 1j * rng.normal(size=10000)).astype(np.complex64)
+    ab = np.empty(a.size, np.float32)
+    lib.ref_abs_f32(p(a), a.size, p(ab))
+    out["abs_in"], out["abs_out"] = a, ab
+    rs = np.empty(1000, np.float32)
+    assert lib.ref_reshape_sum_f32(p(ab), ab.size, 1000, p(rs)) == 0
+    out["reshape_out"] = rs
+    assert lib.ref_reshape_sum_f32(p(ab), ab.size, 3000, p(rs)) != 0  # 10000 % 3000 != 0 throws
+    mv, mi = C.c_float(), C.c_size_t()
+    lib.ref_max_index_f32(p(ab), ab.size, C.byref(mv), C.byref(mi))
+    out["max_value"], out["max_index"] = np.array(mv.value, np.float32), np.array(mi.value)
+    m, s = C.c_float(), C.c_float()
+    lib.ref_mean_std_f32(p(ab), ab.size, C.byref(m), C.byref(s))
+    out["mean"], out["sigma"] = np.array(m.value, np.float32), np.array(s.value, np.float32)
+    sig = ca[0].astype(np.complex64)
+    cor = np.empty(1, np.complex64)
+    lib.ref_correlate_f32(p(sig), p(ca[0]), 1023, p(cor))
+    out["correlate_ca"] = cor
+    # upsampler ramp (basic_tests.cpp:764-850) and code upsampling
+    up = np.empty(50000, np.float32)
+    lib.ref_repeat_upsample(p(ca[3]), 1023, 1, p(up), 50000)
+    out["ups_ca3_50000"] = up
+    e1b = unpack(code_fix, "galileo_e1b")[0]
+    up2 = np.empty(200000, np.float32)
+    lib.ref_repeat_upsample(p(e1b), e1b.size, 1, p(up2), 200000)
+    out["ups_e1b0_200000"] = up2
+    up3 = np.empty(16000, np.float32)
+    lib.ref_repeat_upsample(p(ca[5]), 1023, 4, p(up3), 16000)
+    out["ups_ca5_rep4_16000"] = up3
+    # resampler: complex ramp 1000 samples at several rate pairs
+    ramp = (np.arange(1000) + 1j * np.arange(1000)[::-1]).astype(np.complex64)
+    out["resample_in"] = ramp
+    pairs = [(2, 3), (3, 2), (1023, 2000), (4, 4)]
+    out["resample_pairs"] = np.array(pairs)
+    for k, (nf, of) in enumerate(pairs):
+        n_out = lib.ref_resample_c32(p(ramp), ramp.size, None, 0, nf, of)
+        dst = np.empty(n_out, np.complex64)
+        lib.ref_resample_c32(p(ramp), ramp.size, p(dst), n_out, nf, of)
+        out[f"resample_out_{k}"] = dst
+    return out
+
+
+def acquisition(lib, code_fix) -> dict[str, np.ndarray]:
+    """Full-size GPS L1 C/A acquisition (int8 IQ, 4 MHz, 10 ms, 1 ms x 10 blocks,
+    +-5 kHz / 500 Hz) on a seeded synthetic capture, reference primitives in
+    float and double, for 8 PRNs (the 6 visible + 2 absent)."""
+    ca = unpack(code_fix, "gps_l1ca")
+    codes = {i: ca[i] for i in range(32)}
+    raw, truth = signals.gps_l1_config(seed=1, codes=codes)
+    iq = raw.astype(np.float32).reshape(-1)  # int8 -> float exactly (GetPartialSignal)
+    visible = [t["prn"] for t in truth]
+    absent = [p_ for p_ in range(32) if p_ not in visible][:2]
+    prns = visible + absent
+    recs, recs64, outs = [], [], []
+    fs, n, k = 4.0e6, 4000, 10
+    for prn in prns:
+        code = np.empty(n, np.float32)
+        lib.ref_repeat_upsample(p(ca[prn]), 1023, 1, p(code), n)
+        rec = np.zeros(7)
+        best = np.zeros(n, np.float32)
+        lib.ref_acquire_f32(p(iq), iq.size // 2, n, k, p(code), fs, 5000.0, 500.0, 0.0, 1.0, 0, 1, p(rec), p(best))
+        recs.append(rec)
+        outs.append(best)
+        iq64 = iq.astype(np.float64)
+        code64 = code.astype(np.float64)
+        rec64 = np.zeros(7)
+        lib.ref_acquire_f64(p(iq64), iq64.size // 2, n, k, p(code64), fs, 5000.0, 500.0, 0.0, 1.0, 0, 1, p(rec64), None)
+        recs64.append(rec64)
+    return dict(acq_raw=raw, acq_prns=np.array(prns), acq_visible=np.array(visible), acq_rec=np.array(recs),
+                acq_rec64=np.array(recs64), acq_best=np.array(outs),
+                acq_truth=np.array([[t["prn"], t["doppler"], t["code_phase_samples"], t["cn0"]] for t in truth]))
+
+
+def main() -> None:
+    ref_dir = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    lib = ref_lib(ref_dir)
+    c = codes(lib)
+    np.savez_compressed(HERE / "codes.npz", **c)
+    k = kats(lib, c)
+    np.savez_compressed(HERE / "kats.npz", **k)
+    a = acquisition(lib, c)
+    np.savez_compressed(HERE / "acq_gps_l1_4mhz.npz", **a)
+    for f in sorted(HERE.glob("*.npz")):
+        print(f.name, f.stat().st_size)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,119 @@
+"""Pins the CPU oracle (oracle/oracle.cpp) against the reference's own
+primitives: every golden vector in tests/golden/ was produced by the
+reference sources compiled into oracle/_ref (tests/golden/make_golden.py)."""
+import numpy as np
+import pytest
+
+from conftest import unpack_codes
+
+
+def test_table_mixer_bit_exact(oracle, kats):
+    x = kats["mix_in"]
+    for k, (fs, f, ph) in enumerate(kats["mix_params"]):
+        np.testing.assert_array_equal(oracle.table_mix(x, fs, f, ph), kats[f"mix_out_{k}"], err_msg=f"case {k}")
+        y64 = oracle.table_mix(x.astype(np.complex128), fs, f, ph)
+        np.testing.assert_array_equal(y64, kats[f"mix_out64_{k}"], err_msg=f"case {k} f64")
+
+
+def test_mixer_kat_half_rate(oracle, kats):
+    y = oracle.table_mix(np.ones(1000, np.complex64), 1e6, 0.5e6)
+    np.testing.assert_array_equal(y, kats["mix_half"])
+    # basic_tests.cpp:321-357: alternating +-1, imag ~ 0
+    np.testing.assert_array_equal(y.real, 1.0 - 2.0 * (np.arange(1000) & 1))
+    assert np.abs(y.imag).max() < 1e-6
+
+
+@pytest.mark.parametrize("n", [1000, 4000, 2046, 511])
+def test_dft(oracle, kats, n):
+    lib = oracle.load()
+    v = kats[f"dft_in_{n}"]
+    for inv, key in ((0, "fwd"), (1, "inv")):
+        out = np.empty_like(v)
+        lib.orc_dft_c2c_f32(v.ctypes.data, out.ctypes.data, n, inv)
+        ref = kats[f"dft_{key}_{n}"]
+        assert np.abs(out - ref).max() <= 1e-6 * np.abs(ref).max() + 1e-6
+
+
+def test_dft_tone_kat(oracle):
+    # basic_tests.cpp:482-505: 1000-point tone at 0.1 fs peaks at bin 100 with value N
+    lib = oracle.load()
+    n = 1000
+    x = np.exp(2j * np.pi * 0.1 * np.arange(n)).astype(np.complex64)
+    out = np.empty_like(x)
+    lib.orc_dft_c2c_f32(x.ctypes.data, out.ctypes.data, n, 0)
+    assert np.argmax(np.abs(out)) == 100
+    assert abs(abs(out[100]) - n) < 5e-3 * n
+
+
+@pytest.mark.parametrize("name", ["glo", "ca4000"])
+def test_matched_filter(oracle, kats, name):
+    lib = oracle.load()
+    code = kats[f"mf_code_{name}"]
+    spec = np.empty(code.size, np.complex64)
+    lib.orc_prepare_code_spectrum_f32(code.ctypes.data, code.size, 0, spec.ctypes.data)
+    ref_spec = kats[f"mf_spec_{name}"]
+    assert np.abs(spec - ref_spec).max() <= 1e-6 * np.abs(ref_spec).max()
+    sig = code.astype(np.complex64)
+    lib.orc_filter_optimized_f32(sig.ctypes.data, sig.size, spec.ctypes.data, 0)
+    ref = kats[f"mf_out_{name}"]
+    assert np.abs(sig - ref).max() <= 1e-5 * np.abs(ref).max()
+    if name == "glo":
+        # basic_tests.cpp:368-383
+        assert abs(sig[0].real - 511) < 5e-3
+        assert np.abs(sig[1:].real + 1).max() < 5e-3
+
+
+def test_reductions(oracle, kats):
+    lib = oracle.load()
+    a = kats["abs_in"]
+    ab = np.empty(a.size, np.float32)
+    lib.orc_abs_f32(a.ctypes.data, a.size, ab.ctypes.data)
+    np.testing.assert_allclose(ab, kats["abs_out"], rtol=2e-7)
+    r = kats["abs_out"].copy()
+    assert lib.orc_reshape_sum_f32(r.ctypes.data, r.size, 1000) == 0
+    np.testing.assert_array_equal(r[:1000], kats["reshape_out"])
+    assert lib.orc_reshape_sum_f32(r.ctypes.data, 10000, 3000) == -1
+    ab_ref = kats["abs_out"]
+    assert lib.orc_max_index_f32(ab_ref.ctypes.data, 10000) == int(kats["max_index"])
+    m, s = np.zeros(1, np.float32), np.zeros(1, np.float32)
+    lib.orc_mean_std_f32(ab_ref.ctypes.data, 10000, m.ctypes.data, s.ctypes.data)
+    assert m[0] == kats["mean"] and s[0] == kats["sigma"]
+
+
+def test_correlator_kat(oracle, kats, golden_codes):
+    ca = unpack_codes(golden_codes, "gps_l1ca")[0]
+    out = np.zeros(2, np.float32)
+    sig = ca.astype(np.complex64)
+    oracle.load().orc_correlate_f32(sig.ctypes.data, ca.ctypes.data, 1023, out.ctypes.data)
+    assert out[0] == 1023 and out[1] == 0  # basic_tests.cpp:72-86
+    assert complex(*out) == complex(kats["correlate_ca"][0])
+
+
+def test_upsampler(oracle, kats, golden_codes):
+    ca = unpack_codes(golden_codes, "gps_l1ca")
+    np.testing.assert_array_equal(oracle.upsample(ca[3], 50000), kats["ups_ca3_50000"])
+
+
+def test_resampler(oracle, kats):
+    x = kats["resample_in"]
+    for k, (nf, of) in enumerate(kats["resample_pairs"]):
+        out = oracle.resample(x, int(nf), int(of))
+        ref = kats[f"resample_out_{k}"]
+        assert out.shape == ref.shape
+        np.testing.assert_allclose(out, ref, rtol=1e-5, atol=1e-3)
+
+
+def test_acquisition_matches_reference(oracle, acq_golden, golden_codes):
+    ca = unpack_codes(golden_codes, "gps_l1ca")
+    iq = acq_golden["acq_raw"].astype(np.float32)
+    x = (iq[:, 0] + 1j * iq[:, 1]).astype(np.complex64)
+    for prn, rec, rec64 in zip(acq_golden["acq_prns"], acq_golden["acq_rec"], acq_golden["acq_rec64"]):
+        code = oracle.upsample(ca[prn], 4000)
+        r = oracle.acquire(x, 4000, 10, code, 4e6, 5000, 500)
+        # index and Doppler bin bit-exact against the reference's float path
+        assert r["index"] == rec[4] and r["doppler_bin"] == rec[5], prn
+        assert abs(r["level"] - rec[0]) <= 1e-4 * rec[0]
+        r64 = oracle.acquire(x, 4000, 10, code, 4e6, 5000, 500, double=True)
+        assert r64["index"] == rec64[4] and r64["doppler_bin"] == rec64[5]
+        assert abs(r64["level"] - rec64[0]) <= 1e-9 * rec64[0]
+        assert abs(r64["snr"] - rec64[6]) <= 1e-9 * rec64[6]

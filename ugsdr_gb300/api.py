@@ -1,0 +1,273 @@
+"""Python host layer over the C ABI.
+
+Mirrors the reference's policy vocabulary (ugsdr::Mixer<Impl>::Translate,
+MatchedFilter::PrepareCodeSpectrum / FilterOptimized, Abs, ReshapeAndSum,
+MaxIndex, MeanStdDev, Upsampler, Resampler, Correlator, Codegen) with numpy
+arrays in place of std::vector, and the batched FastSearchEngine entry
+(src/acquisition/fse.hpp:242-276) as `Context.acquire`.  Every call runs on
+the GPU through libugsdr_cuda.so; errors surface as UgsdrError the way the
+reference policies throw std::runtime_error.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib as L
+
+
+def _ptr(a: np.ndarray) -> int:
+    return a.ctypes.data
+
+
+class Context:
+    """One device context (stream, plan cache, code-spectrum cache, scratch)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = L.load()
+        h = C.c_void_p()
+        st = self.lib.ugsdr_ctx_create(device, C.byref(h))
+        if st != L.OK:
+            raise L.UgsdrError(st, f"ugsdr_ctx_create({device}) failed")
+        self.h = h
+        self._codes: dict[int, tuple] = {}
+
+    def close(self) -> None:
+        if self.h:
+            self.lib.ugsdr_ctx_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st: int) -> None:
+        L.check(st, self.h)
+
+    def set_stream(self, stream_ptr: int | None) -> None:
+        self._check(self.lib.ugsdr_ctx_set_stream(self.h, C.c_void_p(stream_ptr or 0)))
+
+    def synchronize(self) -> None:
+        self._check(self.lib.ugsdr_ctx_synchronize(self.h))
+
+    def launch_count(self) -> int:
+        n = C.c_uint64()
+        self._check(self.lib.ugsdr_ctx_launch_count(self.h, C.byref(n)))
+        return n.value
+
+    def enable_timing(self, on: bool = True) -> None:
+        self._check(self.lib.ugsdr_ctx_enable_timing(self.h, 1 if on else 0))
+
+    def reset_timing(self) -> None:
+        self._check(self.lib.ugsdr_ctx_reset_timing(self.h))
+
+    def kernel_time(self, kernel: str) -> tuple[int, float]:
+        """(launches, total ms) of `kernel` measured with CUDA events on its stream."""
+        n, ms = C.c_uint64(), C.c_double()
+        self._check(self.lib.ugsdr_ctx_kernel_time(self.h, kernel.encode(), C.byref(n), C.byref(ms)))
+        return n.value, ms.value
+
+    # -------------------------------------------------------------- codes
+    def code_put(self, chips: np.ndarray, samples: int, repeats: int = 1, spectrum_mode: int = L.SPECTRUM_ONE_SIDED,
+                 sign_mask: int = 0, sign_segment: int = 0) -> int:
+        chips = np.ascontiguousarray(chips, np.float32)
+        h = C.c_int()
+        self._check(self.lib.ugsdr_code_put(self.h, _ptr(chips), chips.size, repeats, samples, sign_mask, sign_segment,
+                                            spectrum_mode, C.byref(h)))
+        return h.value
+
+    def code_release(self, handle: int) -> None:
+        self._check(self.lib.ugsdr_code_release(self.h, handle))
+
+    # -------------------------------------------------------- acquisition
+    def make_job(self, samples, sample_type: int, fs: float, block_samples: int, n_blocks: int, codes,
+                 doppler_range: float, doppler_step: float, *, n_samples: int | None = None, on_device: bool = False,
+                 intermediate_frequency: float = 0.0, frontend_frequency: float = 0.0,
+                 code_offset_ratio: float = 1.0, fold_samples: int = 0,
+                 fold_coherent: bool = True, statistic: int = L.STAT_ABS,
+                 spectrum_mode: int = L.SPECTRUM_ONE_SIDED) -> "Job":
+        codes_arr = (C.c_int * len(codes))(*codes)
+        if on_device:
+            ptr = int(samples)
+            assert n_samples is not None
+        else:
+            arr = np.ascontiguousarray(samples)
+            ptr = _ptr(arr)
+            per = {L.SAMPLES_CF32: 8, L.SAMPLES_CI8: 2, L.SAMPLES_CI16: 4, L.SAMPLES_RI8: 1}[sample_type]
+            n_samples = arr.nbytes // per
+            samples = arr
+        job = L.AcqJob(ptr, sample_type, 1 if on_device else 0, n_samples, fs, intermediate_frequency, frontend_frequency,
+                       code_offset_ratio,
+                       block_samples, n_blocks, fold_samples, 1 if fold_coherent else 0, doppler_range, doppler_step,
+                       codes_arr, len(codes), statistic, spectrum_mode)
+        return Job(job, codes_arr, samples)
+
+    def acquire(self, job: "Job", cells: bool = False):
+        n = job.c.n_codes
+        res = (L.AcqResult * n)()
+        cell_arr = None
+        if cells:
+            nd = C.c_uint32()
+            self._check(self.lib.ugsdr_doppler_bins(job.c.doppler_range, job.c.doppler_step, C.byref(nd)))
+            cell_arr = (L.AcqCell * (n * nd.value))()
+        self._check(self.lib.ugsdr_acquire(self.h, C.byref(job.c), res, cell_arr))
+        out = [AcqResult.from_c(r) for r in res]
+        if cells:
+            c = np.frombuffer(cell_arr, dtype=np.dtype([("level", "<f4"), ("index", "<u4"), ("mean", "<f4"), ("std", "<f4")]))
+            return out, c.reshape(n, -1).copy()
+        return out
+
+    def acquire_batch(self, jobs: list["Job"]):
+        arr = (L.AcqJob * len(jobs))(*[j.c for j in jobs])
+        res = [(L.AcqResult * j.c.n_codes)() for j in jobs]
+        ptrs = (C.POINTER(L.AcqResult) * len(jobs))(*[C.cast(r, C.POINTER(L.AcqResult)) for r in res])
+        self._check(self.lib.ugsdr_acquire_batch(self.h, arr, len(jobs), ptrs))
+        return [[AcqResult.from_c(x) for x in r] for r in res]
+
+    # ------------------------------------------------------------ per-op
+    def mix(self, iq: np.ndarray, fs: float, frequency: float, phase: float = 0.0) -> np.ndarray:
+        """Mixer<TableMixer>::Translate(src_dst, fs, f, phase), in place (complex64)."""
+        assert iq.dtype == np.complex64 and iq.flags.c_contiguous
+        self._check(self.lib.ugsdr_mix(self.h, _ptr(iq), iq.size, fs, frequency, phase))
+        return iq
+
+    def dft(self, x: np.ndarray, inverse: bool = False) -> np.ndarray:
+        x = np.ascontiguousarray(x, np.complex64)
+        out = np.empty_like(x)
+        self._check(self.lib.ugsdr_dft(self.h, _ptr(x), _ptr(out), x.size, 1 if inverse else 0))
+        return out
+
+    def prepare_code_spectrum(self, code: np.ndarray, spectrum_mode: int = L.SPECTRUM_ONE_SIDED) -> np.ndarray:
+        code = np.ascontiguousarray(code, np.float32)
+        out = np.empty(code.size, np.complex64)
+        self._check(self.lib.ugsdr_matched_filter_prepare(self.h, _ptr(code), code.size, spectrum_mode, _ptr(out)))
+        return out
+
+    def filter_optimized(self, x: np.ndarray, spectrum: np.ndarray, spectrum_mode: int = L.SPECTRUM_ONE_SIDED) -> np.ndarray:
+        x = np.array(x, np.complex64, copy=True)
+        spectrum = np.ascontiguousarray(spectrum, np.complex64)
+        self._check(self.lib.ugsdr_matched_filter(self.h, _ptr(x), x.size, _ptr(spectrum), spectrum_mode))
+        return x
+
+    def abs(self, x: np.ndarray) -> np.ndarray:
+        x = np.ascontiguousarray(x, np.complex64)
+        out = np.empty(x.size, np.float32)
+        self._check(self.lib.ugsdr_abs(self.h, _ptr(x), x.size, _ptr(out)))
+        return out
+
+    def reshape_and_sum(self, x: np.ndarray, block: int) -> np.ndarray:
+        cplx = np.iscomplexobj(x)
+        x = np.ascontiguousarray(x, np.complex64 if cplx else np.float32)
+        out = np.empty(block, x.dtype)
+        self._check(self.lib.ugsdr_reshape_sum(self.h, _ptr(x), x.size, block, 1 if cplx else 0, _ptr(out)))
+        return out
+
+    def max_index(self, x: np.ndarray) -> tuple[float, int]:
+        x = np.ascontiguousarray(x, np.float32)
+        v, i = C.c_float(), C.c_size_t()
+        self._check(self.lib.ugsdr_max_index(self.h, _ptr(x), x.size, C.byref(v), C.byref(i)))
+        return v.value, i.value
+
+    def mean_stddev(self, x: np.ndarray) -> tuple[float, float]:
+        x = np.ascontiguousarray(x, np.float32)
+        m, s = C.c_float(), C.c_float()
+        self._check(self.lib.ugsdr_mean_stddev(self.h, _ptr(x) if x.size else None, x.size, C.byref(m), C.byref(s)))
+        return m.value, s.value
+
+    def upsample(self, x: np.ndarray, samples: int) -> np.ndarray:
+        cplx = np.iscomplexobj(x)
+        x = np.ascontiguousarray(x, np.complex64 if cplx else np.float32)
+        out = np.empty(samples, x.dtype)
+        self._check(self.lib.ugsdr_upsample(self.h, _ptr(x), x.size, 1 if cplx else 0, _ptr(out), samples))
+        return out
+
+    def resample(self, x: np.ndarray, new_fs: int, old_fs: int) -> np.ndarray:
+        x = np.ascontiguousarray(x, np.complex64)
+        n = C.c_size_t()
+        self._check(self.lib.ugsdr_resample(self.h, _ptr(x), x.size, new_fs, old_fs, None, 0, C.byref(n)))
+        out = np.empty(n.value, np.complex64)
+        self._check(self.lib.ugsdr_resample(self.h, _ptr(x), x.size, new_fs, old_fs, _ptr(out), out.size, C.byref(n)))
+        return out
+
+    def correlate(self, x: np.ndarray, code: np.ndarray) -> complex:
+        x = np.ascontiguousarray(x, np.complex64)
+        code = np.ascontiguousarray(code, np.float32)
+        if x.size != code.size:
+            raise L.UgsdrError(L.E_INVALID, "Size mismatch")
+        out = np.empty(1, np.complex64)
+        self._check(self.lib.ugsdr_correlate(self.h, _ptr(x), _ptr(code), x.size, _ptr(out)))
+        return complex(out[0])
+
+    def convert_samples(self, raw: np.ndarray, sample_type: int) -> np.ndarray:
+        raw = np.ascontiguousarray(raw)
+        per = {L.SAMPLES_CF32: 8, L.SAMPLES_CI8: 2, L.SAMPLES_CI16: 4, L.SAMPLES_RI8: 1}[sample_type]
+        n = raw.nbytes // per
+        out = np.empty(n, np.complex64)
+        self._check(self.lib.ugsdr_convert_samples(self.h, _ptr(raw), sample_type, n, _ptr(out)))
+        return out
+
+
+@dataclass
+class Job:
+    c: L.AcqJob
+    codes_arr: object
+    keep: object = field(repr=False, default=None)
+
+
+@dataclass
+class AcqResult:
+    code: int
+    doppler_bin: int
+    index: int
+    n_doppler: int
+    doppler: float
+    code_offset: float
+    level: float
+    sigma: float
+    mean: float
+    std: float
+    snr: float
+
+    @staticmethod
+    def from_c(r: L.AcqResult) -> "AcqResult":
+        return AcqResult(r.code, r.doppler_bin, r.index, r.n_doppler, r.doppler, r.code_offset, r.level, r.sigma, r.mean,
+                         r.std, r.snr)
+
+
+def prn_code(signal: int, sv: int) -> np.ndarray:
+    """Codegen<Impl>::Get<float>(sv): +-1 chips."""
+    lib = L.load()
+    n = C.c_size_t()
+    buf = np.empty(20000, np.float32)
+    st = lib.ugsdr_prn_code(signal, sv, _ptr(buf), buf.size, C.byref(n))
+    if st != L.OK:
+        raise L.UgsdrError(st, f"ugsdr_prn_code({signal}, {sv}) failed")
+    return buf[: n.value].copy()
+
+
+def repeat_upsample(chips: np.ndarray, repeats: int, samples: int) -> np.ndarray:
+    lib = L.load()
+    chips = np.ascontiguousarray(chips, np.float32)
+    out = np.empty(samples, np.float32)
+    st = lib.ugsdr_repeat_upsample(_ptr(chips), chips.size, repeats, _ptr(out), samples)
+    if st != L.OK:
+        raise L.UgsdrError(st, "ugsdr_repeat_upsample failed")
+    return out
+
+
+def doppler_bins(range_hz: float, step_hz: float) -> int:
+    n = C.c_uint32()
+    st = L.load().ugsdr_doppler_bins(range_hz, step_hz, C.byref(n))
+    if st != L.OK:
+        raise L.UgsdrError(st, "bad doppler grid")
+    return n.value

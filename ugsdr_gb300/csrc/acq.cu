@@ -1,0 +1,545 @@
+// Batched acquisition engine: FFT planning, code-spectrum cache, job launch.
+// Host side of the kernels in acq_kernels.cuh / acq_large.cuh; C entry points
+// ugsdr_code_put / ugsdr_code_release / ugsdr_acquire / ugsdr_acquire_batch.
+#include "internal.hpp"
+#include "acq_kernels.cuh"
+#include "acq_large.cuh"
+#include "fft_plan.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <functional>
+#include <vector>
+
+namespace ugsdr_gpu {
+
+	namespace {
+		constexpr int kThreads = 256;
+
+		void upload_twiddles(ugsdr_ctx* ctx, int n) {
+			if (ctx->twiddles.count(n))
+				return;
+			std::vector<float2> tw(n);
+			const double two_pi = 2.0 * 3.14159265358979323846;
+			for (int m = 0; m < n; ++m) {
+				const double a = two_pi * static_cast<double>(m) / static_cast<double>(n);
+				tw[m] = c2(static_cast<float>(std::cos(a)), static_cast<float>(-std::sin(a)));
+			}
+			auto buf = std::make_unique<DevBuf>();
+			buf->reserve(sizeof(float2) * n);
+			UG_CUDA(cudaMemcpy(buf->ptr, tw.data(), sizeof(float2) * n, cudaMemcpyHostToDevice));
+			ctx->twiddles[n] = std::move(buf);
+		}
+
+		FftPlanDev to_dev(const FftPlanDesc& d) {
+			FftPlanDev p{};
+			p.n = d.n;
+			p.n_pass = d.n_pass;
+			for (int i = 0; i < d.n_pass; ++i)
+				p.radix[i] = d.radix[i];
+			p.tw = d.tw;
+			return p;
+		}
+
+		template <typename K>
+		void set_smem(K kernel, size_t bytes) {
+			static std::mutex mu;
+			std::lock_guard<std::mutex> lock(mu);
+			UG_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes)));
+		}
+	}
+
+	void note_launch(ugsdr_ctx* ctx, int n) {
+		ctx->launches += n;
+		UG_CUDA(cudaGetLastError());
+	}
+
+	const FftPlanDesc& get_plan(ugsdr_ctx* ctx, int n) {
+		auto it = ctx->plans.find(n);
+		if (it != ctx->plans.end())
+			return it->second;
+		std::vector<int> r;
+		require(n >= 2 && plan_radices(n, r) && static_cast<int>(r.size()) <= kMaxPasses,
+			"FFT size " + std::to_string(n) + " has a prime factor above 31", UGSDR_E_UNSUPPORTED);
+		upload_twiddles(ctx, n);
+		FftPlanDesc d;
+		d.n = n;
+		d.n_pass = static_cast<int>(r.size());
+		for (size_t i = 0; i < r.size(); ++i)
+			d.radix[i] = r[i];
+		d.tw = ctx->twiddles[n]->as<float2>();
+		return ctx->plans[n] = d;
+	}
+
+	const float* get_lut(ugsdr_ctx* ctx) {
+		if (!ctx->lut.ptr) {
+			// TableMixer::GetSinCosTable<6, float> (table_mixer.hpp:31-47):
+			// 80 entries sin(i * 5 pi / 80 / 2), computed in double, stored as float
+			float t[80];
+			const double step = 5 * 3.14159265358979323846 / 80 / 2;
+			for (int i = 0; i < 80; ++i)
+				t[i] = static_cast<float>(std::sin(static_cast<double>(i) * step));
+			ctx->lut.reserve(sizeof(t));
+			UG_CUDA(cudaMemcpy(ctx->lut.ptr, t, sizeof(t), cudaMemcpyHostToDevice));
+		}
+		return ctx->lut.as<float>();
+	}
+
+	// Single-CTA path: ping-pong buffers (2 N complex) + accumulator (N floats)
+	bool fits_single_cta(ugsdr_ctx* ctx, int n) {
+		return static_cast<size_t>(n) * (2 * sizeof(float2) + sizeof(float)) + 1024 <= ctx->smem_optin;
+	}
+
+	// ------------------------------------------------------ large-N path
+	namespace {
+		constexpr int kLargeThreads = 512;
+
+		size_t large_tile_bytes(const LargePlan& lp, int cw, int rw) {
+			return 2 * sizeof(float2) * static_cast<size_t>(std::max(cw * lp.n1, rw * lp.n2));
+		}
+	}
+
+	const LargePlan& get_large_plan(ugsdr_ctx* ctx, int n) {
+		auto it = ctx->large_plans.find(n);
+		if (it != ctx->large_plans.end())
+			return it->second;
+		const size_t budget = ctx->smem_optin - 2048;
+		int best1 = 0;
+		std::vector<int> r;
+		for (int a = 2; static_cast<long>(a) * a <= n; ++a) {
+			if (n % a)
+				continue;
+			const int b = n / a;
+			if (!plan_radices(a, r) || !plan_radices(b, r))
+				continue;
+			// both tiles must fit with at least 4 columns / 1 row
+			if (2 * sizeof(float2) * 4 * static_cast<size_t>(a) > budget || 2 * sizeof(float2) * static_cast<size_t>(b) > budget)
+				continue;
+			best1 = a;  // increasing a -> closest to sqrt(n) last
+		}
+		require(best1 > 0, "no four-step split for FFT size " + std::to_string(n), UGSDR_E_UNSUPPORTED);
+		LargePlan lp;
+		lp.n = n;
+		lp.n1 = best1;
+		lp.n2 = n / best1;
+		lp.p1 = get_plan(ctx, lp.n1);
+		lp.p2 = get_plan(ctx, lp.n2);
+		upload_twiddles(ctx, n);
+		lp.tw = ctx->twiddles[n]->as<float2>();
+		return ctx->large_plans[n] = lp;
+	}
+
+	namespace {
+		void tile_shape(ugsdr_ctx* ctx, const LargePlan& lp, int& cw, int& rw) {
+			const size_t budget = ctx->smem_optin - 2048;
+			cw = 16;
+			while (cw > 4 && 2 * sizeof(float2) * cw * static_cast<size_t>(lp.n1) > budget)
+				cw /= 2;
+			rw = 16;
+			while (rw > 1 && 2 * sizeof(float2) * rw * static_cast<size_t>(lp.n2) > budget)
+				rw /= 2;
+		}
+
+		LargeParams large_params(ugsdr_ctx* ctx, const AcqParams& base, int n, size_t& smem) {
+			const LargePlan& lp = get_large_plan(ctx, n);
+			LargeParams p{};
+			p.base = base;
+			p.p1 = to_dev(lp.p1);
+			p.p2 = to_dev(lp.p2);
+			p.n1 = lp.n1;
+			p.n2 = lp.n2;
+			tile_shape(ctx, lp, p.cw, p.rw);
+			p.tw = lp.tw;
+			smem = large_tile_bytes(lp, p.cw, p.rw);
+			return p;
+		}
+
+		template <typename K>
+		int resident_grid(ugsdr_ctx* ctx, K kernel, int threads, size_t smem) {
+			int per_sm = 0;
+			UG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem));
+			return std::max(1, per_sm) * ctx->sm_count;
+		}
+
+		size_t slab_elems(int n, int m) { return static_cast<size_t>(n) + (m + 1) / 2 + m; }
+	}
+
+	size_t large_slab_bytes(ugsdr_ctx* ctx, int n, int m) {
+		size_t smem = 0;
+		AcqParams base{};
+		base.n = n;
+		LargeParams p = large_params(ctx, base, n, smem);
+		set_smem(acq_inverse_large_kernel, smem);
+		const int grid = resident_grid(ctx, acq_inverse_large_kernel, kLargeThreads, smem);
+		(void)p;
+		return sizeof(float2) * slab_elems(n, m) * grid;
+	}
+
+	void large_code_spectrum(ugsdr_ctx* ctx, CodeEntry& e, const float* chips_dev, size_t n_chips, size_t repeats,
+		uint32_t sign_mask, size_t sign_segment) {
+		AcqParams base{};
+		base.n = static_cast<int>(e.n);
+		base.one_sided = e.spectrum_mode == UGSDR_SPECTRUM_ONE_SIDED;
+		size_t smem = 0;
+		LargeParams p = large_params(ctx, base, base.n, smem);
+		p.chips = chips_dev;
+		p.n_chips = static_cast<int>(n_chips);
+		p.repeats = static_cast<int>(repeats);
+		p.sign_mask = sign_mask;
+		p.sign_segment = static_cast<int>(sign_segment);
+		p.code_out = e.spectrum.as<float2>();
+		set_smem(code_spectrum_large_kernel, smem);
+		code_spectrum_large_kernel<<<1, kLargeThreads, smem, ctx->stream>>>(p);
+		note_launch(ctx);
+	}
+
+	void large_job(ugsdr_ctx* ctx, const ugsdr_acq_job& job, const AcqParams& base, int n, float2* slab) {
+		size_t smem = 0;
+		LargeParams p = large_params(ctx, base, n, smem);
+		const int items = base.n_doppler * base.k_blocks;
+		auto launch_fwd = [&](auto kernel) {
+			set_smem(kernel, smem);
+			const int grid = std::min(items, resident_grid(ctx, kernel, kLargeThreads, smem));
+			KernelTimer timer(ctx, "acq_forward_large");
+			kernel<<<grid, kLargeThreads, smem, ctx->stream>>>(p);
+		};
+		switch (job.sample_type) {
+		case UGSDR_SAMPLES_CF32: launch_fwd(acq_forward_large_kernel<UGSDR_SAMPLES_CF32>); break;
+		case UGSDR_SAMPLES_CI8: launch_fwd(acq_forward_large_kernel<UGSDR_SAMPLES_CI8>); break;
+		case UGSDR_SAMPLES_CI16: launch_fwd(acq_forward_large_kernel<UGSDR_SAMPLES_CI16>); break;
+		default: launch_fwd(acq_forward_large_kernel<UGSDR_SAMPLES_RI8>); break;
+		}
+		note_launch(ctx);
+		p.slab = slab;
+		p.slab_elems = slab_elems(n, base.m);
+		set_smem(acq_inverse_large_kernel, smem);
+		const int rows = base.n_doppler * base.n_codes;
+		const int grid = std::min(rows, resident_grid(ctx, acq_inverse_large_kernel, kLargeThreads, smem));
+		KernelTimer timer(ctx, "acq_inverse_large");
+		acq_inverse_large_kernel<<<grid, kLargeThreads, smem, ctx->stream>>>(p);
+		note_launch(ctx);
+	}
+
+	namespace {
+		void build_code_spectrum(ugsdr_ctx* ctx, CodeEntry& e, const float* chips_host, size_t n_chips, size_t repeats,
+			uint32_t sign_mask, size_t sign_segment) {
+			const int n = static_cast<int>(e.n);
+			DevBuf chips;
+			chips.reserve(sizeof(float) * n_chips);
+			UG_CUDA(cudaMemcpyAsync(chips.ptr, chips_host, sizeof(float) * n_chips, cudaMemcpyHostToDevice, ctx->stream));
+			e.spectrum.reserve(sizeof(float2) * n);
+			if (!e.large) {
+				CodeSpecParams p{};
+				p.chips = chips.as<float>();
+				p.n_chips = static_cast<int>(n_chips);
+				p.repeats = static_cast<int>(repeats);
+				p.sign_mask = sign_mask;
+				p.sign_segment = static_cast<int>(sign_segment);
+				p.one_sided = e.spectrum_mode == UGSDR_SPECTRUM_ONE_SIDED;
+				p.out = e.spectrum.as<float2>();
+				p.plan = to_dev(get_plan(ctx, n));
+				const size_t smem = 2 * sizeof(float2) * n;
+				set_smem(code_spectrum_kernel, smem);
+				code_spectrum_kernel<<<1, kThreads, smem, ctx->stream>>>(p);
+				note_launch(ctx);
+			}
+			else {
+				large_code_spectrum(ctx, e, chips.as<float>(), n_chips, repeats, sign_mask, sign_segment);
+			}
+			UG_CUDA(cudaStreamSynchronize(ctx->stream));
+		}
+	}
+
+	// --------------------------------------------------------------- jobs
+	struct JobLaunch {
+		std::vector<double> grid;
+		std::vector<uint32_t> adders;
+		int n = 0, k = 0, m = 0, n_codes = 0, fold_mode = 0;
+		bool large = false;
+	};
+
+	namespace {
+		JobLaunch validate(ugsdr_ctx* ctx, const ugsdr_acq_job& job) {
+			JobLaunch L;
+			require(job.samples != nullptr, "null samples");
+			require(job.sample_type >= 0 && job.sample_type <= 3, "unknown sample type");
+			require(job.block_samples >= 2 && job.block_samples <= (1u << 24), "block size out of range");
+			require(job.n_blocks >= 1, "n_blocks must be >= 1");
+			require(job.n_samples >= job.block_samples * job.n_blocks, "not enough samples for n_blocks blocks");
+			require(job.sampling_rate > 0, "sampling rate must be positive");
+			require(job.codes != nullptr && job.n_codes >= 1, "no codes");
+			require(job.statistic == UGSDR_STAT_ABS || job.statistic == UGSDR_STAT_ABS2, "unknown statistic");
+			L.n = static_cast<int>(job.block_samples);
+			L.k = static_cast<int>(job.n_blocks);
+			L.n_codes = job.n_codes;
+			if (job.fold_samples) {
+				// ReshapeAndSum::CheckBlockSize (reshape_and_sum.hpp:15-18)
+				require(job.block_samples % job.fold_samples == 0, "Signal size is not divided by block size");
+				L.m = static_cast<int>(job.fold_samples);
+				L.fold_mode = job.fold_coherent ? 1 : 2;
+			}
+			else {
+				L.m = L.n;
+				L.fold_mode = 0;
+			}
+			L.grid = doppler_grid(job.doppler_range, job.doppler_step);
+			for (double d : L.grid)
+				L.adders.push_back(nco_adder(job.sampling_rate, -d));  // Translate(signal, fs, -doppler)
+			for (int c = 0; c < job.n_codes; ++c) {
+				auto it = ctx->codes.find(job.codes[c]);
+				require(it != ctx->codes.end(), "unknown code handle " + std::to_string(job.codes[c]), UGSDR_E_NOT_FOUND);
+				require(it->second->n == job.block_samples, "code length differs from block_samples");
+				require(it->second->spectrum_mode == job.spectrum_mode, "code spectrum mode differs from the job's");
+			}
+			L.large = !fits_single_cta(ctx, L.n);
+			return L;
+		}
+
+		size_t sample_bytes(int type) {
+			switch (type) {
+			case UGSDR_SAMPLES_CF32: return 8;
+			case UGSDR_SAMPLES_CI8: return 2;
+			case UGSDR_SAMPLES_CI16: return 4;
+			default: return 1;
+			}
+		}
+	}
+
+	// Launches one job on ctx->stream; cells/best_bin stay on the device.
+	void launch_job(ugsdr_ctx* ctx, const ugsdr_acq_job& job, const JobLaunch& L, const void* dev_samples,
+		AcqCellDev* cells, int* best_bin, uint32_t* adders_dev, const float2** code_ptrs_dev, float2* spectra,
+		float2* slab) {
+		AcqParams p{};
+		p.samples = dev_samples;
+		p.n = L.n;
+		p.k_blocks = L.k;
+		p.n_doppler = static_cast<int>(L.grid.size());
+		p.n_codes = L.n_codes;
+		p.m = L.m;
+		p.fold_mode = L.fold_mode;
+		p.stat = job.statistic;
+		p.one_sided = job.spectrum_mode == UGSDR_SPECTRUM_ONE_SIDED;
+		p.adders = adders_dev;
+		p.phase0 = 0;
+		// const Translate (mixer.hpp:44-51) has no zero-frequency shortcut, but a
+		// zero adder multiplies by table[16] + i table[0] = 1 + 0i: skipping is equal
+		p.fe_on = job.frontend_frequency != 0.0;
+		p.fe_adder = p.fe_on ? nco_adder(job.sampling_rate, job.frontend_frequency) : 0u;
+		p.lut = get_lut(ctx);
+		p.spectra = spectra;
+		p.codes = code_ptrs_dev;
+		p.cells = cells;
+		if (!L.large) {
+			p.plan = to_dev(get_plan(ctx, L.n));
+			const size_t smem_f = 2 * sizeof(float2) * L.n;
+			const int grid_f = p.n_doppler * L.k;
+			{
+			KernelTimer timer(ctx, "acq_forward");
+			switch (job.sample_type) {
+			case UGSDR_SAMPLES_CF32:
+				set_smem(acq_forward_kernel<UGSDR_SAMPLES_CF32>, smem_f);
+				acq_forward_kernel<UGSDR_SAMPLES_CF32><<<grid_f, kThreads, smem_f, ctx->stream>>>(p);
+				break;
+			case UGSDR_SAMPLES_CI8:
+				set_smem(acq_forward_kernel<UGSDR_SAMPLES_CI8>, smem_f);
+				acq_forward_kernel<UGSDR_SAMPLES_CI8><<<grid_f, kThreads, smem_f, ctx->stream>>>(p);
+				break;
+			case UGSDR_SAMPLES_CI16:
+				set_smem(acq_forward_kernel<UGSDR_SAMPLES_CI16>, smem_f);
+				acq_forward_kernel<UGSDR_SAMPLES_CI16><<<grid_f, kThreads, smem_f, ctx->stream>>>(p);
+				break;
+			default:
+				set_smem(acq_forward_kernel<UGSDR_SAMPLES_RI8>, smem_f);
+				acq_forward_kernel<UGSDR_SAMPLES_RI8><<<grid_f, kThreads, smem_f, ctx->stream>>>(p);
+				break;
+			}
+			}
+			note_launch(ctx);
+			const size_t smem_i = 2 * sizeof(float2) * L.n + sizeof(float) * L.m;
+			set_smem(acq_inverse_kernel, smem_i);
+			KernelTimer timer(ctx, "acq_inverse");
+			acq_inverse_kernel<<<p.n_doppler * L.n_codes, kThreads, smem_i, ctx->stream>>>(p);
+			note_launch(ctx);
+		}
+		else {
+			large_job(ctx, job, p, L.n, slab);
+		}
+		acq_select_kernel<<<(L.n_codes + 127) / 128, 128, 0, ctx->stream>>>(cells, L.n_codes, p.n_doppler, best_bin);
+		note_launch(ctx);
+	}
+
+	size_t spectra_bytes(const JobLaunch& L) {
+		return sizeof(float2) * static_cast<size_t>(L.n) * L.k * L.grid.size();
+	}
+
+	void run_jobs(ugsdr_ctx* ctx, const ugsdr_acq_job* jobs, int n_jobs, ugsdr_acq_result* const* results,
+		ugsdr_acq_cell* cells_out) {
+		require(jobs != nullptr && n_jobs >= 1, "no jobs");
+		std::vector<JobLaunch> launches;
+		size_t samples_bytes = 0, spectra_b = 0, cells_n = 0, params_b = 0, slab_b = 0;
+		for (int j = 0; j < n_jobs; ++j) {
+			launches.push_back(validate(ctx, jobs[j]));
+			const auto& L = launches.back();
+			if (!jobs[j].samples_on_device)
+				samples_bytes += (sample_bytes(jobs[j].sample_type) * jobs[j].n_samples + 255) / 256 * 256;
+			spectra_b = std::max(spectra_b, spectra_bytes(L));
+			cells_n += static_cast<size_t>(L.n_codes) * L.grid.size();
+			params_b += (L.grid.size() * sizeof(uint32_t) + L.n_codes * sizeof(void*) + L.n_codes * sizeof(int) + 512) / 256 * 256;
+			if (L.large)
+				slab_b = std::max(slab_b, large_slab_bytes(ctx, L.n, L.m));
+		}
+		ctx->samples.reserve(std::max<size_t>(samples_bytes, 256));
+		ctx->spectra.reserve(spectra_b);
+		ctx->cells.reserve(sizeof(AcqCellDev) * cells_n);
+		ctx->params.reserve(params_b);
+		if (slab_b)
+			ctx->slab.reserve(slab_b);
+
+		// stage parameters and host samples
+		std::vector<char> host_params(params_b);
+		size_t s_off = 0, p_off = 0, c_off = 0;
+		std::vector<const void*> dev_samples(n_jobs);
+		std::map<std::pair<const void*, size_t>, const void*> staged;  // one upload per host buffer
+		std::vector<size_t> p_offsets(n_jobs), c_offsets(n_jobs);
+		for (int j = 0; j < n_jobs; ++j) {
+			const auto& job = jobs[j];
+			const auto& L = launches[j];
+			if (job.samples_on_device) {
+				dev_samples[j] = job.samples;
+			}
+			else {
+				const size_t bytes = sample_bytes(job.sample_type) * job.n_samples;
+				auto key = std::make_pair(job.samples, bytes);
+				auto it = staged.find(key);
+				if (it != staged.end()) {
+					dev_samples[j] = it->second;
+				}
+				else {
+					char* dst = ctx->samples.as<char>() + s_off;
+					UG_CUDA(cudaMemcpyAsync(dst, job.samples, bytes, cudaMemcpyHostToDevice, ctx->stream));
+					dev_samples[j] = dst;
+					staged[key] = dst;
+					s_off += (bytes + 255) / 256 * 256;
+				}
+			}
+			p_offsets[j] = p_off;
+			char* hp = host_params.data() + p_off;
+			std::memcpy(hp, L.adders.data(), L.adders.size() * sizeof(uint32_t));
+			size_t o = (L.adders.size() * sizeof(uint32_t) + 15) / 16 * 16;
+			for (int c = 0; c < L.n_codes; ++c) {
+				const float2* ptr = ctx->codes[job.codes[c]]->spectrum.as<float2>();
+				std::memcpy(hp + o + c * sizeof(void*), &ptr, sizeof(void*));
+			}
+			o += L.n_codes * sizeof(void*);
+			o = (o + 15) / 16 * 16;
+			p_off += (L.grid.size() * sizeof(uint32_t) + L.n_codes * sizeof(void*) + L.n_codes * sizeof(int) + 512) / 256 * 256;
+			c_offsets[j] = c_off;
+			c_off += static_cast<size_t>(L.n_codes) * L.grid.size();
+		}
+		UG_CUDA(cudaMemcpyAsync(ctx->params.ptr, host_params.data(), params_b, cudaMemcpyHostToDevice, ctx->stream));
+
+		for (int j = 0; j < n_jobs; ++j) {
+			const auto& L = launches[j];
+			char* dp = ctx->params.as<char>() + p_offsets[j];
+			auto* adders = reinterpret_cast<uint32_t*>(dp);
+			size_t o = (L.adders.size() * sizeof(uint32_t) + 15) / 16 * 16;
+			auto* code_ptrs = reinterpret_cast<const float2**>(dp + o);
+			o += L.n_codes * sizeof(void*);
+			o = (o + 15) / 16 * 16;
+			auto* best = reinterpret_cast<int*>(dp + o);
+			launch_job(ctx, jobs[j], L, dev_samples[j], ctx->cells.as<AcqCellDev>() + c_offsets[j], best, adders,
+				code_ptrs, ctx->spectra.as<float2>(), ctx->slab.as<float2>());
+		}
+
+		// gather
+		std::vector<AcqCellDev> cells(c_off);
+		UG_CUDA(cudaMemcpyAsync(cells.data(), ctx->cells.ptr, sizeof(AcqCellDev) * c_off, cudaMemcpyDeviceToHost, ctx->stream));
+		UG_CUDA(cudaStreamSynchronize(ctx->stream));
+		for (int j = 0; j < n_jobs; ++j) {
+			const auto& job = jobs[j];
+			const auto& L = launches[j];
+			const size_t nd = L.grid.size();
+			for (int c = 0; c < L.n_codes; ++c) {
+				const AcqCellDev* row = cells.data() + c_offsets[j] + static_cast<size_t>(c) * nd;
+				// first strictly greater level wins (fse.hpp:265), recomputed on the host
+				size_t bd = 0;
+				for (size_t d = 1; d < nd; ++d)
+					if (row[bd].level < row[d].level)
+						bd = d;
+				ugsdr_acq_result& r = results[j][c];
+				r.code = job.codes[c];
+				r.doppler_bin = static_cast<int>(bd);
+				r.index = row[bd].index;
+				r.n_doppler = static_cast<uint32_t>(nd);
+				r.doppler = L.grid[bd] + job.intermediate_frequency;
+				r.code_offset = job.code_offset_ratio * static_cast<double>(row[bd].index);
+				r.level = row[bd].level;
+				r.mean = row[bd].mean;
+				r.std = row[bd].std;
+				r.sigma = static_cast<double>(row[bd].std + row[bd].mean);
+				r.snr = r.level / r.sigma;
+			}
+			if (cells_out && n_jobs == 1)
+				std::memcpy(cells_out, cells.data(), sizeof(AcqCellDev) * c_off);
+		}
+	}
+}
+
+using namespace ugsdr_gpu;
+
+extern "C" {
+
+int ugsdr_code_put(ugsdr_ctx* ctx, const float* chips, size_t n_chips, size_t repeats, size_t samples,
+	uint32_t sign_mask, size_t sign_segment, int spectrum_mode, int* handle) {
+	if (!ctx)
+		return UGSDR_E_INVALID;
+	std::lock_guard<std::mutex> lock(ctx->mutex);
+	return guarded(ctx, [&] {
+		require(chips && handle && n_chips > 0 && repeats > 0, "null chips/handle or empty code");
+		require(samples >= 2 && samples <= (1u << 24), "code samples out of range");
+		require(spectrum_mode == UGSDR_SPECTRUM_ONE_SIDED || spectrum_mode == UGSDR_SPECTRUM_TWO_SIDED, "bad spectrum mode");
+		auto e = std::make_unique<CodeEntry>();
+		e->n = samples;
+		e->spectrum_mode = spectrum_mode;
+		e->large = !fits_single_cta(ctx, static_cast<int>(samples));
+		build_code_spectrum(ctx, *e, chips, n_chips, repeats, sign_mask, sign_segment);
+		const int h = ctx->next_code++;
+		ctx->codes[h] = std::move(e);
+		*handle = h;
+	});
+}
+
+int ugsdr_code_release(ugsdr_ctx* ctx, int handle) {
+	if (!ctx)
+		return UGSDR_E_INVALID;
+	std::lock_guard<std::mutex> lock(ctx->mutex);
+	return guarded(ctx, [&] {
+		auto it = ctx->codes.find(handle);
+		require(it != ctx->codes.end(), "unknown code handle", UGSDR_E_NOT_FOUND);
+		UG_CUDA(cudaStreamSynchronize(ctx->stream));
+		ctx->codes.erase(it);
+	});
+}
+
+int ugsdr_acquire(ugsdr_ctx* ctx, const ugsdr_acq_job* job, ugsdr_acq_result* results, ugsdr_acq_cell* cells) {
+	if (!ctx)
+		return UGSDR_E_INVALID;
+	std::lock_guard<std::mutex> lock(ctx->mutex);
+	return guarded(ctx, [&] {
+		require(job && results, "null job/results");
+		ugsdr_acq_result* const rs[1] = {results};
+		run_jobs(ctx, job, 1, rs, cells);
+	});
+}
+
+int ugsdr_acquire_batch(ugsdr_ctx* ctx, const ugsdr_acq_job* jobs, int n_jobs, ugsdr_acq_result* const* results) {
+	if (!ctx)
+		return UGSDR_E_INVALID;
+	std::lock_guard<std::mutex> lock(ctx->mutex);
+	return guarded(ctx, [&] {
+		require(results != nullptr, "null results");
+		run_jobs(ctx, jobs, n_jobs, results, nullptr);
+	});
+}
+}

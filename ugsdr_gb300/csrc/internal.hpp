@@ -1,0 +1,188 @@
+// Host-side internals shared by the translation units of libugsdr_cuda.so.
+#pragma once
+
+#include "../../include/ugsdr_cuda.h"
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdint>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace ugsdr_gpu {
+
+	// Thrown inside the library, converted to a status at the C boundary.
+	struct Error : std::runtime_error {
+		int status;
+		Error(int s, const std::string& msg) : std::runtime_error(msg), status(s) {}
+	};
+
+	inline void check_cuda(cudaError_t e, const char* what) {
+		if (e != cudaSuccess)
+			throw Error(UGSDR_E_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+	}
+#define UG_CUDA(call) ::ugsdr_gpu::check_cuda((call), #call)
+
+	inline void require(bool cond, const std::string& msg, int status = UGSDR_E_INVALID) {
+		if (!cond)
+			throw Error(status, msg);
+	}
+
+	// Device buffer that only grows (scratch reused across calls).
+	struct DevBuf {
+		void* ptr = nullptr;
+		size_t bytes = 0;
+		void reserve(size_t n) {
+			if (n <= bytes)
+				return;
+			if (ptr)
+				cudaFree(ptr);
+			ptr = nullptr;
+			bytes = 0;
+			if (cudaMalloc(&ptr, n) != cudaSuccess) {
+				cudaGetLastError();
+				throw Error(UGSDR_E_NOMEM, "device allocation of " + std::to_string(n) + " bytes failed");
+			}
+			bytes = n;
+		}
+		template <typename T>
+		T* as() const { return static_cast<T*>(ptr); }
+		~DevBuf() {
+			if (ptr)
+				cudaFree(ptr);
+		}
+		DevBuf() = default;
+		DevBuf(const DevBuf&) = delete;
+		DevBuf& operator=(const DevBuf&) = delete;
+	};
+
+	// FFT plan for one size: radix sequence and the device twiddle table
+	// W_N^m = exp(-2 pi i m/N), m < N (double-precision angles, rounded to float).
+	constexpr int kMaxPasses = 12;
+	struct FftPlanDesc {
+		int n = 0;
+		int n_pass = 0;
+		int radix[kMaxPasses] = {};
+		const float2* tw = nullptr;
+	};
+
+	// Four-step split N = N1 * N2 for sizes above the single-CTA limit.
+	struct LargePlan {
+		int n = 0;
+		int n1 = 0, n2 = 0;
+		FftPlanDesc p1, p2;    // N1-point and N2-point plans
+		const float2* tw = nullptr;  // N-point table for the inter-step twiddle
+	};
+
+	struct CodeEntry {
+		size_t n = 0;
+		int spectrum_mode = 0;
+		bool large = false;           // stored in the four-step (k1-major) layout
+		DevBuf spectrum;              // N complex
+	};
+
+	struct Plans;  // fft planning (acq.cu)
+}
+
+struct ugsdr_ctx {
+	int device = 0;
+	cudaStream_t own_stream = nullptr;
+	cudaStream_t stream = nullptr;
+	std::string last_error;
+	std::atomic<uint64_t> launches{0};
+	std::mutex mutex;
+
+	// twiddle tables and plans per size
+	std::map<int, std::unique_ptr<ugsdr_gpu::DevBuf>> twiddles;
+	std::map<int, ugsdr_gpu::FftPlanDesc> plans;
+	std::map<int, ugsdr_gpu::LargePlan> large_plans;
+
+	// code spectra
+	std::map<int, std::unique_ptr<ugsdr_gpu::CodeEntry>> codes;
+	int next_code = 1;
+
+	// scratch
+	ugsdr_gpu::DevBuf lut;        // float[80] TableMixer sine table
+	ugsdr_gpu::DevBuf samples;    // staged input samples
+	ugsdr_gpu::DevBuf spectra;    // forward spectra X[d][b][N]
+	ugsdr_gpu::DevBuf slab;       // per-CTA four-step slabs
+	ugsdr_gpu::DevBuf cells;      // per (code, doppler) records
+	ugsdr_gpu::DevBuf results;    // per code results
+	ugsdr_gpu::DevBuf params;     // small per-job parameter arrays
+	ugsdr_gpu::DevBuf op_a, op_b, op_c;  // per-op entry staging
+	int sm_count = 0;
+	size_t smem_optin = 0;
+
+	// per-kernel event timing (ugsdr_ctx_enable_timing)
+	bool timing = false;
+	struct TimedLaunch {
+		std::string name;
+		cudaEvent_t start, stop;
+	};
+	std::vector<TimedLaunch> timed;
+	std::map<std::string, std::pair<uint64_t, double>> kernel_totals;
+};
+
+namespace ugsdr_gpu {
+	// Records a start/stop event pair around the launches in its scope when
+	// the context has timing enabled.
+	struct KernelTimer {
+		ugsdr_ctx* ctx;
+		ugsdr_ctx::TimedLaunch t{};
+		bool on;
+		KernelTimer(ugsdr_ctx* c, const char* name) : ctx(c), on(c->timing) {
+			if (!on)
+				return;
+			t.name = name;
+			cudaEventCreate(&t.start);
+			cudaEventCreate(&t.stop);
+			cudaEventRecord(t.start, ctx->stream);
+		}
+		~KernelTimer() {
+			if (!on)
+				return;
+			cudaEventRecord(t.stop, ctx->stream);
+			ctx->timed.push_back(t);
+		}
+	};
+}
+
+namespace ugsdr_gpu {
+	// status wrapper used by every C entry point
+	template <typename F>
+	int guarded(ugsdr_ctx* ctx, F&& f) {
+		try {
+			f();
+			return UGSDR_OK;
+		}
+		catch (const Error& e) {
+			if (ctx)
+				ctx->last_error = e.what();
+			return e.status;
+		}
+		catch (const std::exception& e) {
+			if (ctx)
+				ctx->last_error = e.what();
+			return UGSDR_E_INVALID;
+		}
+	}
+
+	// plan accessors (acq.cu)
+	const FftPlanDesc& get_plan(ugsdr_ctx* ctx, int n);
+	const LargePlan& get_large_plan(ugsdr_ctx* ctx, int n);
+	bool fits_single_cta(ugsdr_ctx* ctx, int n);
+	const float* get_lut(ugsdr_ctx* ctx);
+	void note_launch(ugsdr_ctx* ctx, int n = 1);
+
+	// shared host helpers (codes.cpp)
+	int prn_code(int signal, int sv, float* out, size_t cap, size_t* len);
+	// TableMixer adder for Translate(signal, fs, f): f < 0 -> fs + f (mixer.hpp:46-47)
+	uint32_t nco_adder(double fs, double f);
+	uint32_t nco_phase(double phase);
+	std::vector<double> doppler_grid(double range, double step);
+}

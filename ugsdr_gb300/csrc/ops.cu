@@ -1,0 +1,567 @@
+// Per-op entry points: one C function per reference policy so that each
+// Cuda* adapter (include/ugsdr_cuda_policies.hpp) is a drop-in for the
+// Sequential*/Ipp*/Af* implementation it replaces.  Host buffers in and out;
+// every call stages through the context's device scratch on its stream.
+#include "internal.hpp"
+#include "acq_kernels.cuh"
+#include "acq_large.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+
+namespace ugsdr_gpu {
+	namespace {
+		constexpr int kT = 256;
+
+		int blocks_for(size_t n, int per = kT) {
+			return static_cast<int>(std::min<size_t>((n + per - 1) / per, 152 * 32));
+		}
+
+		FftPlanDev dev_plan(const FftPlanDesc& d) {
+			FftPlanDev p{};
+			p.n = d.n;
+			p.n_pass = d.n_pass;
+			for (int i = 0; i < d.n_pass; ++i)
+				p.radix[i] = d.radix[i];
+			p.tw = d.tw;
+			return p;
+		}
+
+		template <typename K>
+		void smem_attr(K kernel, size_t bytes) {
+			UG_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes)));
+		}
+
+		// ------------------------------------------------------- kernels
+		__global__ void mix_kernel(float2* x, size_t n, uint32_t adder, uint32_t phase0, const float* lut_g) {
+			__shared__ float lut[80];
+			if (threadIdx.x < 80)
+				lut[threadIdx.x] = lut_g[threadIdx.x];
+			__syncthreads();
+			for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n; i += static_cast<size_t>(gridDim.x) * blockDim.x)
+				x[i] = table_mix(x[i], i, adder, phase0, lut);
+		}
+
+		// single-CTA complex DFT; conj_in/conj_out implement the inverse by conjugation
+		__global__ void dft_small_kernel(const float2* in, float2* out, FftPlanDev plan, int inverse, float scale) {
+			extern __shared__ float2 sm[];
+			float2* a = sm;
+			float2* b = sm + plan.n;
+			for (int i = threadIdx.x; i < plan.n; i += blockDim.x)
+				a[i] = in[i];
+			__syncthreads();
+			const float2* y = inverse ? fft_passes<true>(a, b, plan) : fft_passes<false>(a, b, plan);
+			for (int i = threadIdx.x; i < plan.n; i += blockDim.x)
+				out[i] = scale == 1.0f ? y[i] : cscale(y[i], scale);
+		}
+
+		// four-step forward of one array (k1-major output) for sizes above one CTA
+		__global__ void dft_large_kernel(LargeParams p, const float2* in, int conj_in) {
+			extern __shared__ float2 sm[];
+			const int tile = max(p.cw * p.n1, p.rw * p.n2);
+			four_step_forward(p, sm, sm + tile, p.code_out, [&](int64_t i) {
+				const float2 v = in[i];
+				return conj_in ? c2(v.x, -v.y) : v;
+			});
+		}
+
+		// k1-major (X_T[k1][k2] = X[k1 + N1 k2]) -> natural order, optional conj and scale
+		__global__ void untranspose_kernel(const float2* t, float2* out, int n1, int n2, int conj_out, float scale) {
+			const size_t n = static_cast<size_t>(n1) * n2;
+			for (size_t e = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; e < n; e += static_cast<size_t>(gridDim.x) * blockDim.x) {
+				const size_t k1 = e / n2, k2 = e % n2;
+				float2 v = t[e];
+				if (conj_out)
+					v.y = -v.y;
+				out[k1 + static_cast<size_t>(n1) * k2] = scale == 1.0f ? v : cscale(v, scale);
+			}
+		}
+
+		__global__ void cmul_kernel(float2* x, const float2* s, size_t n) {
+			for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n; i += static_cast<size_t>(gridDim.x) * blockDim.x)
+				x[i] = cmul(x[i], s[i]);
+		}
+
+		__global__ void real_to_complex_kernel(const float* in, float2* out, size_t n) {
+			for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n; i += static_cast<size_t>(gridDim.x) * blockDim.x)
+				out[i] = c2(in[i], 0.f);
+		}
+
+		__global__ void conj_mask_kernel(float2* x, size_t n, int one_sided) {
+			for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n; i += static_cast<size_t>(gridDim.x) * blockDim.x)
+				x[i] = (one_sided && i > n / 2) ? c2(0.f, 0.f) : c2(x[i].x, -x[i].y);
+		}
+
+		// (v / N) * 2 as the reference's FFTW inverse (dft.hpp:194-198), or v / N
+		__global__ void inverse_scale_kernel(float2* x, size_t n, int one_sided) {
+			const float fn = static_cast<float>(n);
+			for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n; i += static_cast<size_t>(gridDim.x) * blockDim.x) {
+				float2 v = c2(__fdiv_rn(x[i].x, fn), __fdiv_rn(x[i].y, fn));
+				if (one_sided)
+					v = c2(v.x * 2.0f, v.y * 2.0f);
+				x[i] = v;
+			}
+		}
+
+		__global__ void abs_kernel(const float2* x, float* out, size_t n) {
+			for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n; i += static_cast<size_t>(gridDim.x) * blockDim.x)
+				out[i] = hypotf(x[i].x, x[i].y);
+		}
+
+		template <typename V>
+		__global__ void fold_kernel(const V* in, V* out, size_t n, size_t block) {
+			const size_t folds = n / block;
+			for (size_t j = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; j < block; j += static_cast<size_t>(gridDim.x) * blockDim.x) {
+				V s = in[j];
+				for (size_t f = 1; f < folds; ++f) {
+					const V v = in[j + f * block];
+					if constexpr (std::is_same_v<V, float2>)
+						s = cadd(s, v);
+					else
+						s += v;
+				}
+				out[j] = s;
+			}
+		}
+
+		struct Partial {
+			float max_v;
+			uint32_t max_i_lo, max_i_hi;
+			double sum;
+		};
+
+		// grid-stride first-max + sum partials, one per block
+		__global__ void max_sum_kernel(const float* x, size_t n, Partial* parts) {
+			__shared__ float s_v[32];
+			__shared__ unsigned long long s_i[32];
+			__shared__ double s_s[32];
+			float bv = -INFINITY;
+			unsigned long long bi = ~0ull;
+			double sum = 0;
+			for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n; i += static_cast<size_t>(gridDim.x) * blockDim.x) {
+				const float v = x[i];
+				if (v > bv) {
+					bv = v;
+					bi = i;
+				}
+				sum += v;
+			}
+			for (int o = 16; o > 0; o >>= 1) {
+				const float ov = __shfl_down_sync(0xffffffffu, bv, o);
+				const unsigned long long oi = __shfl_down_sync(0xffffffffu, bi, o);
+				if (ov > bv || (ov == bv && oi < bi)) {
+					bv = ov;
+					bi = oi;
+				}
+				sum += __shfl_down_sync(0xffffffffu, sum, o);
+			}
+			const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+			if (lane == 0) {
+				s_v[w] = bv;
+				s_i[w] = bi;
+				s_s[w] = sum;
+			}
+			__syncthreads();
+			if (threadIdx.x == 0) {
+				for (int k = 1; k < (blockDim.x + 31) / 32; ++k) {
+					if (s_v[k] > bv || (s_v[k] == bv && s_i[k] < bi)) {
+						bv = s_v[k];
+						bi = s_i[k];
+					}
+					sum += s_s[k];
+				}
+				parts[blockIdx.x] = Partial{bv, static_cast<uint32_t>(bi), static_cast<uint32_t>(bi >> 32), sum};
+			}
+		}
+
+		__global__ void sq_dev_kernel(const float* x, size_t n, double mean, double* parts) {
+			__shared__ double s[32];
+			double acc = 0;
+			for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n; i += static_cast<size_t>(gridDim.x) * blockDim.x) {
+				const double d = static_cast<double>(x[i]) - mean;
+				acc += d * d;
+			}
+			for (int o = 16; o > 0; o >>= 1)
+				acc += __shfl_down_sync(0xffffffffu, acc, o);
+			if ((threadIdx.x & 31) == 0)
+				s[threadIdx.x >> 5] = acc;
+			__syncthreads();
+			if (threadIdx.x == 0) {
+				for (int k = 1; k < (blockDim.x + 31) / 32; ++k)
+					acc += s[k];
+				parts[blockIdx.x] = acc;
+			}
+		}
+
+		template <typename V>
+		__global__ void upsample_kernel(const V* in, size_t len, V* out, size_t samples) {
+			for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < samples; i += static_cast<size_t>(gridDim.x) * blockDim.x)
+				out[i] = in[(static_cast<unsigned __int128>(i) * len / samples) % len];
+		}
+
+		// ZOH to the lcm then boxcar mean over `ratio` (decimator.hpp:144-160); output k
+		// averages upsampled indices [k ratio, (k+1) ratio) clipped to `up` (zero pad).
+		// Input j covers upsampled [ceil(j up/n), ceil((j+1) up/n)); weights are overlaps.
+		__global__ void resample_kernel(const float2* in, size_t n, uint64_t up, uint64_t ratio, float2* out, size_t n_out) {
+			for (size_t k = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; k < n_out; k += static_cast<size_t>(gridDim.x) * blockDim.x) {
+				const uint64_t i0 = k * ratio;
+				const uint64_t i1 = min(i0 + ratio, up);
+				float2 acc = c2(0.f, 0.f);
+				if (i0 < i1) {
+					uint64_t j = static_cast<uint64_t>((static_cast<unsigned __int128>(i0) * n) / up);
+					uint64_t i = i0;
+					while (i < i1) {
+						// first upsampled index of input j + 1
+						const uint64_t next = static_cast<uint64_t>((static_cast<unsigned __int128>(j + 1) * up + n - 1) / n);
+						const uint64_t stop = min(next, i1);
+						const float w = static_cast<float>(stop - i);
+						const float2 v = in[j % n];
+						acc = c2(acc.x + w * v.x, acc.y + w * v.y);
+						i = stop;
+						++j;
+					}
+				}
+				const float r = static_cast<float>(ratio);
+				out[k] = c2(acc.x / r, acc.y / r);
+			}
+		}
+
+		__global__ void dot_kernel(const float2* x, const float* code, size_t n, double* parts) {
+			__shared__ double s[2][32];
+			double re = 0, im = 0;
+			for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n; i += static_cast<size_t>(gridDim.x) * blockDim.x) {
+				re += static_cast<double>(x[i].x) * code[i];
+				im += static_cast<double>(x[i].y) * code[i];
+			}
+			for (int o = 16; o > 0; o >>= 1) {
+				re += __shfl_down_sync(0xffffffffu, re, o);
+				im += __shfl_down_sync(0xffffffffu, im, o);
+			}
+			if ((threadIdx.x & 31) == 0) {
+				s[0][threadIdx.x >> 5] = re;
+				s[1][threadIdx.x >> 5] = im;
+			}
+			__syncthreads();
+			if (threadIdx.x == 0) {
+				for (int k = 1; k < (blockDim.x + 31) / 32; ++k) {
+					re += s[0][k];
+					im += s[1][k];
+				}
+				parts[2 * blockIdx.x] = re;
+				parts[2 * blockIdx.x + 1] = im;
+			}
+		}
+
+		template <int ST>
+		__global__ void convert_kernel(const void* in, float2* out, size_t n) {
+			for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n; i += static_cast<size_t>(gridDim.x) * blockDim.x)
+				out[i] = load_sample<ST>(in, i);
+		}
+
+		// ------------------------------------------------------- helpers
+		void h2d(ugsdr_ctx* ctx, void* d, const void* h, size_t bytes) {
+			UG_CUDA(cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, ctx->stream));
+		}
+		void d2h(ugsdr_ctx* ctx, void* h, const void* d, size_t bytes) {
+			UG_CUDA(cudaMemcpyAsync(h, d, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+			UG_CUDA(cudaStreamSynchronize(ctx->stream));
+		}
+
+		// complex DFT device->device: out = DFT(in) (unnormalised, sign by `inverse`)
+		void dft_device(ugsdr_ctx* ctx, const float2* in, float2* out, size_t n, bool inverse, DevBuf& tmp) {
+			require(n >= 2 && n <= (1u << 24), "DFT size out of range");
+			const int ni = static_cast<int>(n);
+			if (fits_single_cta(ctx, ni)) {
+				FftPlanDev p = dev_plan(get_plan(ctx, ni));
+				const size_t smem = 2 * sizeof(float2) * n;
+				smem_attr(dft_small_kernel, smem);
+				dft_small_kernel<<<1, kT, smem, ctx->stream>>>(in, out, p, inverse ? 1 : 0, 1.0f);
+				note_launch(ctx);
+				return;
+			}
+			const LargePlan& lp = get_large_plan(ctx, ni);
+			LargeParams p{};
+			p.base.n = ni;
+			p.p1 = dev_plan(lp.p1);
+			p.p2 = dev_plan(lp.p2);
+			p.n1 = lp.n1;
+			p.n2 = lp.n2;
+			const size_t budget = ctx->smem_optin - 2048;
+			p.cw = 16;
+			while (p.cw > 4 && 2 * sizeof(float2) * p.cw * static_cast<size_t>(lp.n1) > budget)
+				p.cw /= 2;
+			p.rw = 16;
+			while (p.rw > 1 && 2 * sizeof(float2) * p.rw * static_cast<size_t>(lp.n2) > budget)
+				p.rw /= 2;
+			p.tw = lp.tw;
+			tmp.reserve(sizeof(float2) * n);
+			p.code_out = tmp.as<float2>();
+			const size_t smem = 2 * sizeof(float2) * std::max(p.cw * lp.n1, p.rw * lp.n2);
+			smem_attr(dft_large_kernel, smem);
+			// inverse via conj(DFT(conj(x)))
+			dft_large_kernel<<<1, 512, smem, ctx->stream>>>(p, in, inverse ? 1 : 0);
+			untranspose_kernel<<<blocks_for(n), kT, 0, ctx->stream>>>(tmp.as<float2>(), out, lp.n1, lp.n2, inverse ? 1 : 0, 1.0f);
+			note_launch(ctx, 2);
+		}
+	}
+}
+
+using namespace ugsdr_gpu;
+
+#define UG_ENTRY(ctx) \
+	if (!(ctx))       \
+		return UGSDR_E_INVALID; \
+	std::lock_guard<std::mutex> lock_((ctx)->mutex); \
+	return guarded((ctx), [&]
+
+extern "C" {
+
+int ugsdr_mix(ugsdr_ctx* ctx, float* iq, size_t n, double fs, double frequency, double phase) {
+	UG_ENTRY(ctx) {
+		require(iq != nullptr || n == 0, "null buffer");
+		require(fs > 0, "sampling rate must be positive");
+		// Mixer::Translate(T&) (mixer.hpp:33-42): FixPhase, zero frequency is a no-op
+		const uint32_t phase0 = nco_phase(phase);
+		if (std::abs(frequency) == 0.0 || n == 0)
+			return;
+		const uint32_t adder = nco_adder(fs, frequency);
+		ctx->op_a.reserve(sizeof(float2) * n);
+		h2d(ctx, ctx->op_a.ptr, iq, sizeof(float2) * n);
+		mix_kernel<<<blocks_for(n), kT, 0, ctx->stream>>>(ctx->op_a.as<float2>(), n, adder, phase0, get_lut(ctx));
+		note_launch(ctx);
+		d2h(ctx, iq, ctx->op_a.ptr, sizeof(float2) * n);
+	});
+}
+
+int ugsdr_dft(ugsdr_ctx* ctx, const float* in_iq, float* out_iq, size_t n, int inverse) {
+	UG_ENTRY(ctx) {
+		require(in_iq && out_iq, "null buffer");
+		ctx->op_a.reserve(sizeof(float2) * n);
+		ctx->op_b.reserve(sizeof(float2) * n);
+		h2d(ctx, ctx->op_a.ptr, in_iq, sizeof(float2) * n);
+		dft_device(ctx, ctx->op_a.as<float2>(), ctx->op_b.as<float2>(), n, inverse != 0, ctx->op_c);
+		if (inverse) {
+			inverse_scale_kernel<<<blocks_for(n), kT, 0, ctx->stream>>>(ctx->op_b.as<float2>(), n, 1);
+			note_launch(ctx);
+		}
+		d2h(ctx, out_iq, ctx->op_b.ptr, sizeof(float2) * n);
+	});
+}
+
+int ugsdr_matched_filter_prepare(ugsdr_ctx* ctx, const float* code, size_t n, int spectrum_mode, float* spectrum_iq) {
+	UG_ENTRY(ctx) {
+		require(code && spectrum_iq, "null buffer");
+		require(spectrum_mode == 0 || spectrum_mode == 1, "bad spectrum mode");
+		ctx->op_a.reserve(sizeof(float2) * n);
+		ctx->op_b.reserve(sizeof(float2) * n);
+		float* staged = reinterpret_cast<float*>(ctx->op_b.as<float2>());
+		h2d(ctx, staged, code, sizeof(float) * n);
+		real_to_complex_kernel<<<blocks_for(n), kT, 0, ctx->stream>>>(staged, ctx->op_a.as<float2>(), n);
+		note_launch(ctx);
+		dft_device(ctx, ctx->op_a.as<float2>(), ctx->op_b.as<float2>(), n, false, ctx->op_c);
+		conj_mask_kernel<<<blocks_for(n), kT, 0, ctx->stream>>>(ctx->op_b.as<float2>(), n, spectrum_mode == 0);
+		note_launch(ctx);
+		d2h(ctx, spectrum_iq, ctx->op_b.ptr, sizeof(float2) * n);
+	});
+}
+
+int ugsdr_matched_filter(ugsdr_ctx* ctx, float* iq, size_t n, const float* spectrum_iq, int spectrum_mode) {
+	UG_ENTRY(ctx) {
+		require(iq && spectrum_iq, "null buffer");
+		ctx->op_a.reserve(sizeof(float2) * n * 2);
+		ctx->op_b.reserve(sizeof(float2) * n);
+		float2* x = ctx->op_a.as<float2>();
+		float2* s = x + n;
+		h2d(ctx, x, iq, sizeof(float2) * n);
+		h2d(ctx, s, spectrum_iq, sizeof(float2) * n);
+		dft_device(ctx, x, ctx->op_b.as<float2>(), n, false, ctx->op_c);
+		cmul_kernel<<<blocks_for(n), kT, 0, ctx->stream>>>(ctx->op_b.as<float2>(), s, n);
+		note_launch(ctx);
+		dft_device(ctx, ctx->op_b.as<float2>(), x, n, true, ctx->op_c);
+		inverse_scale_kernel<<<blocks_for(n), kT, 0, ctx->stream>>>(x, n, spectrum_mode == 0);
+		note_launch(ctx);
+		d2h(ctx, iq, x, sizeof(float2) * n);
+	});
+}
+
+int ugsdr_abs(ugsdr_ctx* ctx, const float* iq, size_t n, float* out) {
+	UG_ENTRY(ctx) {
+		require(iq && out, "null buffer");
+		ctx->op_a.reserve(sizeof(float2) * n);
+		ctx->op_b.reserve(sizeof(float) * n);
+		h2d(ctx, ctx->op_a.ptr, iq, sizeof(float2) * n);
+		abs_kernel<<<blocks_for(n), kT, 0, ctx->stream>>>(ctx->op_a.as<float2>(), ctx->op_b.as<float>(), n);
+		note_launch(ctx);
+		d2h(ctx, out, ctx->op_b.ptr, sizeof(float) * n);
+	});
+}
+
+int ugsdr_reshape_sum(ugsdr_ctx* ctx, const float* in, size_t n, size_t block, int is_complex, float* out) {
+	UG_ENTRY(ctx) {
+		require(in && out, "null buffer");
+		// ReshapeAndSum::CheckBlockSize (reshape_and_sum.hpp:15-18)
+		require(block > 0 && n % block == 0, "Signal size is not divided by block size");
+		const size_t w = is_complex ? 8 : 4;
+		ctx->op_a.reserve(w * n);
+		ctx->op_b.reserve(w * block);
+		h2d(ctx, ctx->op_a.ptr, in, w * n);
+		if (is_complex)
+			fold_kernel<float2><<<blocks_for(block), kT, 0, ctx->stream>>>(ctx->op_a.as<float2>(), ctx->op_b.as<float2>(), n, block);
+		else
+			fold_kernel<float><<<blocks_for(block), kT, 0, ctx->stream>>>(ctx->op_a.as<float>(), ctx->op_b.as<float>(), n, block);
+		note_launch(ctx);
+		d2h(ctx, out, ctx->op_b.ptr, w * block);
+	});
+}
+
+int ugsdr_max_index(ugsdr_ctx* ctx, const float* in, size_t n, float* value, size_t* index) {
+	UG_ENTRY(ctx) {
+		require(in && value && index && n > 0, "null buffer or empty input");
+		const int blocks = std::max(1, std::min(blocks_for(n), 1024));
+		ctx->op_a.reserve(sizeof(float) * n);
+		ctx->op_b.reserve(sizeof(Partial) * blocks);
+		h2d(ctx, ctx->op_a.ptr, in, sizeof(float) * n);
+		max_sum_kernel<<<blocks, kT, 0, ctx->stream>>>(ctx->op_a.as<float>(), n, ctx->op_b.as<Partial>());
+		note_launch(ctx);
+		std::vector<Partial> parts(blocks);
+		d2h(ctx, parts.data(), ctx->op_b.ptr, sizeof(Partial) * blocks);
+		float bv = parts[0].max_v;
+		uint64_t bi = parts[0].max_i_lo | (static_cast<uint64_t>(parts[0].max_i_hi) << 32);
+		for (int b = 1; b < blocks; ++b) {
+			const uint64_t i = parts[b].max_i_lo | (static_cast<uint64_t>(parts[b].max_i_hi) << 32);
+			if (parts[b].max_v > bv || (parts[b].max_v == bv && i < bi)) {
+				bv = parts[b].max_v;
+				bi = i;
+			}
+		}
+		*value = bv;
+		*index = static_cast<size_t>(bi);
+	});
+}
+
+int ugsdr_mean_stddev(ugsdr_ctx* ctx, const float* in, size_t n, float* mean, float* sigma) {
+	UG_ENTRY(ctx) {
+		require(mean && sigma, "null output");
+		// mean_stddev.hpp:30-31: fewer than two samples give {0, 0}
+		if (n < 2) {
+			*mean = 0;
+			*sigma = 0;
+			return;
+		}
+		require(in != nullptr, "null buffer");
+		const int blocks = std::max(1, std::min(blocks_for(n), 1024));
+		ctx->op_a.reserve(sizeof(float) * n);
+		ctx->op_b.reserve(sizeof(Partial) * blocks + sizeof(double) * blocks);
+		h2d(ctx, ctx->op_a.ptr, in, sizeof(float) * n);
+		max_sum_kernel<<<blocks, kT, 0, ctx->stream>>>(ctx->op_a.as<float>(), n, ctx->op_b.as<Partial>());
+		note_launch(ctx);
+		std::vector<Partial> parts(blocks);
+		d2h(ctx, parts.data(), ctx->op_b.ptr, sizeof(Partial) * blocks);
+		double sum = 0;
+		for (auto& p : parts)
+			sum += p.sum;
+		const double m = sum / static_cast<double>(n);
+		double* sq = reinterpret_cast<double*>(ctx->op_b.as<char>() + sizeof(Partial) * blocks);
+		sq_dev_kernel<<<blocks, kT, 0, ctx->stream>>>(ctx->op_a.as<float>(), n, m, sq);
+		note_launch(ctx);
+		std::vector<double> sqs(blocks);
+		d2h(ctx, sqs.data(), sq, sizeof(double) * blocks);
+		const double ss = std::accumulate(sqs.begin(), sqs.end(), 0.0);
+		*mean = static_cast<float>(m);
+		*sigma = static_cast<float>(std::sqrt(ss / static_cast<double>(n - 1)));
+	});
+}
+
+int ugsdr_upsample(ugsdr_ctx* ctx, const float* in, size_t n, int is_complex, float* out, size_t samples) {
+	UG_ENTRY(ctx) {
+		require(in && out && n > 0, "null buffer or empty input");
+		const size_t w = is_complex ? 8 : 4;
+		ctx->op_a.reserve(w * n);
+		ctx->op_b.reserve(w * samples);
+		h2d(ctx, ctx->op_a.ptr, in, w * n);
+		if (is_complex)
+			upsample_kernel<float2><<<blocks_for(samples), kT, 0, ctx->stream>>>(ctx->op_a.as<float2>(), n, ctx->op_b.as<float2>(), samples);
+		else
+			upsample_kernel<float><<<blocks_for(samples), kT, 0, ctx->stream>>>(ctx->op_a.as<float>(), n, ctx->op_b.as<float>(), samples);
+		note_launch(ctx);
+		d2h(ctx, out, ctx->op_b.ptr, w * samples);
+	});
+}
+
+int ugsdr_resample(ugsdr_ctx* ctx, const float* in_iq, size_t n, uint64_t new_fs, uint64_t old_fs, float* out_iq, size_t cap,
+	size_t* n_out) {
+	UG_ENTRY(ctx) {
+		require(n_out != nullptr && new_fs > 0 && old_fs > 0, "null output or zero rate");
+		const uint64_t lcm = std::lcm(new_fs, old_fs);
+		const unsigned __int128 up128 = static_cast<unsigned __int128>(lcm) * n / old_fs;
+		require(up128 < (static_cast<unsigned __int128>(1) << 62), "resampling ratio too large");
+		const uint64_t up = static_cast<uint64_t>(up128);
+		const uint64_t ratio = lcm / new_fs;
+		const uint64_t padded = (up % ratio) ? (up / ratio + 1) * ratio : up;
+		const size_t out_n = ratio == 1 ? static_cast<size_t>(up) : static_cast<size_t>(padded / ratio);
+		*n_out = out_n;
+		if (!out_iq)
+			return;
+		require(cap >= out_n, "output buffer too small");
+		require(in_iq != nullptr && n > 0, "null input");
+		ctx->op_a.reserve(sizeof(float2) * n);
+		ctx->op_b.reserve(sizeof(float2) * out_n);
+		h2d(ctx, ctx->op_a.ptr, in_iq, sizeof(float2) * n);
+		resample_kernel<<<blocks_for(out_n), kT, 0, ctx->stream>>>(ctx->op_a.as<float2>(), n, up, ratio, ctx->op_b.as<float2>(), out_n);
+		note_launch(ctx);
+		d2h(ctx, out_iq, ctx->op_b.ptr, sizeof(float2) * out_n);
+	});
+}
+
+int ugsdr_correlate(ugsdr_ctx* ctx, const float* iq, const float* code, size_t n, float* out_iq) {
+	UG_ENTRY(ctx) {
+		require(iq && code && out_iq, "null buffer");
+		const int blocks = std::max(1, std::min(blocks_for(n), 1024));
+		ctx->op_a.reserve(sizeof(float2) * n + sizeof(float) * n);
+		ctx->op_b.reserve(2 * sizeof(double) * blocks);
+		float2* x = ctx->op_a.as<float2>();
+		float* c = reinterpret_cast<float*>(x + n);
+		h2d(ctx, x, iq, sizeof(float2) * n);
+		h2d(ctx, c, code, sizeof(float) * n);
+		dot_kernel<<<blocks, kT, 0, ctx->stream>>>(x, c, n, ctx->op_b.as<double>());
+		note_launch(ctx);
+		std::vector<double> parts(2 * blocks);
+		d2h(ctx, parts.data(), ctx->op_b.ptr, sizeof(double) * 2 * blocks);
+		double re = 0, im = 0;
+		for (int b = 0; b < blocks; ++b) {
+			re += parts[2 * b];
+			im += parts[2 * b + 1];
+		}
+		out_iq[0] = static_cast<float>(re);
+		out_iq[1] = static_cast<float>(im);
+	});
+}
+
+int ugsdr_convert_samples(ugsdr_ctx* ctx, const void* in, int sample_type, size_t n, float* out_iq) {
+	UG_ENTRY(ctx) {
+		require(in && out_iq, "null buffer");
+		size_t w = 0;
+		switch (sample_type) {
+		case UGSDR_SAMPLES_CF32: w = 8; break;
+		case UGSDR_SAMPLES_CI8: w = 2; break;
+		case UGSDR_SAMPLES_CI16: w = 4; break;
+		case UGSDR_SAMPLES_RI8: w = 1; break;
+		default: require(false, "unknown sample type");
+		}
+		ctx->op_a.reserve(w * n + 16);
+		ctx->op_b.reserve(sizeof(float2) * n);
+		h2d(ctx, ctx->op_a.ptr, in, w * n);
+		const int g = blocks_for(n);
+		switch (sample_type) {
+		case UGSDR_SAMPLES_CF32: convert_kernel<UGSDR_SAMPLES_CF32><<<g, kT, 0, ctx->stream>>>(ctx->op_a.ptr, ctx->op_b.as<float2>(), n); break;
+		case UGSDR_SAMPLES_CI8: convert_kernel<UGSDR_SAMPLES_CI8><<<g, kT, 0, ctx->stream>>>(ctx->op_a.ptr, ctx->op_b.as<float2>(), n); break;
+		case UGSDR_SAMPLES_CI16: convert_kernel<UGSDR_SAMPLES_CI16><<<g, kT, 0, ctx->stream>>>(ctx->op_a.ptr, ctx->op_b.as<float2>(), n); break;
+		default: convert_kernel<UGSDR_SAMPLES_RI8><<<g, kT, 0, ctx->stream>>>(ctx->op_a.ptr, ctx->op_b.as<float2>(), n); break;
+		}
+		note_launch(ctx);
+		d2h(ctx, out_iq, ctx->op_b.ptr, sizeof(float2) * n);
+	});
+}
+}
