@@ -5,10 +5,12 @@
 #include "internal.hpp"
 #include "acq_kernels.cuh"
 #include "acq_large.cuh"
+#include "fft_plan.hpp"
 
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <numeric>
 
 namespace ugsdr_gpu {
@@ -269,10 +271,99 @@ namespace ugsdr_gpu {
 			UG_CUDA(cudaStreamSynchronize(ctx->stream));
 		}
 
+		// Bluestein chirp-z: X_k = w_k sum_j (x_j w_j) conj(w_{k-j}), w_m = exp(-i pi m^2 / N),
+		// the convolution done with M-point FFTs (M >= 2N - 1, all radices supported).
+		__global__ void chirp_premul_kernel(const float2* x, const float2* w, float2* a, size_t n, size_t m, int conj_in) {
+			for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < m; i += static_cast<size_t>(gridDim.x) * blockDim.x) {
+				if (i < n) {
+					float2 v = x[i];
+					if (conj_in)
+						v.y = -v.y;
+					a[i] = cmul(v, w[i]);
+				}
+				else {
+					a[i] = c2(0.f, 0.f);
+				}
+			}
+		}
+		__global__ void chirp_postmul_kernel(const float2* conv, const float2* w, float2* out, size_t n, float inv_m, int conj_out) {
+			for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n; i += static_cast<size_t>(gridDim.x) * blockDim.x) {
+				float2 v = cscale(cmul(conv[i], w[i]), inv_m);
+				if (conj_out)
+					v.y = -v.y;
+				out[i] = v;
+			}
+		}
+
+		struct Bluestein {
+			size_t n = 0, m = 0;
+			DevBuf w;      // n chirp values
+			DevBuf bf;     // FFT_M of the conjugate chirp, wrapped
+			DevBuf a, b;   // M-point work buffers
+			DevBuf tmp;
+		};
+
+		bool plannable(int n) {
+			std::vector<int> r;
+			return plan_radices(n, r);
+		}
+
+		void dft_device(ugsdr_ctx* ctx, const float2* in, float2* out, size_t n, bool inverse, DevBuf& tmp);
+
+		Bluestein& get_bluestein(ugsdr_ctx* ctx, size_t n) {
+			static std::mutex mu;
+			static std::map<std::pair<ugsdr_ctx*, size_t>, std::unique_ptr<Bluestein>> cache;
+			std::lock_guard<std::mutex> lock(mu);
+			auto& slot = cache[{ctx, n}];
+			if (slot)
+				return *slot;
+			auto bl = std::make_unique<Bluestein>();
+			bl->n = n;
+			size_t m = 2 * n - 1;
+			while (!plannable(static_cast<int>(m)))
+				++m;
+			bl->m = m;
+			std::vector<float2> w(n), b(m, c2(0.f, 0.f));
+			const double pi = 3.14159265358979323846;
+			for (size_t k = 0; k < n; ++k) {
+				const uint64_t e = (static_cast<uint64_t>(k) * k) % (2 * n);  // exact m^2 mod 2N
+				const double ang = -pi * static_cast<double>(e) / static_cast<double>(n);
+				w[k] = c2(static_cast<float>(std::cos(ang)), static_cast<float>(std::sin(ang)));
+				const float2 cw = c2(w[k].x, -w[k].y);
+				b[k] = cw;
+				if (k)
+					b[m - k] = cw;
+			}
+			bl->w.reserve(sizeof(float2) * n);
+			bl->bf.reserve(sizeof(float2) * m);
+			bl->a.reserve(sizeof(float2) * m);
+			bl->b.reserve(sizeof(float2) * m);
+			UG_CUDA(cudaMemcpy(bl->w.ptr, w.data(), sizeof(float2) * n, cudaMemcpyHostToDevice));
+			UG_CUDA(cudaMemcpy(bl->a.ptr, b.data(), sizeof(float2) * m, cudaMemcpyHostToDevice));
+			dft_device(ctx, bl->a.as<float2>(), bl->bf.as<float2>(), m, false, bl->tmp);
+			UG_CUDA(cudaStreamSynchronize(ctx->stream));
+			slot = std::move(bl);
+			return *slot;
+		}
+
 		// complex DFT device->device: out = DFT(in) (unnormalised, sign by `inverse`)
 		void dft_device(ugsdr_ctx* ctx, const float2* in, float2* out, size_t n, bool inverse, DevBuf& tmp) {
 			require(n >= 2 && n <= (1u << 24), "DFT size out of range");
 			const int ni = static_cast<int>(n);
+			if (!plannable(ni)) {
+				// inverse via conj(DFT(conj(x)))
+				Bluestein& bl = get_bluestein(ctx, n);
+				chirp_premul_kernel<<<blocks_for(bl.m), kT, 0, ctx->stream>>>(in, bl.w.as<float2>(), bl.a.as<float2>(), n, bl.m, inverse ? 1 : 0);
+				note_launch(ctx);
+				dft_device(ctx, bl.a.as<float2>(), bl.b.as<float2>(), bl.m, false, bl.tmp);
+				cmul_kernel<<<blocks_for(bl.m), kT, 0, ctx->stream>>>(bl.b.as<float2>(), bl.bf.as<float2>(), bl.m);
+				note_launch(ctx);
+				dft_device(ctx, bl.b.as<float2>(), bl.a.as<float2>(), bl.m, true, bl.tmp);
+				chirp_postmul_kernel<<<blocks_for(n), kT, 0, ctx->stream>>>(bl.a.as<float2>(), bl.w.as<float2>(), out, n,
+					1.0f / static_cast<float>(bl.m), inverse ? 1 : 0);
+				note_launch(ctx);
+				return;
+			}
 			if (fits_single_cta(ctx, ni)) {
 				FftPlanDev p = dev_plan(get_plan(ctx, ni));
 				const size_t smem = 2 * sizeof(float2) * n;
