@@ -185,6 +185,54 @@ int ugsdr_acquire_batch(ugsdr_ctx* ctx, const ugsdr_acq_job* jobs, int n_jobs, u
 /* Number of Doppler bins the reference loop visits for (range, step). */
 int ugsdr_doppler_bins(double range, double step, uint32_t* n);
 
+/* ------------------------------------------- allocation-free acquisition */
+/* No counterpart in the reference: an extra entry point of this library.
+ *
+ * ugsdr_acquire_static runs the same search as ugsdr_acquire (single-CTA block
+ * sizes: block_samples up to about 11,000) without allocating any device
+ * memory.  It is meant for callers that must not call cudaMalloc: real-time
+ * receiver loops, where an allocation can synchronise the device and take an
+ * unbounded time, and host applications whose device memory is owned by
+ * another allocator or pool that reserves HBM up front, so an extra cudaMalloc
+ * would fail or fragment it.  Such callers allocate inputs and outputs
+ * themselves and pass device pointers.
+ *
+ * Scratch (code spectra, mixed spectra, twiddles, Doppler table) lives in one
+ * file-scope device array of UGSDR_STATIC_SCRATCH_BYTES, which every GPU that
+ * loads the library holds until the process exits.  A job needing more is
+ * rejected with UGSDR_E_NOMEM and *scratch_needed set to the bytes it needs.
+ * The first call on a device (with that device current) resolves the array's
+ * device address and uploads the mixer table; make that first call before any
+ * stream capture.  All calls share the one array: calls that overlap on the
+ * GPU (different streams or host threads without ordering) race on it.
+ * Nothing in it needs to start at zero; each call rewrites what it reads. */
+#define UGSDR_STATIC_SCRATCH_BYTES (16u << 20)
+
+typedef struct ugsdr_static_job {
+	const void* samples;       /* DEVICE pointer: n_samples samples of sample_type */
+	int sample_type;           /* ugsdr_sample_type */
+	size_t n_samples;          /* >= block_samples * n_blocks */
+	double sampling_rate;      /* Hz */
+	double frontend_frequency; /* as ugsdr_acq_job::frontend_frequency (0 = none) */
+	size_t block_samples;      /* N */
+	size_t n_blocks;           /* K */
+	size_t fold_samples;       /* as ugsdr_acq_job */
+	int fold_coherent;
+	double doppler_range;
+	double doppler_step;
+	const float* code_samples; /* DEVICE pointer: n_codes x block_samples code samples (+-1) */
+	int n_codes;
+	int statistic;             /* ugsdr_statistic */
+	int spectrum_mode;         /* ugsdr_spectrum_mode */
+} ugsdr_static_job;
+
+/* cells_device: DEVICE pointer to n_codes x n_doppler records (code-major),
+ * written on `cuda_stream` (a cudaStream_t; NULL = legacy default stream).
+ * Returns after enqueueing; synchronise the stream before reading the cells.
+ * scratch_needed (optional) receives the scratch bytes the job uses. */
+int ugsdr_acquire_static(void* cuda_stream, const ugsdr_static_job* job, ugsdr_acq_cell* cells_device,
+	size_t* scratch_needed);
+
 /* ---------------------------------------------- per-op policy entries */
 /* Each replaces one reference policy implementation; host buffers. */
 

@@ -184,3 +184,28 @@ def check(status: int, ctx=None) -> None:
     if status != OK:
         msg = load().ugsdr_last_error(ctx).decode() if ctx else "error"
         raise UgsdrError(status, msg)
+
+
+class StaticJob(C.Structure):
+    """ugsdr_static_job (allocation-free entry point; device pointers)."""
+    _fields_ = [
+        ("samples", C.c_void_p),
+        ("sample_type", C.c_int),
+        ("n_samples", C.c_size_t),
+        ("sampling_rate", C.c_double),
+        ("frontend_frequency", C.c_double),
+        ("block_samples", C.c_size_t),
+        ("n_blocks", C.c_size_t),
+        ("fold_samples", C.c_size_t),
+        ("fold_coherent", C.c_int),
+        ("doppler_range", C.c_double),
+        ("doppler_step", C.c_double),
+        ("code_samples", C.c_void_p),
+        ("n_codes", C.c_int),
+        ("statistic", C.c_int),
+        ("spectrum_mode", C.c_int),
+    ]
+
+
+STATIC_SCRATCH_BYTES = 16 << 20
+SIGNATURES["ugsdr_acquire_static"] = (C.c_int, [C.c_void_p, C.POINTER(StaticJob), C.c_void_p, C.POINTER(C.c_size_t)])
