@@ -81,6 +81,17 @@ def multi_workload(seed: int = 2):
     return jobs, raw
 
 
+def gal_small_workload(seed: int = 2):
+    """Profiling case for the large-N kernels: the Galileo E1B job of the
+    multi-constellation capture cut to 4 codes x 5 Doppler bins (200,000-point
+    blocks, K = 10)."""
+    jobs, raw = multi_workload(seed)
+    gal = dict(jobs[-1])
+    gal["codes"] = gal["codes"][:4]
+    gal["step"] = 2500.0
+    return [gal], raw
+
+
 def gps_4mhz_workload(seed: int = 1):
     from ugsdr_gb300 import _lib as L
     from ugsdr_gb300 import api, signals
@@ -88,6 +99,9 @@ def gps_4mhz_workload(seed: int = 1):
     raw, _ = signals.gps_l1_config(seed=seed, codes=gps)
     jobs = [dict(system="gps", codes=[gps[p] for p in range(32)], n=4000, k=10, step=500.0, fe=0.0, if_=0.0, fs=4e6)]
     return jobs, raw
+
+
+WORKLOADS = {"multi": multi_workload, "gps_l1_4mhz": gps_4mhz_workload, "gal_small": gal_small_workload}
 
 
 def n_doppler(step, rng=5000.0):
@@ -166,7 +180,7 @@ def run_ours(args, world, rank):
 
     dev = int(os.environ.get("LOCAL_RANK", 0))
     torch.cuda.set_device(dev)
-    jobs, raw = (multi_workload() if args.config == "multi" else gps_4mhz_workload())
+    jobs, raw = WORKLOADS[args.config]()
     fs = jobs[0].get("fs", FS)
     stype = L.SAMPLES_CI16 if raw.dtype == np.int16 else L.SAMPLES_CI8
     ctx = api.Context(dev)
@@ -321,7 +335,7 @@ def cpu_baseline(args, jobs, raw, fs, budget_s: float = 20.0):
 def run_reference(args, world, rank):
     if rank != 0:
         return None
-    jobs, raw = (multi_workload() if args.config == "multi" else gps_4mhz_workload())
+    jobs, raw = WORKLOADS[args.config]()
     fs = jobs[0].get("fs", FS)
     vals = []
     for _ in range(args.warmup + args.steps):
@@ -346,7 +360,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--config", choices=["multi", "gps_l1_4mhz"], default="multi")
+    ap.add_argument("--config", choices=sorted(WORKLOADS), default="multi")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", 1))

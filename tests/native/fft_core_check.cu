@@ -29,8 +29,8 @@ static double run(int n, bool inv, const std::vector<int>& radices) {
 	int ns = 1;
 	for (int r : radices) {
 		for (int j = 0; j < n / r; ++j) {
-			const bool ok = inv ? butterfly_dispatch<true>(r, a.data(), b.data(), n, ns, tw.data(), j)
-			                    : butterfly_dispatch<false>(r, a.data(), b.data(), n, ns, tw.data(), j);
+			const bool ok = inv ? butterfly_dispatch<true>(r, a.data(), b.data(), n, ns, tw.data(), j, j % ns)
+			                    : butterfly_dispatch<false>(r, a.data(), b.data(), n, ns, tw.data(), j, j % ns);
 			if (!ok) {
 				std::printf("radix %d unsupported\n", r);
 				std::exit(2);

@@ -3,7 +3,7 @@
 // ugsdr_code_put / ugsdr_code_release / ugsdr_acquire / ugsdr_acquire_batch.
 #include "internal.hpp"
 #include "acq_kernels.cuh"
-#include "acq_large.cuh"
+#include "acq_batched.cuh"
 #include "fft_plan.hpp"
 
 #include <algorithm>
@@ -92,13 +92,10 @@ namespace ugsdr_gpu {
 	}
 
 	// ------------------------------------------------------ large-N path
-	namespace {
-		constexpr int kLargeThreads = 512;
-
-		size_t large_tile_bytes(const LargePlan& lp, int cw, int rw) {
-			return 2 * sizeof(float2) * static_cast<size_t>(std::max(cw * lp.n1, rw * lp.n2));
-		}
-	}
+	// Shape of one job as the large path needs it.
+	struct JobLaunchShape {
+		int n = 0, k = 0, m = 0, rows = 0, fold_mode = 0;
+	};
 
 	const LargePlan& get_large_plan(ugsdr_ctx* ctx, int n) {
 		auto it = ctx->large_plans.find(n);
@@ -131,49 +128,93 @@ namespace ugsdr_gpu {
 	}
 
 	namespace {
+		constexpr int kBatchedThreads = 256;
+
+		// Sub-transforms per CTA: 8 columns/rows (64-byte runs per k1 row) unless
+		// the tiles would exceed a third of shared memory.
+		// inv_cols holds three column tiles (input, work, prefetch) and an
+		// accumulator and runs two CTAs per SM; row kernels hold two row tiles
+		// and run three.
 		void tile_shape(ugsdr_ctx* ctx, const LargePlan& lp, int& cw, int& rw) {
-			const size_t budget = ctx->smem_optin - 2048;
-			cw = 16;
-			while (cw > 4 && 2 * sizeof(float2) * cw * static_cast<size_t>(lp.n1) > budget)
+			const size_t ld = static_cast<size_t>(lp.n1 | 1);
+			cw = 8;
+			while (cw > 1 && (3 * sizeof(float2) + sizeof(float)) * cw * ld > (ctx->smem_optin - 2048) / 2)
 				cw /= 2;
-			rw = 16;
-			while (rw > 1 && 2 * sizeof(float2) * rw * static_cast<size_t>(lp.n2) > budget)
+			rw = 8;
+			while (rw > 1 && 2 * sizeof(float2) * rw * static_cast<size_t>(lp.n2) > (ctx->smem_optin - 2048) / 3)
 				rw /= 2;
 		}
 
-		LargeParams large_params(ugsdr_ctx* ctx, const AcqParams& base, int n, size_t& smem) {
+		BatchedParams batched_params(ugsdr_ctx* ctx, const AcqParams& base, int n) {
 			const LargePlan& lp = get_large_plan(ctx, n);
-			LargeParams p{};
+			BatchedParams p{};
 			p.base = base;
 			p.p1 = to_dev(lp.p1);
 			p.p2 = to_dev(lp.p2);
 			p.n1 = lp.n1;
 			p.n2 = lp.n2;
 			tile_shape(ctx, lp, p.cw, p.rw);
-			p.tw = lp.tw;
-			smem = large_tile_bytes(lp, p.cw, p.rw);
+			p.ld1 = lp.n1 | 1;  // odd column stride: the 8 columns of a tile fall in distinct banks
+			p.cw_shift = 0;
+			while ((1 << p.cw_shift) < p.cw)
+				++p.cw_shift;
 			return p;
 		}
 
-		template <typename K>
-		int resident_grid(ugsdr_ctx* ctx, K kernel, int threads, size_t smem) {
-			int per_sm = 0;
-			UG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem));
-			return std::max(1, per_sm) * ctx->sm_count;
+		// fwd_cols: two tiles; inv_cols: input, work and prefetch tiles + accumulator
+		size_t smem_cols(const BatchedParams& p, bool inverse) {
+			return (inverse ? 3 * sizeof(float2) + sizeof(float) : 2 * sizeof(float2)) * static_cast<size_t>(p.cw) * p.ld1;
+		}
+		// row kernels: two tiles
+		size_t smem_rows(const BatchedParams& p, bool) {
+			return 2 * sizeof(float2) * static_cast<size_t>(p.rw) * p.n2;
 		}
 
-		size_t slab_elems(int n, int m) { return static_cast<size_t>(n) + (m + 1) / 2 + m; }
+		int chunks_of(int total, int per) { return (total + per - 1) / per; }
+
+		// rows per inverse batch: B (rows x K x N complex) within the budget
+		int batch_rows(const JobLaunchShape& s) {
+			const size_t per_row = sizeof(float2) * static_cast<size_t>(s.n) * s.k;
+			const size_t budget = static_cast<size_t>(512) << 20;
+			return static_cast<int>(std::max<size_t>(1, std::min<size_t>(s.rows, budget / per_row)));
+		}
+
+		template <typename K>
+		void launch_fwd_cols(ugsdr_ctx* ctx, K kernel, const BatchedParams& p, int items) {
+			const size_t smem = smem_cols(p, false);
+			set_smem(kernel, smem);
+			kernel<<<items * chunks_of(p.n2, p.cw), kBatchedThreads, smem, ctx->stream>>>(p);
+		}
+
+		void launch_forward(ugsdr_ctx* ctx, int sample_type, const BatchedParams& p, int items) {
+			switch (sample_type) {
+			case UGSDR_SAMPLES_CF32: launch_fwd_cols(ctx, fwd_cols_kernel<UGSDR_SAMPLES_CF32>, p, items); break;
+			case UGSDR_SAMPLES_CI8: launch_fwd_cols(ctx, fwd_cols_kernel<UGSDR_SAMPLES_CI8>, p, items); break;
+			case UGSDR_SAMPLES_CI16: launch_fwd_cols(ctx, fwd_cols_kernel<UGSDR_SAMPLES_CI16>, p, items); break;
+			default: launch_fwd_cols(ctx, fwd_cols_kernel<UGSDR_SAMPLES_RI8>, p, items); break;
+			}
+			const size_t smem = smem_rows(p, false);
+			set_smem(fwd_rows_kernel, smem);
+			fwd_rows_kernel<<<items * chunks_of(p.n1, p.rw), kBatchedThreads, smem, ctx->stream>>>(p);
+			note_launch(ctx, 2);
+		}
 	}
 
-	size_t large_slab_bytes(ugsdr_ctx* ctx, int n, int m) {
-		size_t smem = 0;
+	size_t batched_scratch_bytes(ugsdr_ctx* ctx, const JobLaunchShape& s) {
 		AcqParams base{};
-		base.n = n;
-		LargeParams p = large_params(ctx, base, n, smem);
-		set_smem(acq_inverse_large_kernel, smem);
-		const int grid = resident_grid(ctx, acq_inverse_large_kernel, kLargeThreads, smem);
-		(void)p;
-		return sizeof(float2) * slab_elems(n, m) * grid;
+		base.n = s.n;
+		const BatchedParams p = batched_params(ctx, base, s.n);
+		const size_t r = batch_rows(s);
+		const size_t chunks = chunks_of(p.n2, p.cw);
+		size_t bytes = sizeof(float2) * r * s.k * s.n;                     // B
+		bytes += (sizeof(float4) + sizeof(double2)) * r * chunks + 256;   // partials, sums
+		bytes += sizeof(unsigned int) * r + 256;                          // counters
+		if (s.fold_mode) {
+			bytes += sizeof(float) * r * s.m + 256;                       // accg
+			if (s.fold_mode == 2)
+				bytes += sizeof(float2) * r * s.k * s.m + 256;            // zcg
+		}
+		return bytes;
 	}
 
 	void large_code_spectrum(ugsdr_ctx* ctx, CodeEntry& e, const float* chips_dev, size_t n_chips, size_t repeats,
@@ -181,44 +222,68 @@ namespace ugsdr_gpu {
 		AcqParams base{};
 		base.n = static_cast<int>(e.n);
 		base.one_sided = e.spectrum_mode == UGSDR_SPECTRUM_ONE_SIDED;
-		size_t smem = 0;
-		LargeParams p = large_params(ctx, base, base.n, smem);
+		BatchedParams p = batched_params(ctx, base, base.n);
+		DevBuf mask;
+		mask.reserve(sizeof(uint32_t));
+		UG_CUDA(cudaMemcpyAsync(mask.ptr, &sign_mask, sizeof(uint32_t), cudaMemcpyHostToDevice, ctx->stream));
+		p.code_mode = 1;
 		p.chips = chips_dev;
 		p.n_chips = static_cast<int>(n_chips);
+		p.chip_stride = static_cast<int>(n_chips);
 		p.repeats = static_cast<int>(repeats);
-		p.sign_mask = sign_mask;
 		p.sign_segment = static_cast<int>(sign_segment);
-		p.code_out = e.spectrum.as<float2>();
-		set_smem(code_spectrum_large_kernel, smem);
-		code_spectrum_large_kernel<<<1, kLargeThreads, smem, ctx->stream>>>(p);
-		note_launch(ctx);
+		p.sign_masks = mask.as<uint32_t>();
+		p.out = e.spectrum.as<float2>();
+		launch_forward(ctx, UGSDR_SAMPLES_CF32, p, 1);
+		UG_CUDA(cudaStreamSynchronize(ctx->stream));
 	}
 
-	void large_job(ugsdr_ctx* ctx, const ugsdr_acq_job& job, const AcqParams& base, int n, float2* slab) {
-		size_t smem = 0;
-		LargeParams p = large_params(ctx, base, n, smem);
+	void large_job(ugsdr_ctx* ctx, const ugsdr_acq_job& job, const AcqParams& base, const JobLaunchShape& s, char* scratch) {
+		BatchedParams p = batched_params(ctx, base, s.n);
 		const int items = base.n_doppler * base.k_blocks;
-		auto launch_fwd = [&](auto kernel) {
-			set_smem(kernel, smem);
-			const int grid = std::min(items, resident_grid(ctx, kernel, kLargeThreads, smem));
+		p.out = base.spectra;
+		{
 			KernelTimer timer(ctx, "acq_forward_large");
-			kernel<<<grid, kLargeThreads, smem, ctx->stream>>>(p);
-		};
-		switch (job.sample_type) {
-		case UGSDR_SAMPLES_CF32: launch_fwd(acq_forward_large_kernel<UGSDR_SAMPLES_CF32>); break;
-		case UGSDR_SAMPLES_CI8: launch_fwd(acq_forward_large_kernel<UGSDR_SAMPLES_CI8>); break;
-		case UGSDR_SAMPLES_CI16: launch_fwd(acq_forward_large_kernel<UGSDR_SAMPLES_CI16>); break;
-		default: launch_fwd(acq_forward_large_kernel<UGSDR_SAMPLES_RI8>); break;
+			launch_forward(ctx, job.sample_type, p, items);
 		}
-		note_launch(ctx);
-		p.slab = slab;
-		p.slab_elems = slab_elems(n, base.m);
-		set_smem(acq_inverse_large_kernel, smem);
-		const int rows = base.n_doppler * base.n_codes;
-		const int grid = std::min(rows, resident_grid(ctx, acq_inverse_large_kernel, kLargeThreads, smem));
+		const int r_max = batch_rows(s);
+		const int chunks = chunks_of(p.n2, p.cw);
+		char* at = scratch;
+		auto carve = [&](size_t bytes) {
+			char* q = at;
+			at += (bytes + 255) / 256 * 256;
+			return q;
+		};
+		p.bbuf = reinterpret_cast<float2*>(carve(sizeof(float2) * static_cast<size_t>(r_max) * s.k * s.n));
+		p.partials = reinterpret_cast<float4*>(carve(sizeof(float4) * static_cast<size_t>(r_max) * chunks));
+		p.sums = reinterpret_cast<double2*>(carve(sizeof(double2) * static_cast<size_t>(r_max) * chunks));
+		p.counters = reinterpret_cast<unsigned int*>(carve(sizeof(unsigned int) * r_max));
+		if (s.fold_mode) {
+			p.accg = reinterpret_cast<float*>(carve(sizeof(float) * static_cast<size_t>(r_max) * s.m));
+			if (s.fold_mode == 2)
+				p.zcg = reinterpret_cast<float2*>(carve(sizeof(float2) * static_cast<size_t>(r_max) * s.k * s.m));
+		}
+		const size_t smem_r = smem_rows(p, true), smem_c = smem_cols(p, true);
+		set_smem(inv_rows_kernel, smem_r);
+		set_smem(inv_cols_kernel, smem_c);
 		KernelTimer timer(ctx, "acq_inverse_large");
-		acq_inverse_large_kernel<<<grid, kLargeThreads, smem, ctx->stream>>>(p);
-		note_launch(ctx);
+		for (int row0 = 0; row0 < s.rows; row0 += r_max) {
+			p.row0 = row0;
+			p.rows = std::min(r_max, s.rows - row0);
+			UG_CUDA(cudaMemsetAsync(p.counters, 0, sizeof(unsigned int) * p.rows, ctx->stream));
+			if (s.fold_mode) {
+				UG_CUDA(cudaMemsetAsync(p.accg, 0, sizeof(float) * static_cast<size_t>(p.rows) * s.m, ctx->stream));
+				if (s.fold_mode == 2)
+					UG_CUDA(cudaMemsetAsync(p.zcg, 0, sizeof(float2) * static_cast<size_t>(p.rows) * s.k * s.m, ctx->stream));
+			}
+			inv_rows_kernel<<<p.rows * s.k * chunks_of(p.n1, p.rw), kBatchedThreads, smem_r, ctx->stream>>>(p);
+			inv_cols_kernel<<<p.rows * chunks, kBatchedThreads, smem_c, ctx->stream>>>(p);
+			note_launch(ctx, 2);
+			if (s.fold_mode) {
+				fold_finish_kernel<<<p.rows, kBatchedThreads, 0, ctx->stream>>>(p);
+				note_launch(ctx);
+			}
+		}
 	}
 
 	namespace {
@@ -260,6 +325,16 @@ namespace ugsdr_gpu {
 	};
 
 	namespace {
+		JobLaunchShape shape_of(const JobLaunch& L) {
+			JobLaunchShape s;
+			s.n = L.n;
+			s.k = L.k;
+			s.m = L.m;
+			s.rows = static_cast<int>(L.grid.size()) * L.n_codes;
+			s.fold_mode = L.fold_mode;
+			return s;
+		}
+
 		JobLaunch validate(ugsdr_ctx* ctx, const ugsdr_acq_job& job) {
 			JobLaunch L;
 			require(job.samples != nullptr, "null samples");
@@ -309,7 +384,7 @@ namespace ugsdr_gpu {
 	// Launches one job on ctx->stream; cells/best_bin stay on the device.
 	void launch_job(ugsdr_ctx* ctx, const ugsdr_acq_job& job, const JobLaunch& L, const void* dev_samples,
 		AcqCellDev* cells, int* best_bin, uint32_t* adders_dev, const float2** code_ptrs_dev, float2* spectra,
-		float2* slab) {
+		char* scratch) {
 		AcqParams p{};
 		p.samples = dev_samples;
 		p.n = L.n;
@@ -363,7 +438,7 @@ namespace ugsdr_gpu {
 			note_launch(ctx);
 		}
 		else {
-			large_job(ctx, job, p, L.n, slab);
+			large_job(ctx, job, p, shape_of(L), scratch);
 		}
 		acq_select_kernel<<<(L.n_codes + 127) / 128, 128, 0, ctx->stream>>>(cells, L.n_codes, p.n_doppler, best_bin);
 		note_launch(ctx);
@@ -387,7 +462,7 @@ namespace ugsdr_gpu {
 			cells_n += static_cast<size_t>(L.n_codes) * L.grid.size();
 			params_b += (L.grid.size() * sizeof(uint32_t) + L.n_codes * sizeof(void*) + L.n_codes * sizeof(int) + 512) / 256 * 256;
 			if (L.large)
-				slab_b = std::max(slab_b, large_slab_bytes(ctx, L.n, L.m));
+				slab_b = std::max(slab_b, batched_scratch_bytes(ctx, shape_of(L)));
 		}
 		ctx->samples.reserve(std::max<size_t>(samples_bytes, 256));
 		ctx->spectra.reserve(spectra_b);
@@ -449,7 +524,7 @@ namespace ugsdr_gpu {
 			o = (o + 15) / 16 * 16;
 			auto* best = reinterpret_cast<int*>(dp + o);
 			launch_job(ctx, jobs[j], L, dev_samples[j], ctx->cells.as<AcqCellDev>() + c_offsets[j], best, adders,
-				code_ptrs, ctx->spectra.as<float2>(), ctx->slab.as<float2>());
+				code_ptrs, ctx->spectra.as<float2>(), ctx->slab.as<char>());
 		}
 
 		// gather

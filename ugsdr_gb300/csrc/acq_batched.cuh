@@ -1,0 +1,371 @@
+// Large-N acquisition as batched two-stage transforms.
+//
+// For block sizes above one CTA's shared memory (N = 50,000 at 50 MHz / 1 ms,
+// 200,000 at 4 ms, 204,600 for L5 at 20.46 MHz / 10 ms, up to 1,000,000) the
+// N-point transform is split N = N1 * N2 (four-step) and each step is one
+// kernel over every sub-transform of a batch, so every launch has thousands
+// of independent CTAs:
+//   forward   fwd_cols  x[N2 n1 + n2] -> N1-point FFTs over n1, times W_N^{n2 k1}
+//             fwd_rows  N2-point FFTs over n2 -> X_T[k1][k2] = X[k1 + N1 k2]
+//   inverse   inv_rows  Z_T = X_T * C_T -> N2-point IFFTs over k2, times W_N^{-n2 k1}
+//                       -> B[row][block][k1][n2]
+//             inv_cols  per (row, column chunk): for each block (the next
+//                       block's tile prefetched with cp.async while the current
+//                       one is transformed), N1-point IFFTs over k1 ->
+//                       y[N2 n1 + n2] -> |.| or |.|^2 accumulated over the K
+//                       blocks in shared memory -> chunk partial (first max,
+//                       sum, sum of squares); the last CTA of a row combines
+//                       the partials into the row's cell.
+// Folded outputs (reshape, fse.hpp:209-218) accumulate through atomics into a
+// per-row buffer reduced by a finishing kernel.
+// Spectra (signal and code) stay in the k1-major layout X_T, so the pointwise
+// product needs no transpose; only bins k <= N/2 are written/read one-sided.
+#pragma once
+
+#include "acq_kernels.cuh"
+
+namespace ugsdr_gpu {
+
+	// Stockham passes over `batch` FFTs laid out at a[f * ld + i] (whole CTA).
+	template <bool INV>
+	__device__ float2* passes_batch(float2* a, float2* b, const FftPlanDev& plan, int batch, int ld) {
+		int ns = 1;
+		const int n = plan.n;
+		for (int s = 0; s < plan.n_pass; ++s) {
+			const int r = plan.radix[s];
+			const int nb = n / r;
+			const int total = nb * batch;
+			const float inv_nb = 1.0f / static_cast<float>(nb), inv_ns = 1.0f / static_cast<float>(ns);
+			for (int u = threadIdx.x; u < total; u += blockDim.x) {
+				const int f = fdiv(u, inv_nb);
+				const int j = u - f * nb;
+				butterfly_dispatch<INV>(r, a + f * ld, b + f * ld, n, ns, plan.tw, j, j - fdiv(j, inv_ns) * ns);
+			}
+			__syncthreads();
+			float2* t = a;
+			a = b;
+			b = t;
+			ns *= r;
+		}
+		return a;
+	}
+
+	// W_N^e (conjugated when inv) for 0 <= e < N: sincospi of 2 e' / N with
+	// e' = e or e - N reduced to (-N/2, N/2] (float argument error < 2^-24 of
+	// the angle; the inter-step twiddle's contribution stays near 1e-7).
+	__device__ __forceinline__ float2 tw_n(uint32_t e, uint32_t n, float inv_n2, bool inv) {
+		const int32_t er = e > n / 2 ? static_cast<int32_t>(e) - static_cast<int32_t>(n) : static_cast<int32_t>(e);
+		float s, c;
+		sincospif(static_cast<float>(er) * inv_n2, &s, &c);
+		return c2(c, inv ? s : -s);
+	}
+
+	__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+		const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+		asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem));
+	}
+	__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+	__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+	struct BatchedParams {
+		AcqParams base;         // n, k_blocks, n_doppler, n_codes, m, fold_mode, stat, one_sided, adders, lut, spectra, codes, cells
+		FftPlanDev p1, p2;      // N1-point, N2-point plans
+		int n1, n2;
+		int cw, rw;             // columns per column-kernel CTA (power of two), rows per row-kernel CTA
+		int cw_shift;           // log2(cw)
+		int ld1;                // column-tile stride: N1 rounded up to odd (conflict-free smem)
+		// forward / code items
+		int code_mode;          // 1: items are codes (chips -> spectra), 0: signal (Doppler, block)
+		const float* chips;     // code mode: chips of code `item` at chips + item * chip_stride
+		int n_chips, chip_stride, repeats, sign_segment;
+		const uint32_t* sign_masks;
+		float2* out;            // forward output base (item * N)
+		// inverse batch
+		int row0, rows;         // rows [row0, row0 + rows) of (code fastest, Doppler) in this batch
+		float2* bbuf;           // B[row - row0][block][N]
+		float4* partials;       // [row - row0][chunk]: (max, index bits, -, -)
+		double2* sums;          // [row - row0][chunk]: (sum, sum of squares)
+		unsigned int* counters; // [row - row0], zeroed per batch
+		float* accg;            // fold modes: [row - row0][M]
+		float2* zcg;            // fold mode 2: [row - row0][block][M]
+	};
+
+	// ------------------------------------------------------------- forward
+	template <int ST>
+	__device__ __forceinline__ float2 fwd_load(const BatchedParams& p, int item, int64_t i, const float* lut) {
+		if (p.code_mode) {
+			const float* chips = p.chips + static_cast<size_t>(item) * p.chip_stride;
+			const uint32_t mask = p.sign_masks ? p.sign_masks[item] : 0u;
+			return c2(code_sample(chips, p.n_chips, p.repeats, p.base.n, static_cast<int>(i), mask, p.sign_segment), 0.f);
+		}
+		const int d = item / p.base.k_blocks;
+		const int blk = item - d * p.base.k_blocks;
+		const uint64_t g = static_cast<uint64_t>(blk) * p.base.n + static_cast<uint64_t>(i);
+		float2 v = load_sample<ST>(p.base.samples, g);
+		if (p.base.fe_on)
+			v = table_mix(v, g, p.base.fe_adder, 0u, lut);
+		return table_mix(v, g, p.base.adders[d], p.base.phase0, lut);
+	}
+
+	// grid: items * ceil(N2 / cw)
+	template <int ST>
+	__global__ void __launch_bounds__(256, 3) fwd_cols_kernel(BatchedParams p) {
+		extern __shared__ float2 smem[];
+		__shared__ float lut[80];
+		if (threadIdx.x < 80 && p.base.lut)
+			lut[threadIdx.x] = p.base.lut[threadIdx.x];
+		__syncthreads();
+		const int n1 = p.n1, n2 = p.n2;
+		const int chunks = (n2 + p.cw - 1) >> p.cw_shift;
+		const int item = blockIdx.x / chunks;
+		const int c0 = (blockIdx.x - item * chunks) << p.cw_shift;
+		const int cw = min(p.cw, n2 - c0);
+		const int ld = p.ld1;
+		const int mask = p.cw - 1;
+		float2* a = smem;
+		float2* b = smem + p.cw * ld;
+		// consecutive threads take consecutive columns of one n1 row: coalesced reads
+		for (int e = threadIdx.x; e < p.cw * n1; e += blockDim.x) {
+			const int f = e & mask, i1 = e >> p.cw_shift;
+			if (f < cw)
+				a[f * ld + i1] = fwd_load<ST>(p, item, static_cast<int64_t>(n2) * i1 + c0 + f, lut);
+		}
+		__syncthreads();
+		const float2* y = passes_batch<false>(a, b, p.p1, cw, ld);
+		float2* out = p.out + static_cast<size_t>(item) * p.base.n;
+		const float inv_n2 = 2.0f / static_cast<float>(p.base.n);
+		for (int e = threadIdx.x; e < p.cw * n1; e += blockDim.x) {
+			const int f = e & mask, k1 = e >> p.cw_shift;
+			if (f < cw)
+				out[static_cast<size_t>(k1) * n2 + c0 + f] =
+					cmul(y[f * ld + k1], tw_n(static_cast<uint32_t>(c0 + f) * static_cast<uint32_t>(k1), p.base.n, inv_n2, false));
+		}
+	}
+
+	// grid: items * ceil(N1 / rw); code mode also conjugates and masks (conj(FFT(code)))
+	__global__ void __launch_bounds__(256, 3) fwd_rows_kernel(BatchedParams p) {
+		extern __shared__ float2 smem[];
+		const int n1 = p.n1, n2 = p.n2;
+		const int chunks = (n1 + p.rw - 1) / p.rw;
+		const int item = blockIdx.x / chunks;
+		const int r0 = (blockIdx.x - item * chunks) * p.rw;
+		const int rw = min(p.rw, n1 - r0);
+		float2* a = smem;
+		float2* b = smem + p.rw * n2;
+		float2* out = p.out + static_cast<size_t>(item) * p.base.n + static_cast<size_t>(r0) * n2;
+		for (int e = threadIdx.x; e < rw * n2; e += blockDim.x)
+			a[e] = out[e];
+		__syncthreads();
+		const float2* y = passes_batch<false>(a, b, p.p2, rw, n2);
+		const int half = p.base.n / 2;
+		const float inv_n2f = 1.0f / static_cast<float>(n2);
+		for (int e = threadIdx.x; e < rw * n2; e += blockDim.x) {
+			const int ri = fdiv(e, inv_n2f), k2 = e - ri * n2;
+			const int64_t k = (r0 + ri) + static_cast<int64_t>(n1) * k2;
+			const bool zero = p.base.one_sided && k > half;
+			if (p.code_mode) {
+				const float2 v = y[e];
+				out[e] = zero ? c2(0.f, 0.f) : c2(v.x, -v.y);
+			}
+			else if (!zero) {
+				out[e] = y[e];  // bins above N/2 are never read in one-sided mode
+			}
+		}
+	}
+
+	// ------------------------------------------------------------- inverse
+	// grid: rows * K * ceil(N1 / rw)
+	__global__ void __launch_bounds__(256, 3) inv_rows_kernel(BatchedParams p) {
+		extern __shared__ float2 smem[];
+		const AcqParams& q = p.base;
+		const int n1 = p.n1, n2 = p.n2, n = q.n;
+		const int chunks = (n1 + p.rw - 1) / p.rw;
+		const int item = blockIdx.x / chunks;       // (local row, block)
+		const int r0 = (blockIdx.x - item * chunks) * p.rw;
+		const int rw = min(p.rw, n1 - r0);
+		const int lrow = item / q.k_blocks;
+		const int blk = item - lrow * q.k_blocks;
+		const int row = p.row0 + lrow;
+		const int c = row % q.n_codes;
+		const int d = row / q.n_codes;
+		const float2* x = q.spectra + (static_cast<size_t>(d) * q.k_blocks + blk) * n + static_cast<size_t>(r0) * n2;
+		const float2* code = q.codes[c] + static_cast<size_t>(r0) * n2;
+		float2* a = smem;
+		float2* b = smem + p.rw * n2;
+		const int half = n / 2;
+		const float inv_n2f = 1.0f / static_cast<float>(n2);
+		for (int e = threadIdx.x; e < rw * n2; e += blockDim.x) {
+			const int ri = fdiv(e, inv_n2f), k2 = e - ri * n2;
+			const int64_t k = (r0 + ri) + static_cast<int64_t>(n1) * k2;
+			a[e] = (q.one_sided && k > half) ? c2(0.f, 0.f) : cmul(__ldg(x + e), __ldg(code + e));
+		}
+		__syncthreads();
+		const float2* y = passes_batch<true>(a, b, p.p2, rw, n2);
+		float2* out = p.bbuf + static_cast<size_t>(item) * n + static_cast<size_t>(r0) * n2;
+		const float inv_n2 = 2.0f / static_cast<float>(n);
+		for (int e = threadIdx.x; e < rw * n2; e += blockDim.x) {
+			const int ri = fdiv(e, inv_n2f), i2 = e - ri * n2;
+			out[e] = cmul(y[e], tw_n(static_cast<uint32_t>(i2) * static_cast<uint32_t>(r0 + ri), n, inv_n2, true));
+		}
+	}
+
+	// grid: rows * ceil(N2 / cw); shared: 3 * cw * ld1 float2 (input, work, prefetch) + cw * ld1 float
+	__global__ void __launch_bounds__(256, 2) inv_cols_kernel(BatchedParams p) {
+		extern __shared__ float2 smem[];
+		__shared__ MaxIdx s_max[8];
+		__shared__ double s_sum[8], s_sq[8];
+		__shared__ bool s_last;
+		const AcqParams& q = p.base;
+		const int n1 = p.n1, n2 = p.n2, n = q.n, m = q.m;
+		const int chunks = (n2 + p.cw - 1) >> p.cw_shift;
+		const int lrow = blockIdx.x / chunks;
+		const int chunk = blockIdx.x - lrow * chunks;
+		const int c0 = chunk << p.cw_shift;
+		const int cw = min(p.cw, n2 - c0);
+		const int ld = p.ld1;
+		const int mask = p.cw - 1;
+		const int tile = p.cw * ld;
+		float2* in = smem;
+		float2* work = smem + tile;
+		float2* pre = smem + 2 * tile;
+		float* acc = reinterpret_cast<float*>(smem + 3 * tile);
+		const float inv_n = 1.0f / static_cast<float>(n);
+		const float post = q.one_sided ? 2.0f : 1.0f;
+		const float inv_n1 = 1.0f / static_cast<float>(n1);
+		for (int e = threadIdx.x; e < tile; e += blockDim.x)
+			acc[e] = 0.f;
+		auto prefetch = [&](float2* dst, int blk) {
+			const float2* bsrc = p.bbuf + (static_cast<size_t>(lrow) * q.k_blocks + blk) * n + c0;
+			for (int e = threadIdx.x; e < p.cw * n1; e += blockDim.x) {
+				const int f = e & mask, k1 = e >> p.cw_shift;
+				if (f < cw)
+					cp_async8(dst + f * ld + k1, bsrc + static_cast<size_t>(k1) * n2 + f);
+			}
+			cp_async_commit();
+		};
+		prefetch(in, 0);
+		for (int blk = 0; blk < q.k_blocks; ++blk) {
+			cp_async_wait_all();
+			__syncthreads();
+			if (blk + 1 < q.k_blocks)
+				prefetch(pre, blk + 1);
+			const float2* y = passes_batch<true>(in, work, p.p1, cw, ld);
+			if (q.fold_mode == 0) {
+				for (int e = threadIdx.x; e < cw * n1; e += blockDim.x) {
+					const int f = fdiv(e, inv_n1), i1 = e - f * n1;
+					acc[f * ld + i1] += stat_of(cscale(cscale(y[f * ld + i1], inv_n), post), q.stat);
+				}
+			}
+			else if (q.fold_mode == 1) {
+				float* ag = p.accg + static_cast<size_t>(lrow) * m;
+				for (int e = threadIdx.x; e < cw * n1; e += blockDim.x) {
+					const int f = fdiv(e, inv_n1), i1 = e - f * n1;
+					const uint32_t tau = static_cast<uint32_t>(n2) * i1 + c0 + f;
+					atomicAdd(ag + tau % static_cast<uint32_t>(m), stat_of(cscale(cscale(y[f * ld + i1], inv_n), post), q.stat));
+				}
+			}
+			else {
+				float2* zg = p.zcg + (static_cast<size_t>(lrow) * q.k_blocks + blk) * m;
+				for (int e = threadIdx.x; e < cw * n1; e += blockDim.x) {
+					const int f = fdiv(e, inv_n1), i1 = e - f * n1;
+					const uint32_t tau = static_cast<uint32_t>(n2) * i1 + c0 + f;
+					const float2 v = cscale(cscale(y[f * ld + i1], inv_n), post);
+					float2* z = zg + tau % static_cast<uint32_t>(m);
+					atomicAdd(&z->x, v.x);
+					atomicAdd(&z->y, v.y);
+				}
+			}
+			__syncthreads();
+			float2* t = in;  // the consumed input buffer receives the block after next
+			in = pre;
+			pre = t;
+		}
+		if (q.fold_mode != 0)
+			return;
+		// chunk partial: first max (lowest natural index on ties), sum, sum of squares
+		MaxIdx best{-1.0f, 0xFFFFFFFFu};
+		float sum = 0.f, sq = 0.f;
+		for (int e = threadIdx.x; e < cw * n1; e += blockDim.x) {
+			const int f = fdiv(e, inv_n1), i1 = e - f * n1;
+			const float v = acc[f * ld + i1];
+			const MaxIdx cand{v, static_cast<uint32_t>(n2) * i1 + c0 + f};
+			best = better(best, cand);
+			sum += v;
+			sq += v * v;
+		}
+		double dsum = sum, dsq = sq;
+		for (int o = 16; o > 0; o >>= 1) {
+			const MaxIdx other{__shfl_down_sync(0xffffffffu, best.v, o), __shfl_down_sync(0xffffffffu, best.i, o)};
+			best = better(best, other);
+			dsum += __shfl_down_sync(0xffffffffu, dsum, o);
+			dsq += __shfl_down_sync(0xffffffffu, dsq, o);
+		}
+		const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+		if (lane == 0) {
+			s_max[warp] = best;
+			s_sum[warp] = dsum;
+			s_sq[warp] = dsq;
+		}
+		__syncthreads();
+		if (threadIdx.x == 0) {
+			for (int w = 1; w < (blockDim.x + 31) / 32; ++w) {
+				s_max[0] = better(s_max[0], s_max[w]);
+				s_sum[0] += s_sum[w];
+				s_sq[0] += s_sq[w];
+			}
+			const size_t slot = static_cast<size_t>(lrow) * chunks + chunk;
+			p.partials[slot] = make_float4(s_max[0].v, __uint_as_float(s_max[0].i), 0.f, 0.f);
+			p.sums[slot] = make_double2(s_sum[0], s_sq[0]);
+			__threadfence();
+			s_last = atomicAdd(p.counters + lrow, 1u) == static_cast<unsigned>(chunks - 1);
+		}
+		__syncthreads();
+		if (!s_last || threadIdx.x != 0)
+			return;
+		// last chunk of this row: combine every chunk's partial into the cell
+		__threadfence();
+		MaxIdx rb{-1.0f, 0xFFFFFFFFu};
+		double ts = 0, tq = 0;
+		for (int k = 0; k < chunks; ++k) {
+			const size_t slot = static_cast<size_t>(lrow) * chunks + k;
+			const float4 pt = __ldcg(p.partials + slot);
+			const double2 sm = __ldcg(p.sums + slot);
+			rb = better(rb, MaxIdx{pt.x, __float_as_uint(pt.y)});
+			ts += sm.x;
+			tq += sm.y;
+		}
+		const int row = p.row0 + lrow;
+		const int c = row % q.n_codes;
+		const int d = row / q.n_codes;
+		const double mean = ts / m;
+		const double var = m > 1 ? (tq - ts * mean) / (m - 1) : 0.0;
+		AcqCellDev cell;
+		cell.level = rb.v;
+		cell.index = rb.i;
+		cell.mean = static_cast<float>(mean);
+		cell.std = static_cast<float>(sqrt(var > 0 ? var : 0.0));
+		q.cells[static_cast<size_t>(c) * q.n_doppler + d] = cell;
+	}
+
+	// folded rows: acc (fold 1) or |complex fold| summed over blocks (fold 2) -> cell; grid: rows
+	__global__ void __launch_bounds__(256) fold_finish_kernel(BatchedParams p) {
+		const AcqParams& q = p.base;
+		const int lrow = blockIdx.x;
+		const int m = q.m;
+		float* ag = p.accg + static_cast<size_t>(lrow) * m;
+		if (q.fold_mode == 2) {
+			const float2* zg = p.zcg + static_cast<size_t>(lrow) * q.k_blocks * m;
+			for (int i = threadIdx.x; i < m; i += blockDim.x) {
+				float s = 0.f;
+				for (int blk = 0; blk < q.k_blocks; ++blk)
+					s += stat_of(zg[static_cast<size_t>(blk) * m + i], q.stat);
+				ag[i] = s;
+			}
+			__syncthreads();
+		}
+		const int row = p.row0 + lrow;
+		const int c = row % q.n_codes;
+		const int d = row / q.n_codes;
+		reduce_cell(ag, m, q.cells + static_cast<size_t>(c) * q.n_doppler + d);
+	}
+}

@@ -78,8 +78,9 @@ namespace ugsdr_gpu {
 		for (int s = 0; s < plan.n_pass; ++s) {
 			const int r = plan.radix[s];
 			const int nb = plan.n / r;
+			const float inv_ns = 1.0f / static_cast<float>(ns);
 			for (int j = threadIdx.x; j < nb; j += blockDim.x)
-				butterfly_dispatch<INV>(r, a, b, plan.n, ns, plan.tw, j);
+				butterfly_dispatch<INV>(r, a, b, plan.n, ns, plan.tw, j, j - fdiv(j, inv_ns) * ns);
 			__syncthreads();
 			float2* t = a;
 			a = b;

@@ -265,23 +265,25 @@ namespace ugsdr_gpu {
 	//   v[r] = in[j + r N/R] * W_{Ns R}^{r (j mod Ns)},  DFT_R(v),
 	//   out[(j / Ns) Ns R + (j mod Ns) + r Ns] = v[r].
 	// tw[m] = exp(-2 pi i m / N) (conjugated for the inverse).
+	// k = j mod ns is passed in (callers divide with a float reciprocal).
 	template <int R, bool INV>
-	UG_HD void stockham_load(const float2* in, int n, int ns, const float2* tw, int j, float2* v) {
+	UG_HD void stockham_load(const float2* in, int n, int ns, const float2* tw, int j, int k, float2* v) {
 		const int stride = n / R;
-		const int k = j % ns;
+#pragma unroll
+		for (int r = 0; r < R; ++r)
+			v[r] = in[j + r * stride];
+		if (ns == 1)
+			return;  // first pass: every twiddle is 1
 		const int tw_step = (n / (ns * R)) * k;  // twiddle exponent per r, in units of 1/N
-		v[0] = in[j];
 #pragma unroll
 		for (int r = 1; r < R; ++r) {
-			const float2 x = in[j + r * stride];
 			const float2 w = tw[r * tw_step];
-			v[r] = INV ? cmulc(x, w) : cmul(x, w);
+			v[r] = INV ? cmulc(v[r], w) : cmul(v[r], w);
 		}
 	}
 
 	template <int R>
-	UG_HD void stockham_store(float2* out, int ns, int j, const float2* v) {
-		const int k = j % ns;
+	UG_HD void stockham_store(float2* out, int ns, int j, int k, const float2* v) {
 		const int base = (j - k) * R + k;
 #pragma unroll
 		for (int r = 0; r < R; ++r)
@@ -289,39 +291,44 @@ namespace ugsdr_gpu {
 	}
 
 	template <int R, bool INV>
-	UG_HD void stockham_butterfly(const float2* in, float2* out, int n, int ns, const float2* tw, int j) {
+	UG_HD void stockham_butterfly(const float2* in, float2* out, int n, int ns, const float2* tw, int j, int k) {
 		float2 v[R];
-		stockham_load<R, INV>(in, n, ns, tw, j, v);
+		stockham_load<R, INV>(in, n, ns, tw, j, k, v);
 		Dft<R, INV>::run(v);
-		stockham_store<R>(out, ns, j, v);
+		stockham_store<R>(out, ns, j, k, v);
 	}
+
+	// floor(a / b) for 0 <= a < 2^20, b >= 1, from inv_b = 1.0f / b:
+	// (a + 0.5) / b is at least 0.5 / b away from an integer and the float
+	// product errs by less than 2^20 / b * 2^-23 = 2^-3 / b, so truncation is exact.
+	UG_HD int fdiv(int a, float inv_b) { return static_cast<int>((static_cast<float>(a) + 0.5f) * inv_b); }
 
 	// Runtime dispatch of one butterfly; returns false for an unsupported radix.
 	template <bool INV>
-	UG_HD bool butterfly_dispatch(int radix, const float2* in, float2* out, int n, int ns, const float2* tw, int j) {
+	UG_HD bool butterfly_dispatch(int radix, const float2* in, float2* out, int n, int ns, const float2* tw, int j, int k) {
 		switch (radix) {
-		case 2: stockham_butterfly<2, INV>(in, out, n, ns, tw, j); return true;
-		case 3: stockham_butterfly<3, INV>(in, out, n, ns, tw, j); return true;
-		case 4: stockham_butterfly<4, INV>(in, out, n, ns, tw, j); return true;
-		case 5: stockham_butterfly<5, INV>(in, out, n, ns, tw, j); return true;
-		case 6: stockham_butterfly<6, INV>(in, out, n, ns, tw, j); return true;
-		case 7: stockham_butterfly<7, INV>(in, out, n, ns, tw, j); return true;
-		case 8: stockham_butterfly<8, INV>(in, out, n, ns, tw, j); return true;
-		case 9: stockham_butterfly<9, INV>(in, out, n, ns, tw, j); return true;
-		case 10: stockham_butterfly<10, INV>(in, out, n, ns, tw, j); return true;
-		case 11: stockham_butterfly<11, INV>(in, out, n, ns, tw, j); return true;
-		case 12: stockham_butterfly<12, INV>(in, out, n, ns, tw, j); return true;
-		case 13: stockham_butterfly<13, INV>(in, out, n, ns, tw, j); return true;
-		case 16: stockham_butterfly<16, INV>(in, out, n, ns, tw, j); return true;
-		case 17: stockham_butterfly<17, INV>(in, out, n, ns, tw, j); return true;
-		case 19: stockham_butterfly<19, INV>(in, out, n, ns, tw, j); return true;
-		case 20: stockham_butterfly<20, INV>(in, out, n, ns, tw, j); return true;
-		case 23: stockham_butterfly<23, INV>(in, out, n, ns, tw, j); return true;
-		case 25: stockham_butterfly<25, INV>(in, out, n, ns, tw, j); return true;
-		case 27: stockham_butterfly<27, INV>(in, out, n, ns, tw, j); return true;
-		case 29: stockham_butterfly<29, INV>(in, out, n, ns, tw, j); return true;
-		case 31: stockham_butterfly<31, INV>(in, out, n, ns, tw, j); return true;
-		case 32: stockham_butterfly<32, INV>(in, out, n, ns, tw, j); return true;
+		case 2: stockham_butterfly<2, INV>(in, out, n, ns, tw, j, k); return true;
+		case 3: stockham_butterfly<3, INV>(in, out, n, ns, tw, j, k); return true;
+		case 4: stockham_butterfly<4, INV>(in, out, n, ns, tw, j, k); return true;
+		case 5: stockham_butterfly<5, INV>(in, out, n, ns, tw, j, k); return true;
+		case 6: stockham_butterfly<6, INV>(in, out, n, ns, tw, j, k); return true;
+		case 7: stockham_butterfly<7, INV>(in, out, n, ns, tw, j, k); return true;
+		case 8: stockham_butterfly<8, INV>(in, out, n, ns, tw, j, k); return true;
+		case 9: stockham_butterfly<9, INV>(in, out, n, ns, tw, j, k); return true;
+		case 10: stockham_butterfly<10, INV>(in, out, n, ns, tw, j, k); return true;
+		case 11: stockham_butterfly<11, INV>(in, out, n, ns, tw, j, k); return true;
+		case 12: stockham_butterfly<12, INV>(in, out, n, ns, tw, j, k); return true;
+		case 13: stockham_butterfly<13, INV>(in, out, n, ns, tw, j, k); return true;
+		case 16: stockham_butterfly<16, INV>(in, out, n, ns, tw, j, k); return true;
+		case 17: stockham_butterfly<17, INV>(in, out, n, ns, tw, j, k); return true;
+		case 19: stockham_butterfly<19, INV>(in, out, n, ns, tw, j, k); return true;
+		case 20: stockham_butterfly<20, INV>(in, out, n, ns, tw, j, k); return true;
+		case 23: stockham_butterfly<23, INV>(in, out, n, ns, tw, j, k); return true;
+		case 25: stockham_butterfly<25, INV>(in, out, n, ns, tw, j, k); return true;
+		case 27: stockham_butterfly<27, INV>(in, out, n, ns, tw, j, k); return true;
+		case 29: stockham_butterfly<29, INV>(in, out, n, ns, tw, j, k); return true;
+		case 31: stockham_butterfly<31, INV>(in, out, n, ns, tw, j, k); return true;
+		case 32: stockham_butterfly<32, INV>(in, out, n, ns, tw, j, k); return true;
 		default: return false;
 		}
 	}

@@ -1,6 +1,7 @@
 // Radix planning shared by the engine and the host-side FFT check.
 #pragma once
 
+#include <algorithm>
 #include <functional>
 #include <vector>
 
@@ -37,6 +38,9 @@ namespace ugsdr_gpu {
 			}
 		};
 		dfs(n);
+		// Odd radices first: the first Stockham pass stores with a stride of R
+		// elements, which is conflict-free in shared memory only for odd R.
+		std::stable_sort(best.begin(), best.end(), [](int a, int b) { return (a & 1) > (b & 1); });
 		return !best.empty();
 	}
 }

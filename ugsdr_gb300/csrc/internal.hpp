@@ -77,6 +77,9 @@ namespace ugsdr_gpu {
 		int n1 = 0, n2 = 0;
 		FftPlanDesc p1, p2;    // N1-point and N2-point plans
 		const float2* tw = nullptr;  // N-point table for the inter-step twiddle
+		// two-level table: W_N^e = hi[e >> 8] * lo[e & 255]; lo has 256 entries, hi n_hi
+		const float2* tw_lohi = nullptr;
+		int n_hi = 0;
 	};
 
 	struct CodeEntry {
@@ -99,6 +102,7 @@ struct ugsdr_ctx {
 
 	// twiddle tables and plans per size
 	std::map<int, std::unique_ptr<ugsdr_gpu::DevBuf>> twiddles;
+	std::map<int, std::unique_ptr<ugsdr_gpu::DevBuf>> twiddles_lohi;
 	std::map<int, ugsdr_gpu::FftPlanDesc> plans;
 	std::map<int, ugsdr_gpu::LargePlan> large_plans;
 

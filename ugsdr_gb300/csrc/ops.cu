@@ -4,7 +4,7 @@
 // every call stages through the context's device scratch on its stream.
 #include "internal.hpp"
 #include "acq_kernels.cuh"
-#include "acq_large.cuh"
+#include "four_step.cuh"
 #include "fft_plan.hpp"
 
 #include <algorithm>
@@ -60,7 +60,7 @@ namespace ugsdr_gpu {
 		}
 
 		// four-step forward of one array (k1-major output) for sizes above one CTA
-		__global__ void dft_large_kernel(LargeParams p, const float2* in, int conj_in) {
+		__global__ void __launch_bounds__(512) dft_large_kernel(LargeParams p, const float2* in, int conj_in) {
 			extern __shared__ float2 sm[];
 			const int tile = max(p.cw * p.n1, p.rw * p.n2);
 			four_step_forward(p, sm, sm + tile, p.code_out, [&](int64_t i) {
