@@ -269,28 +269,33 @@ int ugsdr_correlate(ugsdr_ctx* ctx, const float* iq, const float* code, size_t n
 int ugsdr_convert_samples(ugsdr_ctx* ctx, const void* in, int sample_type, size_t n, float* out_iq);
 
 /* ------------------------------------------------------ tracking bank */
-/* Correlator bank for many channels per 1 ms epoch: carrier wipe-off and
- * VE/E/P/L/VL taps (Tracker::GetEpl / TrackingParameters::CorrelateSplit,
- * src/tracking/tracker.hpp:119-139, src/tracking/tracking_parameters.hpp:472-493)
- * followed by the PLL/FLL and DLL updates (tracking_parameters.hpp:495-528). */
+/* Correlator bank for many channels per 1 ms epoch (Tracker::Track,
+ * src/tracking/tracker.hpp:186-197): per channel and epoch the carrier
+ * wipe-off (TableMixer, 6-bit LUT, with the NCO phase held as a 64-bit
+ * fixed-point accumulator), five taps VE/E/P/L/VL each computed as
+ * TrackingParameters::CorrelateSplit (two dot products split at the code
+ * period, combined by AddWithPhase; tracking_parameters.hpp:89-98, 472-493),
+ * then Pll(prompt) and Dll(early, late) in FP64 (tracking_parameters.hpp:
+ * 495-528; Tracker::GetEpl order, tracker.hpp:119-177).  One launch advances
+ * every channel over many epochs; the state stays on the device between calls. */
 typedef struct ugsdr_track_channel {
 	int code;                 /* index into the bank's code table */
-	double sampling_rate;     /* Hz */
-	double code_frequency;    /* chips/s (base) */
-	double code_length;       /* chips per code period */
-	double code_phase;        /* chips at the first sample of the first epoch */
-	double carrier_frequency; /* Hz (initial Doppler + IF) */
+	double sampling_rate;     /* Hz (all channels of a bank share it) */
+	double code_frequency;    /* chips/s, base (BOC: half-chips, 2.046e6 for E1B) */
+	double code_length;       /* chips per code period (period = length / frequency, in ms) */
+	double code_phase;        /* samples, TrackingParameters::code_phase semantics */
+	double carrier_frequency; /* Hz (Doppler + IF) */
 	double carrier_phase;     /* rad */
-	int boc;                  /* 1: very-early/very-late taps are meaningful */
+	int boc;                  /* informational: VE/VL taps are for BOC signals */
 } ugsdr_track_channel;
 
 typedef struct ugsdr_track_config {
-	double early_late_spacing;      /* chips (0.5 in the spec; reference 0.25 each side) */
-	double very_early_late_spacing; /* chips (0.15) */
-	double pll_bandwidth;           /* Hz (15) */
-	double dll_bandwidth;           /* Hz (1) */
-	double fll_bandwidth;           /* Hz (0 = off) */
-	double integration_time;        /* s (0.001) */
+	double early_late_spacing;      /* chips from prompt to E and L (reference: 0.25) */
+	double very_early_late_spacing; /* chips from prompt to VE and VL */
+	double pll_bandwidth;           /* Hz (reference 25) */
+	double dll_bandwidth;           /* Hz (reference 0.7) */
+	double fll_bandwidth;           /* Hz, FLL assist; 0 = off (reference 250) */
+	double integration_time;        /* s; 0.001 (one epoch) is supported */
 } ugsdr_track_config;
 
 /* Per channel per epoch output: taps VE, E, P, L, VL as I/Q and loop state. */

@@ -134,3 +134,25 @@ def resample(x: np.ndarray, new_fs: int, old_fs: int) -> np.ndarray:
     out = np.empty(up // (lcm // new_fs) + 2, np.complex64)
     n = load().orc_resample_c32(_p(x), x.size, _p(out), new_fs, old_fs)
     return out[:n].copy()
+
+
+TRACK_FIELDS = 21
+
+
+def track(iq_complex: np.ndarray, spm: int, n_epochs: int, chips: np.ndarray, fs: float, code_frequency: float,
+          code_phase: float, carrier_frequency: float, carrier_phase: float = 0.0, early_late: float = 0.25,
+          very_early_late: float = 0.5, pll_bw: float = 25.0, dll_bw: float = 0.7, fll_bw: float = 250.0) -> np.ndarray:
+    """FP64 restatement of one tracking channel (track_oracle.cpp); rows of
+    VE, E, P, L, VL (re, im), carrier_frequency, carrier_phase, code_phase,
+    code_frequency, phase_error, code_error."""
+    lib = load()
+    fn = lib.orc_track_f64
+    fn.argtypes = [C.c_void_p, C.c_size_t, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+    fn.restype = None
+    x = np.ascontiguousarray(iq_complex, np.complex64)
+    c = np.ascontiguousarray(chips, np.float32)
+    cfg = np.array([early_late, very_early_late, pll_bw, dll_bw, fll_bw, 1e-3])
+    ch = np.array([fs, code_frequency, float(len(c)), code_phase, carrier_frequency, carrier_phase])
+    out = np.zeros((n_epochs, TRACK_FIELDS))
+    fn(x.ctypes.data, spm, n_epochs, c.ctypes.data, len(c), cfg.ctypes.data, ch.ctypes.data, out.ctypes.data)
+    return out

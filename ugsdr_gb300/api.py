@@ -271,3 +271,55 @@ def doppler_bins(range_hz: float, step_hz: float) -> int:
     if st != L.OK:
         raise L.UgsdrError(st, "bad doppler grid")
     return n.value
+
+
+TRACK_DTYPE = np.dtype([("taps", "<f4", (5, 2)), ("carrier_frequency", "<f8"), ("carrier_phase", "<f8"),
+                        ("code_phase", "<f8"), ("code_frequency", "<f8"), ("phase_error", "<f8"), ("code_error", "<f8")])
+
+
+class TrackBank:
+    """Correlator bank (ugsdr_track_create / _run): channels advance together,
+    their NCO and loop state stays on the device between run() calls."""
+
+    def __init__(self, ctx: Context, channels: list[dict], codes: list[np.ndarray], *, early_late: float = 0.25,
+                 very_early_late: float = 0.5, pll_bw: float = 25.0, dll_bw: float = 0.7, fll_bw: float = 250.0):
+        self.ctx = ctx
+        lens = [len(c) for c in codes]
+        lmax = max(lens)
+        table = np.zeros((len(codes), lmax), np.float32)
+        for i, c in enumerate(codes):
+            table[i, : len(c)] = c
+        chs = (L.TrackChannel * len(channels))()
+        for i, ch in enumerate(channels):
+            code_len = lens[ch["code"]] if 0 <= ch["code"] < len(lens) else 0  # the library rejects bad indices
+            chs[i] = L.TrackChannel(ch["code"], ch["fs"], ch["code_frequency"], code_len, ch["code_phase"],
+                                    ch["carrier_frequency"], ch.get("carrier_phase", 0.0), ch.get("boc", 0))
+        cfg = L.TrackConfig(early_late, very_early_late, pll_bw, dll_bw, fll_bw, 1e-3)
+        lens_arr = (C.c_int * len(lens))(*lens)
+        h = C.c_void_p()
+        ctx._check(ctx.lib.ugsdr_track_create(ctx.h, C.byref(cfg), chs, len(channels), _ptr(table), lens_arr, len(codes),
+                                              lmax, C.byref(h)))
+        self.h = h
+        self.n = len(channels)
+        self.spm = int(channels[0]["fs"] // 1000)
+
+    def run(self, samples, sample_type: int, n_epochs: int, on_device: bool = False, outputs: bool = True):
+        ptr = int(samples) if on_device else _ptr(np.ascontiguousarray(samples))
+        keep = samples
+        out = np.zeros((n_epochs, self.n), TRACK_DTYPE) if outputs else None
+        self.ctx._check(self.ctx.lib.ugsdr_track_run(self.h, C.c_void_p(ptr), sample_type, 1 if on_device else 0, self.spm,
+                                                     n_epochs, C.cast(out.ctypes.data, C.POINTER(L.TrackOutput))
+                                                     if outputs else None))
+        del keep
+        return out
+
+    def close(self):
+        if self.h:
+            self.ctx.lib.ugsdr_track_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

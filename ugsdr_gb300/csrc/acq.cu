@@ -130,6 +130,16 @@ namespace ugsdr_gpu {
 	namespace {
 		constexpr int kBatchedThreads = 256;
 
+		// Threads for a CTA running `batch` FFTs of `plan`: enough for the
+		// pass with the most butterflies, rounded to whole warps (<= 256, the
+		// kernels' launch bound), so no pass leaves more than a warp idle.
+		int threads_for(const FftPlanDev& plan, int batch) {
+			int most = 0;
+			for (int s = 0; s < plan.n_pass; ++s)
+				most = std::max(most, batch * plan.n / plan.radix[s]);
+			return std::min(kBatchedThreads, std::max(64, (most + 31) / 32 * 32));
+		}
+
 		// Sub-transforms per CTA: 8 columns/rows (64-byte runs per k1 row) unless
 		// the tiles would exceed a third of shared memory.
 		// inv_cols holds three column tiles (input, work, prefetch) and an
@@ -183,7 +193,7 @@ namespace ugsdr_gpu {
 		void launch_fwd_cols(ugsdr_ctx* ctx, K kernel, const BatchedParams& p, int items) {
 			const size_t smem = smem_cols(p, false);
 			set_smem(kernel, smem);
-			kernel<<<items * chunks_of(p.n2, p.cw), kBatchedThreads, smem, ctx->stream>>>(p);
+			kernel<<<items * chunks_of(p.n2, p.cw), threads_for(p.p1, p.cw), smem, ctx->stream>>>(p);
 		}
 
 		void launch_forward(ugsdr_ctx* ctx, int sample_type, const BatchedParams& p, int items) {
@@ -195,7 +205,7 @@ namespace ugsdr_gpu {
 			}
 			const size_t smem = smem_rows(p, false);
 			set_smem(fwd_rows_kernel, smem);
-			fwd_rows_kernel<<<items * chunks_of(p.n1, p.rw), kBatchedThreads, smem, ctx->stream>>>(p);
+			fwd_rows_kernel<<<items * chunks_of(p.n1, p.rw), threads_for(p.p2, p.rw), smem, ctx->stream>>>(p);
 			note_launch(ctx, 2);
 		}
 	}
@@ -276,8 +286,8 @@ namespace ugsdr_gpu {
 				if (s.fold_mode == 2)
 					UG_CUDA(cudaMemsetAsync(p.zcg, 0, sizeof(float2) * static_cast<size_t>(p.rows) * s.k * s.m, ctx->stream));
 			}
-			inv_rows_kernel<<<p.rows * s.k * chunks_of(p.n1, p.rw), kBatchedThreads, smem_r, ctx->stream>>>(p);
-			inv_cols_kernel<<<p.rows * chunks, kBatchedThreads, smem_c, ctx->stream>>>(p);
+			inv_rows_kernel<<<p.rows * s.k * chunks_of(p.n1, p.rw), threads_for(p.p2, p.rw), smem_r, ctx->stream>>>(p);
+			inv_cols_kernel<<<p.rows * chunks, threads_for(p.p1, p.cw), smem_c, ctx->stream>>>(p);
 			note_launch(ctx, 2);
 			if (s.fold_mode) {
 				fold_finish_kernel<<<p.rows, kBatchedThreads, 0, ctx->stream>>>(p);
