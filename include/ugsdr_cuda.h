@@ -321,22 +321,38 @@ int ugsdr_track_run(ugsdr_track_bank* bank, const void* samples, int sample_type
 int ugsdr_track_destroy(ugsdr_track_bank* bank);
 
 /* ------------------------------------------------------------ serving */
-/* Continuous-batching acquisition server: jobs are admitted while others run,
- * as slots and device memory allow; code spectra stay cached across requests. */
+/* Continuous-batching acquisition server.  A worker thread admits queued jobs
+ * into `max_inflight` slots, each with its own CUDA stream and scratch, as
+ * soon as a slot is free and the job's device-memory estimate fits the
+ * budget; admitted jobs run concurrently on the device while later requests
+ * keep arriving.  Code spectra (ugsdr_code_put handles) stay resident across
+ * requests; do not release a handle that a pending job uses. */
 typedef struct ugsdr_server ugsdr_server;
 typedef struct ugsdr_server_config {
-	int max_inflight;          /* concurrent jobs on the device */
-	size_t memory_budget;      /* bytes of device memory admission may use (0 = free memory) */
-	int queue_capacity;        /* pending requests before UGSDR_E_QUEUE_FULL */
+	int max_inflight;          /* concurrent jobs on the device (0 = 4) */
+	size_t memory_budget;      /* device bytes the slots' scratch may hold (0 = 80 % of free memory) */
+	int queue_capacity;        /* pending requests before UGSDR_E_QUEUE_FULL (0 = 1024) */
 } ugsdr_server_config;
 
+typedef struct ugsdr_server_stats {
+	uint64_t submitted, completed, failed;
+	int inflight;              /* jobs on the device now */
+	int max_inflight_seen;     /* most jobs on the device at once so far */
+	size_t device_bytes;       /* scratch the slots hold */
+	double busy_seconds;       /* wall time with at least one job on the device */
+} ugsdr_server_stats;
+
 int ugsdr_server_create(ugsdr_ctx* ctx, const ugsdr_server_config* cfg, ugsdr_server** server);
-/* Copies the job description (and the host samples) and returns a ticket. */
+/* Copies the job description (and the host samples) and returns a ticket;
+ * UGSDR_E_QUEUE_FULL when queue_capacity requests are pending. */
 int ugsdr_server_submit(ugsdr_server* server, const ugsdr_acq_job* job, uint64_t* ticket);
-/* Non-blocking: 1 + results when done, 0 while pending. results[n_codes]. */
+/* Non-blocking: *done = 1 and results[n_codes] filled when the job finished
+ * (the ticket is then retired), 0 while pending; a failed job returns its
+ * error status (UGSDR_E_NOMEM when its estimate exceeds the budget). */
 int ugsdr_server_poll(ugsdr_server* server, uint64_t ticket, ugsdr_acq_result* results, int* done);
 /* Blocks until every submitted job finished. */
 int ugsdr_server_drain(ugsdr_server* server);
+int ugsdr_server_get_stats(ugsdr_server* server, ugsdr_server_stats* stats);
 int ugsdr_server_destroy(ugsdr_server* server);
 
 #ifdef __cplusplus

@@ -156,3 +156,21 @@ def track(iq_complex: np.ndarray, spm: int, n_epochs: int, chips: np.ndarray, fs
     out = np.zeros((n_epochs, TRACK_FIELDS))
     fn(x.ctypes.data, spm, n_epochs, c.ctypes.data, len(c), cfg.ctypes.data, ch.ctypes.data, out.ctypes.data)
     return out
+
+
+def track_taps(iq_epoch: np.ndarray, chips: np.ndarray, fs: float, code_frequency: float, code_phase: float,
+               carrier_frequency: float, carrier_phase: float, early_late: float = 0.25,
+               very_early_late: float = 0.5) -> np.ndarray:
+    """Open-loop taps of one epoch for a given NCO state (orc_track_taps_f64):
+    10 values (VE, E, P, L, VL re/im) + 5 minor partial magnitudes."""
+    lib = load()
+    fn = lib.orc_track_taps_f64
+    d = C.c_double
+    fn.argtypes = [C.c_void_p, C.c_size_t, C.c_void_p, C.c_int, d, d, d, d, d, d, d, d, C.c_void_p]
+    fn.restype = None
+    x = np.ascontiguousarray(iq_epoch, np.complex64)
+    c = np.ascontiguousarray(chips, np.float32)
+    out = np.zeros(15)
+    fn(x.ctypes.data, x.size, c.ctypes.data, len(c), fs, code_frequency, float(len(c)), code_phase, carrier_frequency,
+       carrier_phase, early_late, very_early_late, out.ctypes.data)
+    return out

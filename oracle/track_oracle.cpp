@@ -49,6 +49,69 @@ namespace {
 
 extern "C" {
 
+// Open-loop correlator of ONE epoch: the five taps for the given NCO state
+// at the start of the epoch (carrier frequency Hz, carrier phase rad, code
+// phase of this epoch in samples), same arithmetic as orc_track_f64's epoch.
+// out: 10 doubles (VE, E, P, L, VL re/im) + 5 minor partial magnitudes.
+void orc_track_taps_f64(const float* iq, size_t spm, const float* chips, int len, double fs, double base, double code_len,
+	double ph, double carrier_freq, double carrier_phase, double el, double vel, double* out) {
+	constexpr double kTwo64l = 18446744073709551616.0;
+	float table[80];
+	const double step = 5 * kPi / 80 / 2;
+	for (int i = 0; i < 80; ++i)
+		table[i] = static_cast<float>(std::sin(static_cast<double>(i) * step));
+	const int period_ms = static_cast<int>(std::lround(code_len / base * 1000.0));
+	const size_t samples_per_ms = static_cast<size_t>(fs / 1e3);
+	const double period = static_cast<double>(samples_per_ms) * period_ms;
+	const uint64_t L3 = 3ull * static_cast<uint64_t>(len);
+	const uint64_t S3 = static_cast<uint64_t>(3 * period_ms * fs / 1e3);
+	const double spc = fs / base;
+	const double offsets[5] = {vel, el, 0.0, -el, -vel};
+	const uint64_t phase_fx = frac_to_fx(carrier_phase / (2 * kPi));
+	double f = -carrier_freq;
+	const bool mix = std::abs(f) != 0.0;
+	if (f < 0)
+		f = fs + f;
+	double av = kTwo64l * f / fs;
+	if (av >= kTwo64l)
+		av = 0.0;
+	const uint64_t adder = static_cast<uint64_t>(av);
+	const uint64_t holder0 = 0ull - phase_fx;
+	std::vector<cd> mixed(spm);
+	for (size_t i = 0; i < spm; ++i) {
+		const float a = iq[2 * i], b = iq[2 * i + 1];
+		if (!mix) {
+			mixed[i] = cd(a, b);
+			continue;
+		}
+		const uint32_t idx = static_cast<uint32_t>((holder0 + static_cast<uint64_t>(i) * adder) >> 58);
+		const float c = table[idx + 16], s = table[idx];
+		const volatile float re1 = a * c, re2 = b * s, im1 = a * s, im2 = b * c;
+		mixed[i] = cd(re1 - re2, im1 + im2);
+	}
+	for (int t = 0; t < 5; ++t) {
+		double p = ph + spc * offsets[t];
+		while (p < 0)
+			p += period;
+		if (p > period)
+			p = std::fmod(p, period);
+		const size_t first_len = static_cast<size_t>(std::ceil(p)) % samples_per_ms;
+		const uint64_t first_phase = static_cast<uint64_t>(std::ceil(2 * period - p));
+		cd A(0, 0), B(0, 0);
+		for (size_t i = 0; i < spm; ++i) {
+			const float cv = chips[(((first_phase + i) * L3) / S3 % L3) % static_cast<uint64_t>(len)];
+			if (i < first_len)
+				A += mixed[i] * static_cast<double>(cv);
+			else
+				B += mixed[i] * static_cast<double>(cv);
+		}
+		const cd tap = add_with_phase(A, B, std::fmod(p, static_cast<double>(samples_per_ms)) / samples_per_ms);
+		out[2 * t] = tap.real();
+		out[2 * t + 1] = tap.imag();
+		out[10 + t] = std::min(std::abs(A), std::abs(B));
+	}
+}
+
 // One channel over n_epochs epochs of spm samples (complex float I/Q).
 // cfg: [el_offset, vel_offset, pll_bw, dll_bw, fll_bw, T]
 // ch:  [fs, code_frequency, code_length, code_phase, carrier_frequency, carrier_phase]

@@ -1,0 +1,82 @@
+"""Serving loop (ugsdr_server_*): every result is the same alone and in the
+mix (continuous batching must not change results), jobs overlap on the
+device, and the queue and memory-admission limits are enforced."""
+import time
+
+import numpy as np
+import pytest
+
+from conftest import unpack_codes
+from ugsdr_gb300 import _lib as L
+from ugsdr_gb300 import signals
+from ugsdr_gb300.api import Server
+
+pytestmark = pytest.mark.gpu
+
+
+def make_jobs(ctx, golden_codes):
+    """Uneven jobs: 2.046 / 4 / 10 / 50 MHz, 1-4 ms coherent, K 1-10, int8 and int16."""
+    ca = unpack_codes(golden_codes, "gps_l1ca")
+    specs = [(2.046e6, 1, 6, "ci16", 500.0), (4e6, 1, 10, "ci8", 500.0), (4e6, 2, 3, "ci16", 250.0),
+             (10e6, 1, 4, "ci8", 500.0), (50e6, 1, 2, "ci16", 1000.0), (4e6, 4, 2, "ci8", 125.0)]
+    jobs, keep = [], []
+    for i, (fs, t_ms, k, st, step) in enumerate(specs):
+        n = int(fs * t_ms / 1000)
+        codes = {p: ca[p] for p in range(3 + i)}
+        raw, _ = signals.gps_l1_config(seed=40 + i, codes=codes, fs=fs, ms=t_ms * k, visible=2, sample_type=st)
+        hs = [ctx.code_put(codes[p], n, repeats=t_ms) for p in codes]
+        stype = L.SAMPLES_CI8 if st == "ci8" else L.SAMPLES_CI16
+        jobs.append(ctx.make_job(raw, stype, fs, n, k, hs, 3000.0, step))
+        keep.append(hs)
+    return jobs, keep
+
+
+def test_results_same_alone_and_in_mix(ctx, golden_codes):
+    jobs, handles = make_jobs(ctx, golden_codes)
+    try:
+        alone = [ctx.acquire(j) for j in jobs]
+        srv = Server(ctx, max_inflight=4)
+        tickets = [srv.submit(j) for j in jobs for _ in range(3)]  # each job three times, interleaved
+        srv.drain()
+        mixed = [srv.poll(t) for t in tickets]
+        stats = srv.stats()
+        srv.close()
+        for i, res in enumerate(mixed):
+            ref = alone[i // 3]
+            assert len(res) == len(ref)
+            for a, b in zip(ref, res):
+                assert (a.index, a.doppler_bin) == (b.index, b.doppler_bin)
+                assert abs(a.level - b.level) <= 1e-6 * a.level and abs(a.snr - b.snr) <= 1e-6 * a.snr
+        assert stats["completed"] == len(tickets) and stats["failed"] == 0
+        assert stats["max_inflight_seen"] >= 2  # jobs were on the device together
+    finally:
+        for hs in handles:
+            for h in hs:
+                ctx.code_release(h)
+
+
+def test_queue_full_and_budget(ctx, golden_codes):
+    jobs, handles = make_jobs(ctx, golden_codes)
+    try:
+        srv = Server(ctx, max_inflight=1, queue_capacity=2)
+        codes = []
+        with pytest.raises(L.UgsdrError) as e:
+            for _ in range(50):
+                codes.append(srv.submit(jobs[4]))
+        assert e.value.status == L.E_QUEUE_FULL
+        srv.drain()
+        for t in codes:
+            assert srv.poll(t) is not None
+        srv.close()
+        # a budget below one job's scratch: refused with E_NOMEM when nothing else runs
+        small = Server(ctx, max_inflight=2, memory_budget=1 << 20)
+        t = small.submit(jobs[4])
+        small.drain()
+        with pytest.raises(L.UgsdrError) as e:
+            small.poll(t)
+        assert e.value.status == L.E_NOMEM
+        small.close()
+    finally:
+        for hs in handles:
+            for h in hs:
+                ctx.code_release(h)

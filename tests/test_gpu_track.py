@@ -1,9 +1,18 @@
 """Tracking correlator bank (ugsdr_track_*) against the FP64 oracle
 restatement of the reference's tracking step (oracle/track_oracle.cpp).
 
-Bars: prompt (and every tap) I/Q within 1e-4 of the FP64 oracle relative to
-the channel's peak prompt magnitude; carrier frequency within 1e-2 Hz and
-code phase within 1e-3 samples of the oracle at every epoch."""
+Two levels, because the carrier wipe-off uses the reference's 6-bit phase
+LUT: a phase difference of 1e-9 cycles between two runs eventually moves one
+sample to the neighbouring LUT entry, so closed-loop trajectories that differ
+only by FP32-versus-FP64 rounding drift apart by a few LUT steps.
+  1. Correlator parity, open loop: every epoch's five taps recomputed by the
+     oracle from the GPU's own NCO state at the start of that epoch must agree
+     within 1e-4 of the channel's peak prompt magnitude (AddWithPhase's sign
+     choice, a near-tie when one partial sum is tiny, may differ on at most 2 %
+     of the taps, and then by twice that partial).
+  2. Loop parity, closed loop: the GPU and oracle trajectories agree within
+     0.1 Hz (carrier), 1e-3 samples (code phase) and 0.1 chip/s (code
+     frequency), and the loops lock."""
 import numpy as np
 import pytest
 
@@ -20,24 +29,31 @@ def to_complex(raw):
     return (f[:, 0] + 1j * f[:, 1]).astype(np.complex64)
 
 
-def compare(out, ref, name):
-    """Taps within RTOL of the peak prompt, except where AddWithPhase's sign
-    choice (a near-tie when one CorrelateSplit partial is tiny) went the other
-    way under FP32 rounding: then the difference is twice that partial, which
-    the oracle reports per tap; such epochs must stay rare."""
+def check_open_loop(out, x, spm, chips, fs, base, ch0, el, vel, name):
+    period = int(round(len(chips) / base * 1000))
     taps = out["taps"].reshape(len(out), 10).astype(np.float64)
+    ref = np.zeros((len(out), 15))
+    for e in range(len(out)):
+        if e == 0:
+            cf, cph, cp = ch0["carrier_frequency"], ch0.get("carrier_phase", 0.0), ch0["code_phase"]
+        else:
+            cf, cph, cp = out["carrier_frequency"][e - 1], out["carrier_phase"][e - 1], out["code_phase"][e - 1]
+        ph = cp - fs / 1e3 * (e % period)
+        ref[e] = __import__("pyoracle").track_taps(x[e * spm:(e + 1) * spm], chips, fs, base, ph, cf, cph, el, vel)
     scale = np.abs(ref[:, 4] + 1j * ref[:, 5]).max()
     diff = np.abs(taps - ref[:, :10]).reshape(len(out), 5, 2).max(axis=2)
-    minor = ref[:, 16:21]
-    assert (diff <= RTOL * scale + 2.0 * minor * 1.0001).all(), name
+    assert (diff <= RTOL * scale + 2.0 * ref[:, 10:15] * 1.0001).all(), name
     assert (diff > RTOL * scale).mean() <= 0.02, name
-    assert np.abs(out["carrier_frequency"] - ref[:, 10]).max() <= 1e-2, name
+
+
+def check_closed_loop(out, ref, name):
+    assert np.abs(out["carrier_frequency"] - ref[:, 10]).max() <= 0.1, name
     assert np.abs(out["code_phase"] - ref[:, 12]).max() <= 1e-3, name
-    assert np.abs(out["code_frequency"] - ref[:, 13]).max() <= 1e-3, name
+    assert np.abs(out["code_frequency"] - ref[:, 13]).max() <= 0.1, name  # chips/s, 1e-7 of 1.023e6
 
 
 def test_gps_l1_bank_vs_oracle(ctx, oracle, golden_codes):
-    """Three GPS L1 C/A channels, int8 I/Q at 4 MHz, 120 epochs, reference loop constants."""
+    """Three GPS L1 C/A channels, int8 I/Q at 4 MHz, 120 epochs in two calls, reference loop constants."""
     from ugsdr_gb300.api import TrackBank
     ca = unpack_codes(golden_codes, "gps_l1ca")
     codes = {p: ca[p] for p in range(8)}
@@ -53,13 +69,15 @@ def test_gps_l1_bank_vs_oracle(ctx, oracle, golden_codes):
     out = np.concatenate([bank.run(raw[:60 * 4000], L.SAMPLES_CI8, 60), bank.run(raw[60 * 4000:], L.SAMPLES_CI8, 60)])
     bank.close()
     for i, (ch, t) in enumerate(zip(chans, truth)):
+        name = f"prn {t['prn']}"
+        check_open_loop(out[:, i], x, 4000, chips[i], 4e6, 1.023e6, ch, 0.25, 0.5, name)
         ref = oracle.track(x, 4000, 120, chips[i], 4e6, 1.023e6, ch["code_phase"], ch["carrier_frequency"])
-        compare(out[:, i], ref, f"prn {t['prn']}")
-        # the loop locks: prompt dominates the early/late taps, frequency near truth
+        check_closed_loop(out[:, i], ref, name)
+        # the loop locks: prompt dominates the early tap, frequency near the truth
         p = np.abs(out["taps"][60:, i, 2, 0] + 1j * out["taps"][60:, i, 2, 1]).mean()
         e = np.abs(out["taps"][60:, i, 1, 0] + 1j * out["taps"][60:, i, 1, 1]).mean()
-        assert p > e
-        assert abs(out["carrier_frequency"][-1, i] - t["doppler"]) < 30.0
+        assert p > e, name
+        assert abs(out["carrier_frequency"][-1, i] - t["doppler"]) < 30.0, name
 
 
 def test_galileo_e1b_bank_vs_oracle(ctx, oracle, golden_codes):
@@ -75,8 +93,9 @@ def test_galileo_e1b_bank_vs_oracle(ctx, oracle, golden_codes):
     bank = TrackBank(ctx, chans, [e1b[5]], **kw)
     out = bank.run(raw, L.SAMPLES_CI16, 40)
     bank.close()
+    check_open_loop(out[:, 0], x, 10000, e1b[5], 10e6, 2.046e6, chans[0], 0.15, 0.5, "e1b")
     ref = oracle.track(x, 10000, 40, e1b[5], 10e6, 2.046e6, chans[0]["code_phase"], 1200.0, **kw)
-    compare(out[:, 0], ref, "e1b")
+    check_closed_loop(out[:, 0], ref, "e1b")
 
 
 def test_bank_rejects_bad_configs(ctx, golden_codes):

@@ -207,5 +207,12 @@ class StaticJob(C.Structure):
     ]
 
 
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("failed", C.c_uint64), ("inflight", C.c_int),
+                ("max_inflight_seen", C.c_int), ("device_bytes", C.c_size_t), ("busy_seconds", C.c_double)]
+
+
+SIGNATURES["ugsdr_server_get_stats"] = (C.c_int, [C.c_void_p, C.POINTER(ServerStats)])
+
 STATIC_SCRATCH_BYTES = 16 << 20
 SIGNATURES["ugsdr_acquire_static"] = (C.c_int, [C.c_void_p, C.POINTER(StaticJob), C.c_void_p, C.POINTER(C.c_size_t)])

@@ -323,3 +323,51 @@ class TrackBank:
             self.close()
         except Exception:
             pass
+
+
+class Server:
+    """Continuous-batching acquisition server (ugsdr_server_*)."""
+
+    def __init__(self, ctx: Context, max_inflight: int = 4, memory_budget: int = 0, queue_capacity: int = 1024):
+        self.ctx = ctx
+        cfg = L.ServerConfig(max_inflight, memory_budget, queue_capacity)
+        h = C.c_void_p()
+        ctx._check(ctx.lib.ugsdr_server_create(ctx.h, C.byref(cfg), C.byref(h)))
+        self.h = h
+        self._n_codes: dict[int, int] = {}
+
+    def submit(self, job: Job) -> int:
+        t = C.c_uint64()
+        self.ctx._check(self.ctx.lib.ugsdr_server_submit(self.h, C.byref(job.c), C.byref(t)))
+        self._n_codes[t.value] = job.c.n_codes
+        return t.value
+
+    def poll(self, ticket: int):
+        """None while pending, else the per-code results (the ticket is retired)."""
+        n = self._n_codes[ticket]
+        res = (L.AcqResult * n)()
+        done = C.c_int()
+        self.ctx._check(self.ctx.lib.ugsdr_server_poll(self.h, ticket, res, C.byref(done)))
+        if not done.value:
+            return None
+        del self._n_codes[ticket]
+        return [AcqResult.from_c(r) for r in res]
+
+    def drain(self) -> None:
+        self.ctx._check(self.ctx.lib.ugsdr_server_drain(self.h))
+
+    def stats(self) -> dict:
+        s = L.ServerStats()
+        self.ctx._check(self.ctx.lib.ugsdr_server_get_stats(self.h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in L.ServerStats._fields_}
+
+    def close(self) -> None:
+        if self.h:
+            self.ctx.lib.ugsdr_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

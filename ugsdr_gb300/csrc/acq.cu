@@ -458,28 +458,60 @@ namespace ugsdr_gpu {
 		return sizeof(float2) * static_cast<size_t>(L.n) * L.k * L.grid.size();
 	}
 
-	void run_jobs(ugsdr_ctx* ctx, const ugsdr_acq_job* jobs, int n_jobs, ugsdr_acq_result* const* results,
-		ugsdr_acq_cell* cells_out) {
-		require(jobs != nullptr && n_jobs >= 1, "no jobs");
-		std::vector<JobLaunch> launches;
-		size_t samples_bytes = 0, spectra_b = 0, cells_n = 0, params_b = 0, slab_b = 0;
-		for (int j = 0; j < n_jobs; ++j) {
-			launches.push_back(validate(ctx, jobs[j]));
-			const auto& L = launches.back();
-			if (!jobs[j].samples_on_device)
-				samples_bytes += (sample_bytes(jobs[j].sample_type) * jobs[j].n_samples + 255) / 256 * 256;
-			spectra_b = std::max(spectra_b, spectra_bytes(L));
-			cells_n += static_cast<size_t>(L.n_codes) * L.grid.size();
-			params_b += (L.grid.size() * sizeof(uint32_t) + L.n_codes * sizeof(void*) + L.n_codes * sizeof(int) + 512) / 256 * 256;
-			if (L.large)
-				slab_b = std::max(slab_b, batched_scratch_bytes(ctx, shape_of(L)));
+	namespace {
+		struct BatchSizes {
+			std::vector<JobLaunch> launches;
+			size_t samples = 0, spectra = 0, cells = 0, params = 0, slab = 0;
+		};
+
+		BatchSizes size_batch(ugsdr_ctx* ctx, const ugsdr_acq_job* jobs, int n_jobs) {
+			require(jobs != nullptr && n_jobs >= 1, "no jobs");
+			BatchSizes s;
+			std::map<std::pair<const void*, size_t>, bool> seen;
+			for (int j = 0; j < n_jobs; ++j) {
+				s.launches.push_back(validate(ctx, jobs[j]));
+				const auto& L = s.launches.back();
+				if (!jobs[j].samples_on_device) {
+					const size_t bytes = sample_bytes(jobs[j].sample_type) * jobs[j].n_samples;
+					if (!seen[{jobs[j].samples, bytes}])
+						s.samples += (bytes + 255) / 256 * 256;
+					seen[{jobs[j].samples, bytes}] = true;
+				}
+				s.spectra = std::max(s.spectra, spectra_bytes(L));
+				s.cells += static_cast<size_t>(L.n_codes) * L.grid.size();
+				s.params += (L.grid.size() * sizeof(uint32_t) + L.n_codes * sizeof(void*) + L.n_codes * sizeof(int) + 512) / 256 * 256;
+				if (L.large)
+					s.slab = std::max(s.slab, batched_scratch_bytes(ctx, shape_of(L)));
+			}
+			s.samples = std::max<size_t>(s.samples, 256);
+			return s;
 		}
-		ctx->samples.reserve(std::max<size_t>(samples_bytes, 256));
-		ctx->spectra.reserve(spectra_b);
-		ctx->cells.reserve(sizeof(AcqCellDev) * cells_n);
-		ctx->params.reserve(params_b);
-		if (slab_b)
-			ctx->slab.reserve(slab_b);
+
+		struct StreamSwap {  // route the launch helpers (which use ctx->stream) to `stream`
+			ugsdr_ctx* ctx;
+			cudaStream_t saved;
+			StreamSwap(ugsdr_ctx* c, cudaStream_t s) : ctx(c), saved(c->stream) { c->stream = s; }
+			~StreamSwap() { ctx->stream = saved; }
+		};
+	}
+
+	size_t jobs_device_bytes(ugsdr_ctx* ctx, const ugsdr_acq_job* jobs, int n_jobs) {
+		const BatchSizes s = size_batch(ctx, jobs, n_jobs);
+		return s.samples + s.spectra + sizeof(AcqCellDev) * s.cells + s.params + s.slab;
+	}
+
+	EnqueuedBatch enqueue_jobs(ugsdr_ctx* ctx, Workspace& ws, cudaStream_t stream, const ugsdr_acq_job* jobs, int n_jobs,
+		void* host_cells) {
+		BatchSizes sizes = size_batch(ctx, jobs, n_jobs);
+		const std::vector<JobLaunch>& launches = sizes.launches;
+		const size_t params_b = sizes.params;
+		ws.samples.reserve(sizes.samples);
+		ws.spectra.reserve(sizes.spectra);
+		ws.cells.reserve(sizeof(AcqCellDev) * sizes.cells);
+		ws.params.reserve(params_b);
+		if (sizes.slab)
+			ws.slab.reserve(sizes.slab);
+		StreamSwap swap(ctx, stream);
 
 		// stage parameters and host samples
 		std::vector<char> host_params(params_b);
@@ -501,7 +533,7 @@ namespace ugsdr_gpu {
 					dev_samples[j] = it->second;
 				}
 				else {
-					char* dst = ctx->samples.as<char>() + s_off;
+					char* dst = ws.samples.as<char>() + s_off;
 					UG_CUDA(cudaMemcpyAsync(dst, job.samples, bytes, cudaMemcpyHostToDevice, ctx->stream));
 					dev_samples[j] = dst;
 					staged[key] = dst;
@@ -522,31 +554,38 @@ namespace ugsdr_gpu {
 			c_offsets[j] = c_off;
 			c_off += static_cast<size_t>(L.n_codes) * L.grid.size();
 		}
-		UG_CUDA(cudaMemcpyAsync(ctx->params.ptr, host_params.data(), params_b, cudaMemcpyHostToDevice, ctx->stream));
+		UG_CUDA(cudaMemcpyAsync(ws.params.ptr, host_params.data(), params_b, cudaMemcpyHostToDevice, ctx->stream));
 
 		for (int j = 0; j < n_jobs; ++j) {
 			const auto& L = launches[j];
-			char* dp = ctx->params.as<char>() + p_offsets[j];
+			char* dp = ws.params.as<char>() + p_offsets[j];
 			auto* adders = reinterpret_cast<uint32_t*>(dp);
 			size_t o = (L.adders.size() * sizeof(uint32_t) + 15) / 16 * 16;
 			auto* code_ptrs = reinterpret_cast<const float2**>(dp + o);
 			o += L.n_codes * sizeof(void*);
 			o = (o + 15) / 16 * 16;
 			auto* best = reinterpret_cast<int*>(dp + o);
-			launch_job(ctx, jobs[j], L, dev_samples[j], ctx->cells.as<AcqCellDev>() + c_offsets[j], best, adders,
-				code_ptrs, ctx->spectra.as<float2>(), ctx->slab.as<char>());
+			launch_job(ctx, jobs[j], L, dev_samples[j], ws.cells.as<AcqCellDev>() + c_offsets[j], best, adders,
+				code_ptrs, ws.spectra.as<float2>(), ws.slab.as<char>());
 		}
+		UG_CUDA(cudaMemcpyAsync(host_cells, ws.cells.ptr, sizeof(AcqCellDev) * c_off, cudaMemcpyDeviceToHost, ctx->stream));
+		EnqueuedBatch b;
+		for (const auto& L : launches)
+			b.grids.push_back(L.grid);
+		b.cell_offsets = c_offsets;
+		b.n_cells = c_off;
+		return b;
+	}
 
-		// gather
-		std::vector<AcqCellDev> cells(c_off);
-		UG_CUDA(cudaMemcpyAsync(cells.data(), ctx->cells.ptr, sizeof(AcqCellDev) * c_off, cudaMemcpyDeviceToHost, ctx->stream));
-		UG_CUDA(cudaStreamSynchronize(ctx->stream));
+	void finish_jobs(const EnqueuedBatch& b, const ugsdr_acq_job* jobs, int n_jobs, const void* host_cells,
+		ugsdr_acq_result* const* results, ugsdr_acq_cell* cells_out) {
+		const auto* cells = static_cast<const AcqCellDev*>(host_cells);
 		for (int j = 0; j < n_jobs; ++j) {
 			const auto& job = jobs[j];
-			const auto& L = launches[j];
-			const size_t nd = L.grid.size();
-			for (int c = 0; c < L.n_codes; ++c) {
-				const AcqCellDev* row = cells.data() + c_offsets[j] + static_cast<size_t>(c) * nd;
+			const auto& grid = b.grids[j];
+			const size_t nd = grid.size();
+			for (int c = 0; c < job.n_codes; ++c) {
+				const AcqCellDev* row = cells + b.cell_offsets[j] + static_cast<size_t>(c) * nd;
 				// first strictly greater level wins (fse.hpp:265), recomputed on the host
 				size_t bd = 0;
 				for (size_t d = 1; d < nd; ++d)
@@ -557,7 +596,7 @@ namespace ugsdr_gpu {
 				r.doppler_bin = static_cast<int>(bd);
 				r.index = row[bd].index;
 				r.n_doppler = static_cast<uint32_t>(nd);
-				r.doppler = L.grid[bd] + job.intermediate_frequency;
+				r.doppler = grid[bd] + job.intermediate_frequency;
 				r.code_offset = job.code_offset_ratio * static_cast<double>(row[bd].index);
 				r.level = row[bd].level;
 				r.mean = row[bd].mean;
@@ -565,9 +604,23 @@ namespace ugsdr_gpu {
 				r.sigma = static_cast<double>(row[bd].std + row[bd].mean);
 				r.snr = r.level / r.sigma;
 			}
-			if (cells_out && n_jobs == 1)
-				std::memcpy(cells_out, cells.data(), sizeof(AcqCellDev) * c_off);
 		}
+		if (cells_out && n_jobs == 1)
+			std::memcpy(cells_out, cells, sizeof(AcqCellDev) * b.n_cells);
+	}
+
+	void run_jobs(ugsdr_ctx* ctx, const ugsdr_acq_job* jobs, int n_jobs, ugsdr_acq_result* const* results,
+		ugsdr_acq_cell* cells_out) {
+		// cells land in host memory; pageable is fine here since the call waits
+		size_t n_cells = 0;
+		{
+			const BatchSizes s = size_batch(ctx, jobs, n_jobs);
+			n_cells = s.cells;
+		}
+		std::vector<AcqCellDev> cells(std::max<size_t>(n_cells, 1));
+		const EnqueuedBatch b = enqueue_jobs(ctx, ctx->ws, ctx->stream, jobs, n_jobs, cells.data());
+		UG_CUDA(cudaStreamSynchronize(ctx->stream));
+		finish_jobs(b, jobs, n_jobs, cells.data(), results, cells_out);
 	}
 }
 

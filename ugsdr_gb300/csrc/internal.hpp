@@ -52,10 +52,13 @@ namespace ugsdr_gpu {
 		}
 		template <typename T>
 		T* as() const { return static_cast<T*>(ptr); }
-		~DevBuf() {
+		void release() {
 			if (ptr)
 				cudaFree(ptr);
+			ptr = nullptr;
+			bytes = 0;
 		}
+		~DevBuf() { release(); }
 		DevBuf() = default;
 		DevBuf(const DevBuf&) = delete;
 		DevBuf& operator=(const DevBuf&) = delete;
@@ -90,6 +93,24 @@ namespace ugsdr_gpu {
 	};
 
 	struct Plans;  // fft planning (acq.cu)
+
+	// Device scratch of one in-flight batch of acquisition jobs (grow-only).
+	// The context owns one; each serving slot owns its own so batches overlap.
+	struct Workspace {
+		DevBuf samples;    // staged host samples
+		DevBuf spectra;    // forward spectra X[d][b][N]
+		DevBuf slab;       // large-path scratch (B, partials, counters, fold buffers)
+		DevBuf cells;      // per (code, doppler) records
+		DevBuf params;     // per-job parameter arrays
+		size_t reserved() const { return samples.bytes + spectra.bytes + slab.bytes + cells.bytes + params.bytes; }
+		void release() {
+			samples.release();
+			spectra.release();
+			slab.release();
+			cells.release();
+			params.release();
+		}
+	};
 }
 
 struct ugsdr_ctx {
@@ -112,12 +133,7 @@ struct ugsdr_ctx {
 
 	// scratch
 	ugsdr_gpu::DevBuf lut;        // float[80] TableMixer sine table
-	ugsdr_gpu::DevBuf samples;    // staged input samples
-	ugsdr_gpu::DevBuf spectra;    // forward spectra X[d][b][N]
-	ugsdr_gpu::DevBuf slab;       // per-CTA four-step slabs
-	ugsdr_gpu::DevBuf cells;      // per (code, doppler) records
-	ugsdr_gpu::DevBuf results;    // per code results
-	ugsdr_gpu::DevBuf params;     // small per-job parameter arrays
+	ugsdr_gpu::Workspace ws;      // acquisition scratch of the synchronous entry points
 	ugsdr_gpu::DevBuf op_a, op_b, op_c;  // per-op entry staging
 	int sm_count = 0;
 	size_t smem_optin = 0;
@@ -182,6 +198,21 @@ namespace ugsdr_gpu {
 	bool fits_single_cta(ugsdr_ctx* ctx, int n);
 	const float* get_lut(ugsdr_ctx* ctx);
 	void note_launch(ugsdr_ctx* ctx, int n = 1);
+
+	// batched acquisition (acq.cu): a batch of jobs is enqueued on `stream` with
+	// the scratch of `ws`; cells are copied into host_cells (pinned for overlap);
+	// finish_jobs turns them into per-code results once the stream reached them.
+	struct EnqueuedBatch {
+		std::vector<std::vector<double>> grids;    // Doppler grid per job
+		std::vector<size_t> cell_offsets;          // per job, in cells
+		size_t n_cells = 0;
+	};
+	EnqueuedBatch enqueue_jobs(ugsdr_ctx* ctx, Workspace& ws, cudaStream_t stream, const ugsdr_acq_job* jobs, int n_jobs,
+		void* host_cells);
+	void finish_jobs(const EnqueuedBatch& b, const ugsdr_acq_job* jobs, int n_jobs, const void* host_cells,
+		ugsdr_acq_result* const* results, ugsdr_acq_cell* cells_out);
+	// Device bytes a batch needs beyond what `ws` already holds (admission control).
+	size_t jobs_device_bytes(ugsdr_ctx* ctx, const ugsdr_acq_job* jobs, int n_jobs);
 
 	// shared host helpers (codes.cpp)
 	int prn_code(int signal, int sv, float* out, size_t cap, size_t* len);
