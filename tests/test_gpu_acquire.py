@@ -217,3 +217,28 @@ def test_invalid_jobs(ctx, acq_golden, golden_codes):
     with pytest.raises(L.UgsdrError) as e:
         ctx.code_release(h)
     assert e.value.status == L.E_NOT_FOUND
+
+
+@pytest.mark.parametrize("budget_mb", ["1", "8"])
+def test_doppler_chunking_same_results(ctx, acq_golden, golden_codes, monkeypatch, budget_mb):
+    """A small spectra budget splits the Doppler grid into several launches
+    (small path: 4000-point blocks; large path: 50,000-point blocks); results
+    must not change."""
+    ca = unpack_codes(golden_codes, "gps_l1ca")
+    raw = acq_golden["acq_raw"]
+    hs = [ctx.code_put(ca[p], 4000) for p in acq_golden["acq_prns"][:3]]
+    raw50 = signals.gps_l1_config(seed=9, codes={i: ca[i] for i in range(4)}, fs=50e6, ms=2, visible=2,
+                                  sample_type="ci16")[0]
+    hl = [ctx.code_put(ca[p], 50000) for p in range(3)]
+    try:
+        jobs = [ctx.make_job(raw, L.SAMPLES_CI8, 4e6, 4000, 10, hs, 5000, 500),
+                ctx.make_job(raw50, L.SAMPLES_CI16, 50e6, 50000, 2, hl, 2000, 500)]
+        whole = [ctx.acquire(j, cells=True)[1] for j in jobs]
+        monkeypatch.setenv("UGSDR_SPECTRA_BUDGET_MB", budget_mb)
+        chunked = [ctx.acquire(j, cells=True)[1] for j in jobs]
+        for a, b in zip(whole, chunked):
+            np.testing.assert_array_equal(a["index"], b["index"])
+            np.testing.assert_allclose(a["level"], b["level"], rtol=1e-6)
+    finally:
+        for h in hs + hl:
+            ctx.code_release(h)

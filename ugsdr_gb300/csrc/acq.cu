@@ -248,9 +248,11 @@ namespace ugsdr_gpu {
 		UG_CUDA(cudaStreamSynchronize(ctx->stream));
 	}
 
-	void large_job(ugsdr_ctx* ctx, const ugsdr_acq_job& job, const AcqParams& base, const JobLaunchShape& s, char* scratch) {
+	// One Doppler chunk of nd bins (base.d_base first): forward over nd x K
+	// blocks, inverse over the chunk's s.rows = codes x nd rows.
+	void large_job(ugsdr_ctx* ctx, const ugsdr_acq_job& job, const AcqParams& base, const JobLaunchShape& s, int nd, char* scratch) {
 		BatchedParams p = batched_params(ctx, base, s.n);
-		const int items = base.n_doppler * base.k_blocks;
+		const int items = nd * base.k_blocks;
 		p.out = base.spectra;
 		{
 			KernelTimer timer(ctx, "acq_forward_large");
@@ -391,7 +393,19 @@ namespace ugsdr_gpu {
 		}
 	}
 
-	// Launches one job on ctx->stream; cells/best_bin stay on the device.
+	// Doppler bins per launch: mixed spectra (bins x K x N complex) within 4 GB
+	// (UGSDR_SPECTRA_BUDGET_MB overrides, e.g. to exercise chunking in tests).
+	int chunk_bins(const JobLaunch& L) {
+		const size_t per_bin = sizeof(float2) * static_cast<size_t>(L.n) * L.k;
+		size_t budget = static_cast<size_t>(4) << 30;
+		if (const char* env = std::getenv("UGSDR_SPECTRA_BUDGET_MB"))
+			budget = std::max<size_t>(1, std::strtoull(env, nullptr, 10)) << 20;
+		return static_cast<int>(std::max<size_t>(1, std::min<size_t>(L.grid.size(), budget / per_bin)));
+	}
+
+	void launch_chunk(ugsdr_ctx* ctx, const ugsdr_acq_job& job, const JobLaunch& L, AcqParams& p, int nd, char* scratch);
+
+	// Launches one job on ctx->stream; cells stay on the device.
 	void launch_job(ugsdr_ctx* ctx, const ugsdr_acq_job& job, const JobLaunch& L, const void* dev_samples,
 		AcqCellDev* cells, int* best_bin, uint32_t* adders_dev, const float2** code_ptrs_dev, float2* spectra,
 		char* scratch) {
@@ -415,10 +429,21 @@ namespace ugsdr_gpu {
 		p.spectra = spectra;
 		p.codes = code_ptrs_dev;
 		p.cells = cells;
+		// the Doppler grid runs in chunks whose spectra fit the spectra budget
+		const int n_bins = static_cast<int>(L.grid.size());
+		const int chunk = chunk_bins(L);
+		for (int d0 = 0; d0 < n_bins; d0 += chunk) {
+			p.d_base = d0;
+			launch_chunk(ctx, job, L, p, std::min(chunk, n_bins - d0), scratch);
+		}
+		(void)best_bin;
+	}
+
+	void launch_chunk(ugsdr_ctx* ctx, const ugsdr_acq_job& job, const JobLaunch& L, AcqParams& p, int nd, char* scratch) {
 		if (!L.large) {
 			p.plan = to_dev(get_plan(ctx, L.n));
 			const size_t smem_f = 2 * sizeof(float2) * L.n;
-			const int grid_f = p.n_doppler * L.k;
+			const int grid_f = nd * L.k;
 			{
 			KernelTimer timer(ctx, "acq_forward");
 			switch (job.sample_type) {
@@ -444,18 +469,18 @@ namespace ugsdr_gpu {
 			const size_t smem_i = 2 * sizeof(float2) * L.n + sizeof(float) * L.m;
 			set_smem(acq_inverse_kernel, smem_i);
 			KernelTimer timer(ctx, "acq_inverse");
-			acq_inverse_kernel<<<p.n_doppler * L.n_codes, kThreads, smem_i, ctx->stream>>>(p);
+			acq_inverse_kernel<<<nd * L.n_codes, kThreads, smem_i, ctx->stream>>>(p);
 			note_launch(ctx);
 		}
 		else {
-			large_job(ctx, job, p, shape_of(L), scratch);
+			JobLaunchShape s = shape_of(L);
+			s.rows = nd * L.n_codes;
+			large_job(ctx, job, p, s, nd, scratch);
 		}
-		acq_select_kernel<<<(L.n_codes + 127) / 128, 128, 0, ctx->stream>>>(cells, L.n_codes, p.n_doppler, best_bin);
-		note_launch(ctx);
 	}
 
 	size_t spectra_bytes(const JobLaunch& L) {
-		return sizeof(float2) * static_cast<size_t>(L.n) * L.k * L.grid.size();
+		return sizeof(float2) * static_cast<size_t>(L.n) * L.k * chunk_bins(L);
 	}
 
 	namespace {

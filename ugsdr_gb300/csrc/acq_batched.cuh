@@ -104,7 +104,7 @@ namespace ugsdr_gpu {
 		float2 v = load_sample<ST>(p.base.samples, g);
 		if (p.base.fe_on)
 			v = table_mix(v, g, p.base.fe_adder, 0u, lut);
-		return table_mix(v, g, p.base.adders[d], p.base.phase0, lut);
+		return table_mix(v, g, p.base.adders[p.base.d_base + d], p.base.phase0, lut);
 	}
 
 	// grid: items * ceil(N2 / cw)
@@ -336,7 +336,7 @@ namespace ugsdr_gpu {
 		}
 		const int row = p.row0 + lrow;
 		const int c = row % q.n_codes;
-		const int d = row / q.n_codes;
+		const int d = q.d_base + row / q.n_codes;  // rows are local to the Doppler chunk
 		const double mean = ts / m;
 		const double var = m > 1 ? (tq - ts * mean) / (m - 1) : 0.0;
 		AcqCellDev cell;
@@ -365,7 +365,7 @@ namespace ugsdr_gpu {
 		}
 		const int row = p.row0 + lrow;
 		const int c = row % q.n_codes;
-		const int d = row / q.n_codes;
+		const int d = q.d_base + row / q.n_codes;
 		reduce_cell(ag, m, q.cells + static_cast<size_t>(c) * q.n_doppler + d);
 	}
 }

@@ -148,6 +148,7 @@ namespace ugsdr_gpu {
 		uint32_t phase0;
 		uint32_t fe_adder;            // front-end Translate adder (used when fe_on)
 		int fe_on;
+		int d_base;                   // first Doppler bin of this launch (grid processed in chunks)
 		const float* lut;             // 80-entry sine table
 		float2* spectra;              // [d][b][N]
 		const float2* const* codes;   // per code spectrum
@@ -166,7 +167,7 @@ namespace ugsdr_gpu {
 		if (threadIdx.x < 80)
 			lut[threadIdx.x] = p.lut[threadIdx.x];
 		__syncthreads();
-		const uint32_t adder = p.adders[d];
+		const uint32_t adder = p.adders[p.d_base + d];
 		const uint64_t base = static_cast<uint64_t>(blk) * p.n;
 		for (int i = threadIdx.x; i < p.n; i += blockDim.x) {
 			const uint64_t g = base + i;
@@ -311,7 +312,7 @@ namespace ugsdr_gpu {
 			}
 			__syncthreads();
 		}
-		reduce_cell(acc, p.m, p.cells + static_cast<size_t>(c) * p.n_doppler + d);
+		reduce_cell(acc, p.m, p.cells + static_cast<size_t>(c) * p.n_doppler + p.d_base + d);
 	}
 
 	// per code: keep the first Doppler with a strictly greater level (fse.hpp:265)

@@ -33,19 +33,21 @@ namespace ugsdr_gpu {
 			throw Error(status, msg);
 	}
 
-	// Device buffer that only grows (scratch reused across calls).
+	// Device buffer that only grows (scratch reused across calls).  With a
+	// stream it allocates and frees stream-ordered (cudaMallocAsync /
+	// cudaFreeAsync), which, unlike cudaFree, does not wait for the whole device.
 	struct DevBuf {
 		void* ptr = nullptr;
 		size_t bytes = 0;
+		cudaStream_t stream = nullptr;  // set: stream-ordered allocation on it
 		void reserve(size_t n) {
 			if (n <= bytes)
 				return;
-			if (ptr)
-				cudaFree(ptr);
-			ptr = nullptr;
-			bytes = 0;
-			if (cudaMalloc(&ptr, n) != cudaSuccess) {
+			release();
+			const cudaError_t e = stream ? cudaMallocAsync(&ptr, n, stream) : cudaMalloc(&ptr, n);
+			if (e != cudaSuccess) {
 				cudaGetLastError();
+				ptr = nullptr;
 				throw Error(UGSDR_E_NOMEM, "device allocation of " + std::to_string(n) + " bytes failed");
 			}
 			bytes = n;
@@ -53,8 +55,12 @@ namespace ugsdr_gpu {
 		template <typename T>
 		T* as() const { return static_cast<T*>(ptr); }
 		void release() {
-			if (ptr)
-				cudaFree(ptr);
+			if (ptr) {
+				if (stream)
+					cudaFreeAsync(ptr, stream);
+				else
+					cudaFree(ptr);
+			}
 			ptr = nullptr;
 			bytes = 0;
 		}
@@ -103,6 +109,9 @@ namespace ugsdr_gpu {
 		DevBuf cells;      // per (code, doppler) records
 		DevBuf params;     // per-job parameter arrays
 		size_t reserved() const { return samples.bytes + spectra.bytes + slab.bytes + cells.bytes + params.bytes; }
+		void set_stream(cudaStream_t s) {
+			samples.stream = spectra.stream = slab.stream = cells.stream = params.stream = s;
+		}
 		void release() {
 			samples.release();
 			spectra.release();

@@ -20,23 +20,29 @@
 using namespace ugsdr_gpu;
 
 namespace {
+	// Pinned host staging that grows without freeing while the server runs
+	// (cudaFreeHost waits for the device); outgrown buffers are freed at exit.
 	struct PinnedBuf {
 		void* ptr = nullptr;
 		size_t bytes = 0;
+		std::vector<void*> outgrown;
 		void reserve(size_t n) {
 			if (n <= bytes)
 				return;
 			if (ptr)
-				cudaFreeHost(ptr);
+				outgrown.push_back(ptr);
 			ptr = nullptr;
 			bytes = 0;
 			if (cudaHostAlloc(&ptr, n, cudaHostAllocDefault) != cudaSuccess) {
 				cudaGetLastError();
+				ptr = nullptr;
 				throw Error(UGSDR_E_NOMEM, "pinned host allocation failed");
 			}
 			bytes = n;
 		}
 		~PinnedBuf() {
+			for (void* p : outgrown)
+				cudaFreeHost(p);
 			if (ptr)
 				cudaFreeHost(ptr);
 		}
@@ -243,6 +249,7 @@ int ugsdr_server_create(ugsdr_ctx* ctx, const ugsdr_server_config* cfg, ugsdr_se
 		for (auto& sl : s->slots) {
 			UG_CUDA(cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking));
 			UG_CUDA(cudaEventCreateWithFlags(&sl.event, cudaEventDisableTiming));
+			sl.ws.set_stream(sl.stream);  // scratch grows stream-ordered, without a device-wide wait
 		}
 		ugsdr_server* raw = s.get();
 		s->worker = std::thread([raw] { raw->run(); });
@@ -338,8 +345,10 @@ int ugsdr_server_destroy(ugsdr_server* server) {
 	if (server->worker.joinable())
 		server->worker.join();
 	for (auto& sl : server->slots) {
+		sl.ws.release();  // stream-ordered frees, before the stream goes
 		if (sl.stream)
 			cudaStreamSynchronize(sl.stream);
+		sl.ws.set_stream(nullptr);
 		if (sl.event)
 			cudaEventDestroy(sl.event);
 		if (sl.stream)
