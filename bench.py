@@ -101,7 +101,51 @@ def gps_4mhz_workload(seed: int = 1):
     return jobs, raw
 
 
-WORKLOADS = {"multi": multi_workload, "gps_l1_4mhz": gps_4mhz_workload, "gal_small": gal_small_workload}
+def l5_weak_workload(seed: int = 5):
+    """Weak-signal GPS L5I search: real int8 at 40 MHz, IF 10 MHz, 200 ms;
+    mixed and resampled to 20.46 MHz complex on the device (L = 1023, M = 2000),
+    10 ms coherent (204,600-point FFT) with NH10 in the replica, x 20 blocks,
+    +-5 kHz at 25 Hz (401 bins), 63 PRNs: 5.17e9 cells per search.  The
+    reference's L5I table holds PRNs 1-32, so searches 33-63 reuse the codes
+    of PRNs 1-31 (same work per cell)."""
+    from ugsdr_gb300 import _lib as L
+    from ugsdr_gb300 import api, signals
+    l5 = {p: api.prn_code(L.GPS_L5I, p) for p in range(32)}
+    raw, _ = signals.l5_weak_config(seed, l5)
+    jobs = [dict(system="l5", codes=[l5[p % 32] for p in range(63)], n=204600, k=20, step=25.0, fe=-10e6, if_=10e6,
+                 fs=20.46e6, fs_in=40e6, repeats=10, sign_mask=signals.nh10_mask(), sign_segment=20460)]
+    return jobs, raw
+
+
+WORKLOADS = {"multi": multi_workload, "gps_l1_4mhz": gps_4mhz_workload, "gal_small": gal_small_workload,
+             "l5_weak": l5_weak_workload}
+WORKLOAD_DESC = {
+    "multi": "multi-constellation batch: int16 I/Q 50 MHz 40 ms; GPS L1 C/A 32x41x50000x40, "
+             "GLONASS L1OF 14ch x41x50000x40, Galileo E1B 36x161x200000x10",
+    "gps_l1_4mhz": "GPS L1 C/A int8 4 MHz 10 ms; 32 PRN x 21 Doppler x 4000 x 10",
+    "gal_small": "Galileo E1B 4 codes x 5 Doppler x 200000 x 10 (profiling case)",
+    "l5_weak": "GPS L5I weak-signal: real int8 IF 40 MHz 200 ms -> 20.46 MHz complex on device; "
+               "63 PRN x 401 Doppler x 204600 (10 ms, NH10 wiped) x 20",
+}
+
+
+def sample_type_of(raw):
+    from ugsdr_gb300 import _lib as L
+    if raw.ndim == 1:
+        return L.SAMPLES_RI8
+    return L.SAMPLES_CI16 if raw.dtype == np.int16 else L.SAMPLES_CI8
+
+
+def oracle_code(pyoracle, j, chips):
+    """The job's replica as the reference builds it: RepeatCodeNTimes +
+    SequentialUpsampler (fse.hpp:295), then the per-period signs."""
+    reps = j.get("repeats", 1)
+    code = pyoracle.upsample(np.tile(chips, reps), j["n"])
+    seg = j.get("sign_segment", 0)
+    for s in range(32):
+        if (j.get("sign_mask", 0) >> s) & 1:
+            code[s * seg:(s + 1) * seg] *= -1
+    return code
 
 
 def n_doppler(step, rng=5000.0):
@@ -182,13 +226,14 @@ def run_ours(args, world, rank):
     torch.cuda.set_device(dev)
     jobs, raw = WORKLOADS[args.config]()
     fs = jobs[0].get("fs", FS)
-    stype = L.SAMPLES_CI16 if raw.dtype == np.int16 else L.SAMPLES_CI8
+    stype = sample_type_of(raw)
     ctx = api.Context(dev)
     stream = torch.cuda.Stream()
     ctx.set_stream(stream.cuda_stream)
     handles = []
     for j in jobs:
-        hs = [ctx.code_put(c, j["n"], repeats=1) for c in j["codes"]]
+        hs = [ctx.code_put(c, j["n"], repeats=j.get("repeats", 1), sign_mask=j.get("sign_mask", 0),
+                           sign_segment=j.get("sign_segment", 0)) for c in j["codes"]]
         handles.append(hs)
     # inputs resident in HBM for `value`; pinned host copy for `e2e`
     d_raw = torch.from_numpy(raw.copy()).cuda(dev)
@@ -201,8 +246,10 @@ def run_ours(args, world, rank):
         out = []
         for j, hs in zip(jobs, handles):
             src = d_raw.data_ptr() if on_device else h_np
+            fs_in = j.get("fs_in", 0.0)
             out.append(ctx.make_job(src, stype, fs, j["n"], j["k"], hs, 5000.0, j["step"], n_samples=n_samples,
-                                    on_device=on_device, frontend_frequency=j["fe"], intermediate_frequency=j["if_"]))
+                                    on_device=on_device, frontend_frequency=j["fe"], intermediate_frequency=j["if_"],
+                                    input_sampling_rate=fs_in, code_offset_ratio=(fs_in / fs) if fs_in else 1.0))
         return out
 
     dev_jobs, host_jobs = mk(True), mk(False)
@@ -279,9 +326,7 @@ def run_ours(args, world, rank):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic (seeded int16/int8 I/Q captures; Galileo E1B chips from the reference's code tables)",
-        "config": {"workload": "multi-constellation batch: int16 I/Q 50 MHz 40 ms; GPS L1 C/A 32x41x50000x40, "
-                               "GLONASS L1OF 14ch x41x50000x40, Galileo E1B 36x161x200000x10"
-                   if args.config == "multi" else "GPS L1 C/A int8 4 MHz 10 ms; 32 PRN x 21 Doppler x 4000 x 10",
+        "config": {"workload": WORKLOAD_DESC[args.config],
                    "cells_per_step": cells, "jobs_per_step": len(jobs), "parallelism": f"replicas x{world}",
                    "l2": "flushed between steps (256 MB write); working set > L2"},
         "e2e": {"value": world * cells / t_e2e, "unit": "cells/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
@@ -320,9 +365,9 @@ def served_requests(seed: int, n_req: int, rate: float = 2000.0):
     for _ in range(n_req):
         t += rng.exponential(1 / rate)
         sysname = ["gps", "l5i", "e1b"][rng.integers(3)]
-        chips, rate, period_ms = systems[sysname]
+        chips, chip_rate, period_ms = systems[sysname]
         fs = rates[rng.integers(len(rates))]
-        if fs <= rate:  # the code must be oversampled
+        if fs <= chip_rate:  # the code must be oversampled
             fs = rates[-1]
         t_ms = int(rng.integers(1, 21))
         t_ms = max(period_ms, t_ms // period_ms * period_ms)
@@ -431,13 +476,252 @@ def run_served(args):
         "value": served, "unit": "cells/s", "n_gpus": 1, "requests": len(jobs),
         "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
         "offered_rate_req_s": args.rate, "wall_s": t_total, "max_inflight_seen": stats["max_inflight_seen"],
+        "offered_load": args.rate * float(np.mean(cells)) / (sum(cells) / t_seq),
         "sequential_cells_s": sum(cells) / t_seq, "plain_cells_s": plain, "served_over_plain": served / plain,
         "served_over_sequential": served / (sum(cells) / t_seq),
         "plain_sample": f"{rows} (code, Doppler) rows of a {n}-sample x {req['k']}-block request, per-op entries",
-        "config": {"workload": "served stream: Poisson 2000 req/s, fs {2.046,4,10.23,20.46,50} MHz, Tcoh 1-20 ms, "
+        "config": {"workload": f"served stream: Poisson {args.rate:g} req/s, fs {{2.046,4,10.23,20.46,50}} MHz, Tcoh 1-20 ms, "
                                "K 1-40, 1-63 codes of L1 C/A / L5I / E1B, int8/int16", "inflight": args.inflight,
                    "cells_total": int(sum(cells))},
     }
+
+
+# ------------------------------------------------------------ tracking bank
+TRACK_FS = 20e6
+TRACK_FLOPS_PER_CHANNEL_SAMPLE = 26  # carrier wipe-off 6 + five taps x (I, Q) x FMA 2
+TRACK_OUT_BYTES = 88                 # ugsdr_track_output per channel-epoch
+
+
+def golden_chips(name):
+    z = np.load(ROOT / "tests" / "golden" / "codes.npz")
+    n = int(z[f"{name}_len"])
+    bits = np.unpackbits(z[name], axis=1)[:, :n]
+    return (1.0 - 2.0 * bits).astype(np.float32)
+
+
+def track_capture(dev, seconds, seed=3, n_channels=256, sigma=20.0):
+    """256-channel tracking input, synthesised on the device in float64 phase
+    (10 s at 20 MHz is 2e8 int16 I/Q samples): 12 GPS L1 C/A and 12 Galileo E1
+    emitters (E1B data at 250 sps and E1C pilot, BOC(1,1), half the power
+    each), Doppler +-5 kHz with a 0.5 Hz/s ramp, C/N0 35-50 dB-Hz, AWGN sigma
+    20 LSB.  Channels: the 36 signal channels (GPS, E1B, E1C) started at the
+    true code phase and initial Doppler, then channels on the other codes
+    (random phase and Doppler) up to n_channels.  Returns the device capture,
+    the channel list and the code table."""
+    import torch
+    from ugsdr_gb300 import _lib as L
+    from ugsdr_gb300 import api
+    rng = np.random.default_rng(seed)
+    fs = TRACK_FS
+    device = f"cuda:{dev}" if isinstance(dev, int) else dev
+    gps = [api.prn_code(L.GPS_L1CA, p) for p in range(32)]
+    e1b, e1c = golden_chips("galileo_e1b"), golden_chips("galileo_e1c")
+    codes = gps + list(e1b) + list(e1c)
+    rate_of = [1.023e6] * 32 + [2.046e6] * 100
+    ems = []
+    for p in rng.choice(32, 12, replace=False):
+        ems.append(dict(parts=[(int(p), 1.0, 50.0)], rate=1.023e6, delay=rng.uniform(0, 1023),
+                        f0=rng.uniform(-5000, 5000), cn0=rng.uniform(35, 50), phi=rng.uniform(0, 1)))
+    for p in rng.choice(50, 12, replace=False):
+        h = 1 / np.sqrt(2)
+        ems.append(dict(parts=[(32 + int(p), h, 250.0), (82 + int(p), -h, 0.0)], rate=2.046e6,
+                        delay=rng.uniform(0, 8184), f0=rng.uniform(-5000, 5000), cn0=rng.uniform(35, 50),
+                        phi=rng.uniform(0, 1)))
+    n = int(fs * seconds)
+    cap = torch.empty((n, 2), dtype=torch.int16, device=device)
+    gen = torch.Generator(device=device)
+    gen.manual_seed(seed)
+    code_t = [torch.tensor(c, device=device) for c in codes]
+    bits = {}
+    chunk = 10_000_000
+    for a in range(0, n, chunk):
+        m = min(chunk, n - a)
+        t = (a + torch.arange(m, dtype=torch.float64, device=device)) / fs
+        re = torch.zeros(m, dtype=torch.float32, device=device)
+        im = torch.zeros_like(re)
+        for k, e in enumerate(ems):
+            amp = sigma * np.sqrt(2.0 * 10 ** (e["cn0"] / 10.0) / fs)
+            pos = t * (e["rate"] * (1 + e["f0"] / 1575.42e6)) - e["delay"]
+            sig = torch.zeros_like(re)
+            for j, (ci, w, drate) in enumerate(e["parts"]):
+                c = code_t[ci]
+                chip = torch.remainder(torch.floor(pos), len(codes[ci])).long()
+                part = c[chip] * w
+                if drate > 0:
+                    key = (k, j)
+                    if key not in bits:
+                        nb = int(seconds * drate) + 4
+                        bits[key] = torch.tensor(rng.choice([-1.0, 1.0], size=nb).astype(np.float32), device=device)
+                    part = part * bits[key][torch.floor(t * drate).long() + 1]
+                sig += part
+            cyc = e["f0"] * t + 0.25 * t * t + e["phi"]  # 0.5 Hz/s ramp
+            ang = (2 * np.pi * (cyc - torch.floor(cyc))).float()
+            re += amp * sig * torch.cos(ang)
+            im += amp * sig * torch.sin(ang)
+        noise = torch.randn((m, 2), generator=gen, device=device) * sigma
+        x = torch.stack([re, im], dim=1) + noise
+        cap[a:a + m] = torch.clamp(torch.round(x), -32768, 32767).to(torch.int16)
+        del t, re, im, noise, x
+    chans = []
+    for e in ems:
+        for ci, _, _ in e["parts"]:
+            period = len(codes[ci]) / rate_of[ci]  # s
+            cp = (e["delay"] / e["rate"] * fs) % (period * fs)
+            chans.append(dict(code=ci, fs=fs, code_frequency=rate_of[ci], code_phase=float(round(cp)),
+                              carrier_frequency=e["f0"], boc=int(ci >= 32)))
+    used = {c["code"] for c in chans}
+    others = [c for c in range(len(codes)) if c not in used]
+    i = 0
+    while len(chans) < n_channels:
+        ci = others[i % len(others)]
+        i += 1
+        period = len(codes[ci]) / rate_of[ci]
+        chans.append(dict(code=ci, fs=fs, code_frequency=rate_of[ci], code_phase=float(rng.integers(0, int(period * fs))),
+                          carrier_frequency=rng.uniform(-5000, 5000), boc=int(ci >= 32)))
+    return cap, chans, codes
+
+
+TRACK_CFG = dict(early_late=0.15, very_early_late=0.5, pll_bw=15.0, dll_bw=1.0, fll_bw=0.0)
+
+
+def track_cpu_baseline(cap, chans, codes, threads=None, epochs=2000):
+    """FP64 oracle channel loop (oracle/track_oracle.cpp) on the host cores:
+    one channel per thread over `epochs` ms of the capture."""
+    from concurrent.futures import ThreadPoolExecutor
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import pyoracle
+    threads = threads or os.cpu_count() or 1
+    spm = int(TRACK_FS / 1000)
+    raw = cap[: spm * epochs].cpu().numpy().astype(np.float32)
+    x = (raw[:, 0] + 1j * raw[:, 1]).astype(np.complex64)
+    sel = chans[:threads]
+
+    def one(ch):
+        return pyoracle.track(x, spm, epochs, codes[ch["code"]], TRACK_FS, ch["code_frequency"], ch["code_phase"],
+                              ch["carrier_frequency"], **TRACK_CFG)
+
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(threads) as ex:
+        list(ex.map(one, sel))
+    dt = time.perf_counter() - t0
+    return {"value": len(sel) * spm * epochs / dt, "unit": "channel-samples/s", "cores": threads, "kind": "port",
+            "sample": f"{len(sel)} channels x {epochs} epochs of the same capture in {dt:.2f}s "
+                      "(FP64 oracle loop, one channel per thread)"}
+
+
+def run_track(args, world, rank):
+    """Tracking correlator bank: 256 channels over `--track-seconds` (default
+    10 s) of 20 MHz int16 I/Q per step; one step = one ugsdr_track_run of the
+    whole capture on a freshly created bank."""
+    import torch
+    from ugsdr_gb300 import _lib as L
+    from ugsdr_gb300 import api
+    if args.impl == "reference" and rank != 0:
+        return None
+    dev = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(dev)
+    seconds = args.track_seconds
+    cap, chans, codes = track_capture(dev, seconds)
+    n_epochs = int(round(seconds * 1000))
+    spm = int(TRACK_FS / 1000)
+    nch = len(chans)
+    if args.impl == "reference":
+        if rank != 0:
+            return None
+        vals = [track_cpu_baseline(cap, chans, codes) for _ in range(args.warmup + args.steps)][args.warmup:]
+        v = float(np.mean([b["value"] for b in vals]))
+        return {"metric": "tracking channel-samples/s", "value": v, "unit": "channel-samples/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": nch * n_epochs * spm / v * 1e3,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "impl": "reference", "config": {"workload": f"tracking bank {nch} ch, 20 MHz int16, {seconds} s"},
+                "cpu_baseline": {k: vals[-1][k] for k in ("value", "unit", "cores", "kind", "sample")},
+                "e2e": {"value": v, "unit": "channel-samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    ctx = api.Context(dev)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    d_out = torch.empty(n_epochs * nch * TRACK_OUT_BYTES, dtype=torch.uint8, device=f"cuda:{dev}")
+    h_cap = torch.empty(cap.shape, dtype=cap.dtype, pin_memory=True)
+    h_cap.copy_(cap)
+    h_out = torch.empty(n_epochs * nch * TRACK_OUT_BYTES, dtype=torch.uint8, pin_memory=True)
+    h_out_np = h_out.numpy().view(api.TRACK_DTYPE).reshape(n_epochs, nch)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{dev}")
+
+    def bank():
+        return api.TrackBank(ctx, chans, codes, **TRACK_CFG)
+
+    def step(b, on_device):
+        if on_device:
+            b.run_device(cap.data_ptr(), L.SAMPLES_CI16, n_epochs, d_out.data_ptr())
+        else:
+            b.run(h_cap.numpy(), L.SAMPLES_CI16, n_epochs, out=h_out_np)
+
+    for _ in range(args.warmup):
+        b = bank()
+        step(b, True)
+        torch.cuda.synchronize()
+        b.close()
+
+    def timed(k, on_device):
+        times = []
+        l0 = ctx.launch_count()
+        for _ in range(k):
+            b = bank()
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            stream.synchronize()
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record(stream)
+            t0 = time.perf_counter()
+            step(b, on_device)
+            e.record(stream)
+            e.synchronize()
+            times.append(max(s.elapsed_time(e) / 1e3, time.perf_counter() - t0 if not on_device else 0.0))
+            b.close()
+        return times, (ctx.launch_count() - l0) / k
+
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler() as clk:
+        times, launches = timed(args.steps, True)
+    t_step = float(np.mean(times))
+    if world > 1:
+        t = torch.tensor([t_step], device=f"cuda:{dev}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_step = float(t.item())
+    e2e_times, _ = timed(max(2, args.steps // 2), False)
+    t_e2e = float(np.mean(e2e_times))
+    ch_samples = nch * n_epochs * spm
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    sm_max = peaks.get("sm_max_mhz", 2070.0)
+    n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
+    fp32_peak = n_sm * 128 * 2 * sm_max * 1e6 / 1e12
+    achieved = ch_samples * TRACK_FLOPS_PER_CHANNEL_SAMPLE / t_step / 1e12
+    alg_bytes = n_epochs * spm * 4 + n_epochs * nch * TRACK_OUT_BYTES
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    line = {
+        "metric": "tracking channel-samples/s", "value": world * ch_samples / t_step, "unit": "channel-samples/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 loops)",
+        "data": "synthetic (device-synthesised int16 I/Q, seeded)",
+        "config": {"workload": f"tracking bank: {nch} channels (GPS L1 C/A + Galileo E1B/E1C BOC(1,1)), VE/E/P/L/VL "
+                               f"0.5/0.15 chip, PLL 15 Hz, DLL 1 Hz, 1 ms epochs; int16 I/Q 20 MHz, {seconds} s",
+                   "real_time_factor": seconds / t_step, "channels": nch, "epochs": n_epochs,
+                   "parallelism": f"replicas x{world}", "l2": "flushed between steps (256 MB write); input 800 MB > L2"},
+        "e2e": {"value": world * ch_samples / t_e2e, "unit": "channel-samples/s", "h2d_bytes_per_step": int(cap.numel() * 2),
+                "d2h_bytes_per_step": n_epochs * nch * TRACK_OUT_BYTES, "ms_per_step": t_e2e * 1e3},
+        "gpu_launches": launches,
+        "roofline": {"bound": "fp32", "kernel": "track_bank", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                     "frac": achieved / fp32_peak, "traffic": None,
+                     "flops_per_channel_sample": TRACK_FLOPS_PER_CHANNEL_SAMPLE,
+                     "peak_source": f"{n_sm} SMs x 128 FP32 lanes x 2 x sm_max_mhz {sm_max} (MEASURED_PEAKS.json)",
+                     "hbm": {"achieved": alg_bytes / t_step / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                             "frac": alg_bytes / t_step / 1e9 / hbm_peak}},
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = track_cpu_baseline(cap, chans, codes)
+    return line
 
 
 # ------------------------------------------------------------ CPU reference
@@ -455,15 +739,27 @@ def cpu_baseline(args, jobs, raw, fs, budget_s: float = 20.0):
     seen = {}
     for j in jobs:
         key = (j["system"], j["n"], j["k"])
+        fs_in = j.get("fs_in", 0.0)
+        # front-end jobs: 4 blocks timed and scaled to K (the oracle resampler
+        # walks every upsampled index, 1023 per input at 40 -> 20.46 MHz)
+        ks = min(j["k"], 4) if fs_in else j["k"]
+        if fs_in:
+            need = int(np.ceil(j["n"] * ks * fs_in / fs)) + 2
+            t0 = time.perf_counter()
+            xx = pyoracle.table_mix(x[:need], fs_in, j["fe"]) if j["fe"] else x[:need]
+            xx = pyoracle.resample(xx, int(fs), int(fs_in))[: j["n"] * ks]
+            total_t += (time.perf_counter() - t0) * j["k"] / ks  # once per job
+        else:
+            xx = pyoracle.table_mix(x[: j["n"] * j["k"]], fs, j["fe"]) if j["fe"] else x[: j["n"] * j["k"]]
         if key not in seen:
             ncodes = min(len(j["codes"]), threads)
-            codes = np.stack([pyoracle.upsample(c, j["n"]) for c in j["codes"][:ncodes]])
-            xx = pyoracle.table_mix(x[: j["n"] * j["k"]], fs, j["fe"]) if j["fe"] else x[: j["n"] * j["k"]]
+            codes = np.stack([oracle_code(pyoracle, j, c) for c in j["codes"][:ncodes]])
             t0 = time.perf_counter()
-            pyoracle.acquire_many(xx, j["n"], j["k"], codes, fs, 0.0, 1.0, threads=threads)
+            pyoracle.acquire_many(xx, j["n"], ks, codes, fs, 0.0, 1.0, threads=threads)
             dt = time.perf_counter() - t0
-            seen[key] = dt / (ncodes * j["n"])  # seconds per cell
-            sample_desc.append(f"{j['system']}: {ncodes} codes x 1 Doppler x {j['n']} x {j['k']} blocks in {dt:.2f}s")
+            seen[key] = dt / (ncodes * j["n"]) * j["k"] / ks  # seconds per cell
+            sample_desc.append(f"{j['system']}: {ncodes} codes x 1 Doppler x {j['n']} x {ks} blocks in {dt:.2f}s"
+                               + (f" (scaled to {j['k']} blocks; front end timed on the same prefix)" if ks != j["k"] else ""))
         total_t += seen[key] * job_cells(j)
     cells = sum(job_cells(j) for j in jobs)
     return {"value": cells / total_t, "unit": "cells/s", "cores": threads, "kind": "port",
@@ -499,7 +795,8 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--config", choices=sorted(WORKLOADS), default="multi")
+    ap.add_argument("--config", choices=sorted(WORKLOADS) + ["track"], default="multi")
+    ap.add_argument("--track-seconds", type=float, default=10.0, help="capture length of --config track")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--served", action="store_true", help="run the served request stream instead")
     ap.add_argument("--requests", type=int, default=24, help="requests in the served stream")
@@ -514,7 +811,10 @@ def main():
     if args.served:
         print(json.dumps(run_served(args)), flush=True)
         return
-    line = run_ours(args, world, rank) if args.impl == "ours" else run_reference(args, world, rank)
+    if args.config == "track":
+        line = run_track(args, world, rank)
+    else:
+        line = run_ours(args, world, rank) if args.impl == "ours" else run_reference(args, world, rank)
     if rank == 0 and line is not None:
         print(json.dumps(line), flush=True)
     if world > 1 and args.impl == "ours":

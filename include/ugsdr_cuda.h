@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define UGSDR_CUDA_ABI_VERSION 1
+#define UGSDR_CUDA_ABI_VERSION 2
 
 enum ugsdr_status {
 	UGSDR_OK = 0,
@@ -151,6 +151,15 @@ typedef struct ugsdr_acq_job {
 	int n_codes;
 	int statistic;             /* ugsdr_statistic */
 	int spectrum_mode;         /* ugsdr_spectrum_mode, must match the codes */
+	/* Rate of `samples` when it differs from sampling_rate (0 = the same).  The
+	 * front end then runs on the device before the search, as AcquireL5 /
+	 * AcquireGoldCodesL1 do on the host (fse.hpp:289-291, 312-314):
+	 * frontend_frequency is applied at this rate, and the result is resampled
+	 * to sampling_rate by SequentialResampler (resampler.hpp:39-46; ZOH to the
+	 * lcm, boxcar mean, same float rounding).  Both rates must be integers in
+	 * Hz with lcm/sampling_rate <= 65536; n_samples counts input samples, and
+	 * the resampled length must cover block_samples * n_blocks. */
+	double input_sampling_rate;
 } ugsdr_acq_job;
 
 /* Per-code result: the AcquisitionResult<T> fields (src/acquisition/acquisition_result.hpp:11-19). */
@@ -318,6 +327,14 @@ int ugsdr_track_create(ugsdr_ctx* ctx, const ugsdr_track_config* cfg, const ugsd
  * one shared sampling rate), writing n_epochs x n_channels outputs (host or NULL). */
 int ugsdr_track_run(ugsdr_track_bank* bank, const void* samples, int sample_type, int samples_on_device,
 	size_t samples_per_epoch, int n_epochs, ugsdr_track_output* outputs);
+/* Device-resident variant: `samples` and `outputs` (n_epochs x n_channels, or
+ * NULL) are device pointers; enqueued on the context stream without waiting
+ * (ugsdr_ctx_synchronize or the caller's stream order completes it).  No
+ * reference counterpart: Tracker::Track (tracker.hpp:185-200) works on host
+ * vectors; this is the form a device-resident caller chains behind its own
+ * front end. */
+int ugsdr_track_run_device(ugsdr_track_bank* bank, const void* samples, int sample_type, size_t samples_per_epoch,
+	int n_epochs, ugsdr_track_output* outputs);
 int ugsdr_track_destroy(ugsdr_track_bank* bank);
 
 /* ------------------------------------------------------------ serving */

@@ -209,20 +209,28 @@ void orc_track_f64(const float* iq, size_t spm, int n_epochs, const float* chips
 		// the reference's taps are std::complex<float> (tracker.hpp:128-137)
 		for (auto& t : taps)
 			t = cd(static_cast<float>(t.real()), static_cast<float>(t.imag()));
-		// Pll(prompt) (tracking_parameters.hpp:495-511)
-		const cd P = taps[2];
-		const double err = P.real() != 0.0 ? std::atan(P.imag() / P.real()) / (kPi * 2.0) : 0.0;
-		const double cross = P.real() * prev_prompt.imag() - prev_prompt.real() * P.imag();
-		double dot = std::abs(P.real() * prev_prompt.real() + prev_prompt.imag() * P.imag());
+		// Pll(prompt) (tracking_parameters.hpp:495-511), in the reference's types:
+		// the prompt is std::complex<float>, so imag/real, cross and dot are float
+		// products (not contracted) and std::atan2 takes the float overload; atan
+		// of the float ratio and the loop filter are double.
+		const float pr = static_cast<float>(taps[2].real()), pi = static_cast<float>(taps[2].imag());
+		const float ppr = static_cast<float>(prev_prompt.real()), ppi = static_cast<float>(prev_prompt.imag());
+		const volatile float ratio = pi / pr;
+		const double err = pr != 0.0f ? std::atan(static_cast<double>(ratio)) / (kPi * 2.0) : 0.0;
+		const volatile float c1 = pr * ppi, c2 = ppr * pi, d1 = pr * ppr, d2 = ppi * pi;
+		const float cross = c1 - c2;
+		const float dot = std::abs(d1 + d2);
 		const double ferr = std::atan2(cross, dot) / kPi;
 		carrier_freq += K1_PLL * err - K2_PLL * carrier_phase_error - K3_PLL * ferr;
 		carrier_phase_error = err;
 		// carrier_phase += err * pi / 2 rad = err / 4 cycles; |err| <= 1/4 keeps it below 2^60
 		phase_fx += static_cast<uint64_t>(std::llround(err / 4.0 * kTwo64));
-		prev_prompt = P;
+		prev_prompt = cd(pr, pi);
 
-		// Dll(early, late) (tracking_parameters.hpp:513-528)
-		const double ea = std::abs(taps[1]), la = std::abs(taps[3]);
+		// Dll(early, late) (tracking_parameters.hpp:513-528): std::abs of
+		// complex<float> and the normalised difference in float
+		const float ea = std::abs(std::complex<float>(static_cast<float>(taps[1].real()), static_cast<float>(taps[1].imag())));
+		const float la = std::abs(std::complex<float>(static_cast<float>(taps[3].real()), static_cast<float>(taps[3].imag())));
 		double ce = 0.0;
 		if (ea + la != 0)
 			ce = (ea - la) / (ea + la);

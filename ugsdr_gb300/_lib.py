@@ -10,6 +10,8 @@ from pathlib import Path
 
 LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libugsdr_cuda.so"
 
+ABI_VERSION = 2  # UGSDR_CUDA_ABI_VERSION the structs below mirror
+
 OK = 0
 E_INVALID = -1
 E_CUDA = -2
@@ -45,6 +47,7 @@ class AcqJob(C.Structure):
         ("n_codes", C.c_int),
         ("statistic", C.c_int),
         ("spectrum_mode", C.c_int),
+        ("input_sampling_rate", C.c_double),
     ]
 
 
@@ -144,6 +147,7 @@ SIGNATURES = {
     "ugsdr_track_create": (_i, [_vp, C.POINTER(TrackConfig), C.POINTER(TrackChannel), _i, _vp, C.POINTER(_i), _i, _i,
                                 C.POINTER(_vp)]),
     "ugsdr_track_run": (_i, [_vp, _vp, _i, _i, _sz, _i, C.POINTER(TrackOutput)]),
+    "ugsdr_track_run_device": (_i, [_vp, _vp, _i, _sz, _i, _vp]),
     "ugsdr_track_destroy": (_i, [_vp]),
     "ugsdr_server_create": (_i, [_vp, C.POINTER(ServerConfig), C.POINTER(_vp)]),
     "ugsdr_server_submit": (_i, [_vp, C.POINTER(AcqJob), C.POINTER(_u64)]),
@@ -169,6 +173,8 @@ def load(path: Path | None = None) -> C.CDLL:
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
+    if lib.ugsdr_abi_version() != ABI_VERSION:
+        raise RuntimeError(f"{p} has ABI {lib.ugsdr_abi_version()}, these bindings expect {ABI_VERSION}: rebuild it")
     if path is None:
         _lib = lib
     return lib

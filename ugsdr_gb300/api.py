@@ -95,7 +95,7 @@ class Context:
                  intermediate_frequency: float = 0.0, frontend_frequency: float = 0.0,
                  code_offset_ratio: float = 1.0, fold_samples: int = 0,
                  fold_coherent: bool = True, statistic: int = L.STAT_ABS,
-                 spectrum_mode: int = L.SPECTRUM_ONE_SIDED) -> "Job":
+                 spectrum_mode: int = L.SPECTRUM_ONE_SIDED, input_sampling_rate: float = 0.0) -> "Job":
         codes_arr = (C.c_int * len(codes))(*codes)
         if on_device:
             ptr = int(samples)
@@ -109,7 +109,7 @@ class Context:
         job = L.AcqJob(ptr, sample_type, 1 if on_device else 0, n_samples, fs, intermediate_frequency, frontend_frequency,
                        code_offset_ratio,
                        block_samples, n_blocks, fold_samples, 1 if fold_coherent else 0, doppler_range, doppler_step,
-                       codes_arr, len(codes), statistic, spectrum_mode)
+                       codes_arr, len(codes), statistic, spectrum_mode, input_sampling_rate)
         return Job(job, codes_arr, samples)
 
     def acquire(self, job: "Job", cells: bool = False):
@@ -303,15 +303,29 @@ class TrackBank:
         self.n = len(channels)
         self.spm = int(channels[0]["fs"] // 1000)
 
-    def run(self, samples, sample_type: int, n_epochs: int, on_device: bool = False, outputs: bool = True):
+    def run(self, samples, sample_type: int, n_epochs: int, on_device: bool = False, outputs: bool = True,
+            out: np.ndarray | None = None):
+        """Advances n_epochs; returns (n_epochs, n_channels) TRACK_DTYPE rows
+        (into `out` when given, e.g. a view of pinned memory)."""
         ptr = int(samples) if on_device else _ptr(np.ascontiguousarray(samples))
         keep = samples
-        out = np.zeros((n_epochs, self.n), TRACK_DTYPE) if outputs else None
+        if outputs and out is None:
+            out = np.zeros((n_epochs, self.n), TRACK_DTYPE)
+        if not outputs:
+            out = None
+        elif out.dtype != TRACK_DTYPE or out.size != n_epochs * self.n or not out.flags.c_contiguous:
+            raise ValueError("out must be a contiguous TRACK_DTYPE array of n_epochs x n_channels")
         self.ctx._check(self.ctx.lib.ugsdr_track_run(self.h, C.c_void_p(ptr), sample_type, 1 if on_device else 0, self.spm,
                                                      n_epochs, C.cast(out.ctypes.data, C.POINTER(L.TrackOutput))
                                                      if outputs else None))
         del keep
         return out
+
+    def run_device(self, samples_ptr: int, sample_type: int, n_epochs: int, outputs_ptr: int | None = None) -> None:
+        """ugsdr_track_run_device: device samples and (optional) device outputs,
+        enqueued on the context stream without waiting."""
+        self.ctx._check(self.ctx.lib.ugsdr_track_run_device(self.h, C.c_void_p(int(samples_ptr)), sample_type, self.spm,
+                                                            n_epochs, C.c_void_p(int(outputs_ptr or 0))))
 
     def close(self):
         if self.h:

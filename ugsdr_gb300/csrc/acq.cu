@@ -4,12 +4,14 @@
 #include "internal.hpp"
 #include "acq_kernels.cuh"
 #include "acq_batched.cuh"
+#include "dfe.cuh"
 #include "fft_plan.hpp"
 
 #include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <functional>
+#include <numeric>
 #include <vector>
 
 namespace ugsdr_gpu {
@@ -334,6 +336,8 @@ namespace ugsdr_gpu {
 		std::vector<uint32_t> adders;
 		int n = 0, k = 0, m = 0, n_codes = 0, fold_mode = 0;
 		bool large = false;
+		bool front = false;   // device front end (mix at the input rate + resample) first
+		ResamplePlan rs{};
 	};
 
 	namespace {
@@ -353,8 +357,27 @@ namespace ugsdr_gpu {
 			require(job.sample_type >= 0 && job.sample_type <= 3, "unknown sample type");
 			require(job.block_samples >= 2 && job.block_samples <= (1u << 24), "block size out of range");
 			require(job.n_blocks >= 1, "n_blocks must be >= 1");
-			require(job.n_samples >= job.block_samples * job.n_blocks, "not enough samples for n_blocks blocks");
 			require(job.sampling_rate > 0, "sampling rate must be positive");
+			L.front = job.input_sampling_rate != 0.0 && job.input_sampling_rate != job.sampling_rate;
+			if (L.front) {
+				const double fi = job.input_sampling_rate, fo = job.sampling_rate;
+				require(fi > 0 && fi == std::floor(fi) && fo == std::floor(fo) && fi < 1e15 && fo < 1e15,
+					"resampling needs positive integer rates in Hz");
+				const uint64_t in = static_cast<uint64_t>(fi), out = static_cast<uint64_t>(fo);
+				const uint64_t g = std::gcd(in, out);
+				const unsigned __int128 lcm = static_cast<unsigned __int128>(in / g) * out;
+				const uint64_t l = static_cast<uint64_t>(lcm / in), m = static_cast<uint64_t>(lcm / out);
+				require(m <= 65536 && l <= (1u << 20), "resampling ratio too large (lcm / rate above 65536)");
+				require(job.n_samples >= 1 && job.n_samples < (static_cast<size_t>(1) << 40), "input length out of range");
+				L.rs.l = l;
+				L.rs.m = m;
+				L.rs.up = l * job.n_samples;
+				L.rs.n_out = m == 1 ? L.rs.up : (L.rs.up + m - 1) / m;
+				require(L.rs.n_out >= job.block_samples * job.n_blocks, "not enough resampled samples for n_blocks blocks");
+			}
+			else {
+				require(job.n_samples >= job.block_samples * job.n_blocks, "not enough samples for n_blocks blocks");
+			}
 			require(job.codes != nullptr && job.n_codes >= 1, "no codes");
 			require(job.statistic == UGSDR_STAT_ABS || job.statistic == UGSDR_STAT_ABS2, "unknown statistic");
 			L.n = static_cast<int>(job.block_samples);
@@ -479,6 +502,28 @@ namespace ugsdr_gpu {
 		}
 	}
 
+	// Mixes at the input rate and resamples the first n*K outputs into `out`.
+	void launch_front_end(ugsdr_ctx* ctx, const ugsdr_acq_job& job, const JobLaunch& L, const void* samples, float2* out) {
+		FrontEndParams f{};
+		f.samples = samples;
+		f.n_in = job.n_samples;
+		f.rs = L.rs;
+		f.fe_on = job.frontend_frequency != 0.0;
+		f.fe_adder = f.fe_on ? nco_adder(job.input_sampling_rate, job.frontend_frequency) : 0u;
+		f.lut = get_lut(ctx);
+		f.out = out;
+		f.n = static_cast<uint64_t>(L.n) * L.k;
+		const int blocks = static_cast<int>(std::min<uint64_t>((f.n + 255) / 256, static_cast<uint64_t>(ctx->sm_count) * 8));
+		KernelTimer timer(ctx, "front_end");
+		switch (job.sample_type) {
+		case UGSDR_SAMPLES_CF32: front_end_kernel<UGSDR_SAMPLES_CF32><<<blocks, 256, 0, ctx->stream>>>(f); break;
+		case UGSDR_SAMPLES_CI8: front_end_kernel<UGSDR_SAMPLES_CI8><<<blocks, 256, 0, ctx->stream>>>(f); break;
+		case UGSDR_SAMPLES_CI16: front_end_kernel<UGSDR_SAMPLES_CI16><<<blocks, 256, 0, ctx->stream>>>(f); break;
+		default: front_end_kernel<UGSDR_SAMPLES_RI8><<<blocks, 256, 0, ctx->stream>>>(f); break;
+		}
+		note_launch(ctx);
+	}
+
 	size_t spectra_bytes(const JobLaunch& L) {
 		return sizeof(float2) * static_cast<size_t>(L.n) * L.k * chunk_bins(L);
 	}
@@ -486,8 +531,12 @@ namespace ugsdr_gpu {
 	namespace {
 		struct BatchSizes {
 			std::vector<JobLaunch> launches;
-			size_t samples = 0, spectra = 0, cells = 0, params = 0, slab = 0;
+			size_t samples = 0, spectra = 0, cells = 0, params = 0, slab = 0, front = 0;
 		};
+
+		size_t front_bytes(const JobLaunch& L) {
+			return L.front ? (sizeof(float2) * static_cast<size_t>(L.n) * L.k + 255) / 256 * 256 : 0;
+		}
 
 		BatchSizes size_batch(ugsdr_ctx* ctx, const ugsdr_acq_job* jobs, int n_jobs) {
 			require(jobs != nullptr && n_jobs >= 1, "no jobs");
@@ -504,6 +553,7 @@ namespace ugsdr_gpu {
 				}
 				s.spectra = std::max(s.spectra, spectra_bytes(L));
 				s.cells += static_cast<size_t>(L.n_codes) * L.grid.size();
+				s.front += front_bytes(L);
 				s.params += (L.grid.size() * sizeof(uint32_t) + L.n_codes * sizeof(void*) + L.n_codes * sizeof(int) + 512) / 256 * 256;
 				if (L.large)
 					s.slab = std::max(s.slab, batched_scratch_bytes(ctx, shape_of(L)));
@@ -522,7 +572,7 @@ namespace ugsdr_gpu {
 
 	size_t jobs_device_bytes(ugsdr_ctx* ctx, const ugsdr_acq_job* jobs, int n_jobs) {
 		const BatchSizes s = size_batch(ctx, jobs, n_jobs);
-		return s.samples + s.spectra + sizeof(AcqCellDev) * s.cells + s.params + s.slab;
+		return s.samples + s.spectra + sizeof(AcqCellDev) * s.cells + s.params + s.slab + s.front;
 	}
 
 	EnqueuedBatch enqueue_jobs(ugsdr_ctx* ctx, Workspace& ws, cudaStream_t stream, const ugsdr_acq_job* jobs, int n_jobs,
@@ -536,6 +586,8 @@ namespace ugsdr_gpu {
 		ws.params.reserve(params_b);
 		if (sizes.slab)
 			ws.slab.reserve(sizes.slab);
+		if (sizes.front)
+			ws.front.reserve(sizes.front);
 		StreamSwap swap(ctx, stream);
 
 		// stage parameters and host samples
@@ -581,8 +633,20 @@ namespace ugsdr_gpu {
 		}
 		UG_CUDA(cudaMemcpyAsync(ws.params.ptr, host_params.data(), params_b, cudaMemcpyHostToDevice, ctx->stream));
 
+		size_t f_off = 0;
 		for (int j = 0; j < n_jobs; ++j) {
 			const auto& L = launches[j];
+			ugsdr_acq_job job = jobs[j];
+			const void* samples = dev_samples[j];
+			if (L.front) {
+				// the search then reads complex float at sampling_rate, front end done
+				float2* out = reinterpret_cast<float2*>(ws.front.as<char>() + f_off);
+				f_off += front_bytes(L);
+				launch_front_end(ctx, job, L, samples, out);
+				samples = out;
+				job.sample_type = UGSDR_SAMPLES_CF32;
+				job.frontend_frequency = 0.0;
+			}
 			char* dp = ws.params.as<char>() + p_offsets[j];
 			auto* adders = reinterpret_cast<uint32_t*>(dp);
 			size_t o = (L.adders.size() * sizeof(uint32_t) + 15) / 16 * 16;
@@ -590,7 +654,7 @@ namespace ugsdr_gpu {
 			o += L.n_codes * sizeof(void*);
 			o = (o + 15) / 16 * 16;
 			auto* best = reinterpret_cast<int*>(dp + o);
-			launch_job(ctx, jobs[j], L, dev_samples[j], ws.cells.as<AcqCellDev>() + c_offsets[j], best, adders,
+			launch_job(ctx, job, L, samples, ws.cells.as<AcqCellDev>() + c_offsets[j], best, adders,
 				code_ptrs, ws.spectra.as<float2>(), ws.slab.as<char>());
 		}
 		UG_CUDA(cudaMemcpyAsync(host_cells, ws.cells.ptr, sizeof(AcqCellDev) * c_off, cudaMemcpyDeviceToHost, ctx->stream));

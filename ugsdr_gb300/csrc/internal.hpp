@@ -108,11 +108,15 @@ namespace ugsdr_gpu {
 		DevBuf slab;       // large-path scratch (B, partials, counters, fold buffers)
 		DevBuf cells;      // per (code, doppler) records
 		DevBuf params;     // per-job parameter arrays
-		size_t reserved() const { return samples.bytes + spectra.bytes + slab.bytes + cells.bytes + params.bytes; }
+		DevBuf front;      // front-end output (resampled complex float) of jobs that need one
+		size_t reserved() const {
+			return samples.bytes + spectra.bytes + slab.bytes + cells.bytes + params.bytes + front.bytes;
+		}
 		void set_stream(cudaStream_t s) {
-			samples.stream = spectra.stream = slab.stream = cells.stream = params.stream = s;
+			samples.stream = spectra.stream = slab.stream = cells.stream = params.stream = front.stream = s;
 		}
 		void release() {
+			front.release();
 			samples.release();
 			spectra.release();
 			slab.release();

@@ -5,6 +5,7 @@
 #include "internal.hpp"
 #include "acq_kernels.cuh"
 #include "four_step.cuh"
+#include "dfe.cuh"
 #include "fft_plan.hpp"
 
 #include <algorithm>
@@ -203,11 +204,18 @@ namespace ugsdr_gpu {
 				out[i] = in[(static_cast<unsigned __int128>(i) * len / samples) % len];
 		}
 
-		// ZOH to the lcm then boxcar mean over `ratio` (decimator.hpp:144-160); output k
-		// averages upsampled indices [k ratio, (k+1) ratio) clipped to `up` (zero pad).
-		// Input j covers upsampled [ceil(j up/n), ceil((j+1) up/n)); weights are overlaps.
+		// ZOH to the lcm then boxcar mean over `ratio` (decimator.hpp:144-160), with
+		// the reference's sequential float sum (resample_point) for ratios up to
+		// 65536.  Beyond that each input is weighted by its overlap instead
+		// (input j covers upsampled [ceil(j up/n), ceil((j+1) up/n))), which
+		// agrees to float rounding.
 		__global__ void resample_kernel(const float2* in, size_t n, uint64_t up, uint64_t ratio, float2* out, size_t n_out) {
+			const ResamplePlan rs{up / n, ratio, up, n_out};
 			for (size_t k = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; k < n_out; k += static_cast<size_t>(gridDim.x) * blockDim.x) {
+				if (ratio <= 65536) {
+					out[k] = resample_point(k, rs, [&](uint64_t j) { return in[j]; });
+					continue;
+				}
 				const uint64_t i0 = k * ratio;
 				const uint64_t i1 = min(i0 + ratio, up);
 				float2 acc = c2(0.f, 0.f);

@@ -23,6 +23,9 @@
 namespace ugsdr_gpu {
 	namespace {
 		constexpr int kTrackThreads = 256;
+		constexpr int kWinChunk = 8192;   // samples per replica window (a multiple of kTrackThreads)
+		constexpr int kWinPad = 128;      // window margin: taps within +-kWinPad samples of the prompt
+		constexpr int kMaxChunks = 16;    // samples per epoch up to kMaxChunks * kWinChunk
 		constexpr double kTwo64 = 18446744073709551616.0;
 		constexpr double kPi = 3.14159265358979323846;
 
@@ -66,91 +69,155 @@ namespace ugsdr_gpu {
 			return static_cast<unsigned long long>(v);
 		}
 
-		// AddWithPhase (tracking_parameters.hpp:89-98)
-		__device__ void add_with_phase(double lr, double li, double rr, double ri, double rel, double& o_re, double& o_im) {
-			if (rel < 0.5) {
-				double t = lr; lr = rr; rr = t;
-				t = li; li = ri; ri = t;
+		// Loop state of one channel, held in registers of warp 0's lane 0 for the
+		// whole launch (loaded from / stored back to TrackState).
+		struct LoopState {
+			double code_phase, carrier_freq, carrier_phase_error, code_nco, code_error, code_freq;
+			float prev_re, prev_im;
+			unsigned long long phase_fx;
+			long long epoch;
+		};
+
+		// q - floor(q / m) m for q >= 0 and integer m, by a reciprocal and an
+		// exact correction: equals fmod(q, m).
+		__device__ __forceinline__ double mod_pos(double q, double m, double inv_m) {
+			double r = q - floor(q * inv_m) * m;
+			if (r < 0)
+				r += m;
+			else if (r >= m)
+				r -= m;
+			return r;
+		}
+
+		// Full-code index q of the 3-period replica (tracker.hpp:48-49) maps to
+		// chip (q L3 / S3) mod len; an exact (chip, remainder) pair advances by
+		// adding the pair of the step.
+		struct ChipPos {
+			int chip;
+			unsigned int rem;
+		};
+		__device__ __forceinline__ ChipPos chip_add(ChipPos a, ChipPos b, unsigned int s3, int len) {
+			unsigned int r = a.rem + b.rem;
+			int c = a.chip + b.chip;
+			if (r >= s3) {
+				r -= s3;
+				++c;
 			}
-			const double wl = lr / rel;
-			const double wr = rr / (1.0 - rel);
-			if (fabs(wl + wr) > fabs(wl)) {
-				o_re = lr + rr;
-				o_im = li + ri;
-			}
-			else {
-				o_re = lr - rr;
-				o_im = li - ri;
-			}
+			if (c >= len)
+				c -= len;
+			return {c, r};
+		}
+		__device__ __forceinline__ ChipPos chip_of(unsigned long long q, unsigned long long L3, unsigned long long S3, int len) {
+			const unsigned long long num = q * L3;
+			return {static_cast<int>((num / S3) % static_cast<unsigned long long>(len)), static_cast<unsigned int>(num % S3)};
 		}
 
 		template <int ST>
-		__global__ void __launch_bounds__(kTrackThreads) track_bank_kernel(TrackParams p) {
-			extern __shared__ float s_chips[];
+		__global__ void __launch_bounds__(kTrackThreads, 2) track_bank_kernel(TrackParams p) {
+			// The epoch is correlated in chunks of kWinChunk samples.  For each chunk
+			// the code replica is written once to s_win, from kWinPad samples before
+			// the prompt's first index; every tap reads it at its own offset (the
+			// replica is periodic in the code period, so a tap across the period
+			// boundary reads the same values).
+			__shared__ float s_win[kWinChunk + 2 * kWinPad];
 			__shared__ float s_lut[80];
 			__shared__ float s_red[kTrackThreads / 32][20];
+			__shared__ float s_sum[20];
 			__shared__ unsigned long long s_holder0, s_adder;
 			__shared__ int s_mix;
-			__shared__ unsigned long long s_first_phase[5];
-			__shared__ int s_first_len[5];
+			__shared__ int s_first_len[5], s_off[5];
 			__shared__ double s_rel[5];
+			__shared__ ChipPos s_wpos;                     // chip of the window start
+			__shared__ ChipPos s_cpos[kMaxChunks];         // chip step of chunk k's start
 
 			TrackState* st = p.states + blockIdx.x;
 			const int len = st->len;
 			const float* chips = p.chips + static_cast<size_t>(st->code) * p.len_max;
-			for (int i = threadIdx.x; i < len; i += blockDim.x)
-				s_chips[i] = chips[i];
 			if (threadIdx.x < 80)
 				s_lut[threadIdx.x] = p.lut[threadIdx.x];
 
-			const size_t spm = p.spm;
+			const int spm = static_cast<int>(p.spm);
 			const int period_ms = st->period_ms;
 			const double period = static_cast<double>(spm) * period_ms;
+			const double inv_period = 1.0 / period, inv_spm = 1.0 / static_cast<double>(spm);
+			const long long P = static_cast<long long>(spm) * period_ms;
 			const unsigned long long L3 = 3ull * static_cast<unsigned long long>(len);
 			const unsigned long long S3 = static_cast<unsigned long long>(3 * period_ms * p.fs / 1e3);
-			// per-thread chip stride over blockDim samples: blockDim * L3 = dchip * S3 + drem
-			const unsigned long long dnum = static_cast<unsigned long long>(blockDim.x) * L3;
-			const int dchip = static_cast<int>((dnum / S3) % static_cast<unsigned long long>(len));
-			const unsigned int drem = static_cast<unsigned int>(dnum % S3);
+			const unsigned int s3 = static_cast<unsigned int>(S3);
+			const ChipPos tid_pos = chip_of(threadIdx.x, L3, S3, len);
+			const ChipPos step_pos = chip_of(blockDim.x, L3, S3, len);
+			const int n_chunks = (spm + kWinChunk - 1) / kWinChunk;
+			if (threadIdx.x < n_chunks)
+				s_cpos[threadIdx.x] = chip_of(static_cast<unsigned long long>(threadIdx.x) * kWinChunk, L3, S3, len);
 			const double spc = p.fs / st->base;
+			const double base_freq = st->base, dll_scale = st->base / 1.023e6;
+			const int lane = threadIdx.x & 31;
+			const bool warp0 = threadIdx.x < 32;
+
+			LoopState ls{};
+			if (threadIdx.x == 0)
+				ls = LoopState{st->code_phase, st->carrier_freq, st->carrier_phase_error, st->code_nco, st->code_error,
+					st->code_freq, static_cast<float>(st->prev_re), static_cast<float>(st->prev_im), st->phase_fx, st->epoch};
+
+			// carrier NCO of GetEpl's Translate(signal, fs, -f, -phase), lane 0
+			auto nco_setup = [&]() {
+				double f = -ls.carrier_freq;
+				s_mix = fabs(f) != 0.0;
+				if (f < 0)
+					f = p.fs + f;
+				// NumericallyControlledOscillator's order (nco.hpp:17-20): a sample whose
+				// phase lands exactly on a LUT boundary (rational f / fs) then picks
+				// the same entry as the host restatement
+				double av = kTwo64 * f / p.fs;
+				if (av >= kTwo64)
+					av = 0.0;
+				s_adder = static_cast<unsigned long long>(av);
+				s_holder0 = 0ull - ls.phase_fx;
+			};
+			// CorrelateSplit set-up of the five taps from the code phase, lanes 0-4
+			// of warp 0 (one tap each): split point, weight, replica offset.
+			auto tap_setup = [&]() {
+				const double code_phase = __shfl_sync(0xffffffffu, ls.code_phase, 0);
+				const long long epoch = __shfl_sync(0xffffffffu, ls.epoch, 0);
+				long long fp = 0;
+				if (lane < 5) {
+					const double ph = code_phase - p.fs / 1e3 * static_cast<double>(epoch % period_ms);
+					double q = ph + spc * p.offsets[lane];
+					while (q < 0)
+						q += period;
+					if (q > period)
+						q = mod_pos(q, period, inv_period);
+					s_first_len[lane] = static_cast<int>(static_cast<unsigned int>(ceil(q)) % static_cast<unsigned int>(spm));
+					fp = static_cast<long long>(ceil(2 * period - q));
+					s_rel[lane] = mod_pos(q, static_cast<double>(spm), inv_spm) * inv_spm;
+				}
+				const long long fp2 = __shfl_sync(0xffffffffu, fp, 2);
+				if (lane < 5) {
+					long long d = fp - fp2;  // reduced to the prompt's code period
+					while (d > P / 2)
+						d -= P;
+					while (d <= -P / 2)
+						d += P;
+					s_off[lane] = static_cast<int>(d) + kWinPad;
+					if (lane == 2)
+						s_wpos = chip_of(static_cast<unsigned long long>(fp2 - kWinPad), L3, S3, len);
+				}
+			};
+			if (warp0) {
+				if (lane == 0)
+					nco_setup();
+				tap_setup();
+			}
 			__syncthreads();
 
 			for (int ep = 0; ep < p.n_epochs; ++ep) {
-				if (threadIdx.x == 0) {
-					// GetEpl: Translate(signal, fs, -carrier_frequency, -carrier_phase)
-					double f = -st->carrier_freq;
-					s_mix = fabs(f) != 0.0;
-					if (f < 0)
-						f = p.fs + f;
-					double av = kTwo64 * f / p.fs;
-					if (av >= kTwo64)
-						av = 0.0;
-					s_adder = static_cast<unsigned long long>(av);
-					s_holder0 = 0ull - st->phase_fx;
-					const double ph = st->code_phase - p.fs / 1e3 * static_cast<double>(st->epoch % period_ms);
-					for (int t = 0; t < 5; ++t) {
-						double q = ph + spc * p.offsets[t];
-						while (q < 0)
-							q += period;
-						if (q > period)
-							q = fmod(q, period);
-						s_first_len[t] = static_cast<int>(static_cast<unsigned long long>(ceil(q)) % spm);
-						s_first_phase[t] = static_cast<unsigned long long>(ceil(2 * period - q));
-						s_rel[t] = fmod(q, static_cast<double>(spm)) / static_cast<double>(spm);
-					}
-				}
-				__syncthreads();
-				// chip trackers: sample i uses full-code index q = first_phase + i,
-				// chip = (q * L3 / S3) mod len, advanced exactly by (dchip, drem) per step
-				int chip[5];
-				unsigned int rem[5];
-				int first_len[5];
+				int first_len[5], off[5];
+#pragma unroll
 				for (int t = 0; t < 5; ++t) {
-					const unsigned long long num = (s_first_phase[t] + threadIdx.x) * L3;
-					chip[t] = static_cast<int>((num / S3) % static_cast<unsigned long long>(len));
-					rem[t] = static_cast<unsigned int>(num % S3);
 					first_len[t] = s_first_len[t];
+					off[t] = s_off[t];
 				}
+				const ChipPos wpos = s_wpos;
 				float acc[20];
 #pragma unroll
 				for (int k = 0; k < 20; ++k)
@@ -160,93 +227,170 @@ namespace ugsdr_gpu {
 				const unsigned long long hstep = static_cast<unsigned long long>(blockDim.x) * adder;
 				const bool mix = s_mix;
 				const size_t base = static_cast<size_t>(ep) * spm;
-				for (int i = threadIdx.x; i < static_cast<int>(spm); i += blockDim.x) {
-					float2 x = load_sample<ST>(p.samples, base + i);
-					if (mix) {
-						const uint32_t idx = static_cast<uint32_t>(holder >> 58);
-						const float c = s_lut[idx + 16], s = s_lut[idx];
-						x = c2(__fsub_rn(__fmul_rn(x.x, c), __fmul_rn(x.y, s)), __fadd_rn(__fmul_rn(x.x, s), __fmul_rn(x.y, c)));
+				for (int k = 0; k < n_chunks; ++k) {
+					const int c0 = k * kWinChunk;
+					const int n_c = min(kWinChunk, spm - c0);
+					// replica window of this chunk: entries j < n_c + 2 kWinPad
+					ChipPos pos = chip_add(chip_add(wpos, s_cpos[k], s3, len), tid_pos, s3, len);
+					for (int j = threadIdx.x; j < n_c + 2 * kWinPad; j += blockDim.x) {
+						s_win[j] = __ldg(chips + pos.chip);
+						pos = chip_add(pos, step_pos, s3, len);
 					}
-					holder += hstep;
+					__syncthreads();
+					// correlate: four samples in flight per thread
+					for (int i0 = threadIdx.x; i0 < n_c; i0 += 4 * kTrackThreads) {
+						float2 xs[4];
 #pragma unroll
-					for (int t = 0; t < 5; ++t) {
-						const float cv = s_chips[chip[t]];
-						const int slot = 4 * t + (i < first_len[t] ? 0 : 2);
-						acc[slot] += x.x * cv;
-						acc[slot + 1] += x.y * cv;
-						rem[t] += drem;
-						int adv = dchip;
-						if (rem[t] >= S3) {
-							rem[t] -= static_cast<unsigned int>(S3);
-							++adv;
+						for (int u = 0; u < 4; ++u) {
+							const int i = i0 + u * kTrackThreads;
+							xs[u] = i < n_c ? load_sample<ST>(p.samples, base + c0 + i) : c2(0.f, 0.f);
 						}
-						chip[t] += adv;
-						if (chip[t] >= len)
-							chip[t] -= len;
+#pragma unroll
+						for (int u = 0; u < 4; ++u) {
+							const int i = i0 + u * kTrackThreads;
+							if (i >= n_c)
+								break;
+							float2 x = xs[u];
+							if (mix) {
+								const uint32_t idx = static_cast<uint32_t>(holder >> 58);
+								const float c = s_lut[idx + 16], s = s_lut[idx];
+								x = c2(__fsub_rn(__fmul_rn(x.x, c), __fmul_rn(x.y, s)), __fadd_rn(__fmul_rn(x.x, s), __fmul_rn(x.y, c)));
+							}
+							holder += hstep;
+							const int sidx = c0 + i;
+#pragma unroll
+							for (int t = 0; t < 5; ++t) {
+								const float cv = s_win[i + off[t]];
+								// the two CorrelateSplit partial sums (warp-uniform except at the split)
+								if (sidx < first_len[t]) {
+									acc[4 * t] += x.x * cv;
+									acc[4 * t + 1] += x.y * cv;
+								}
+								else {
+									acc[4 * t + 2] += x.x * cv;
+									acc[4 * t + 3] += x.y * cv;
+								}
+							}
+						}
 					}
+					__syncthreads();
 				}
 				// block reduction of the 20 partial sums
 #pragma unroll
 				for (int k = 0; k < 20; ++k) {
 					float v = acc[k];
+#pragma unroll
 					for (int o = 16; o > 0; o >>= 1)
 						v += __shfl_down_sync(0xffffffffu, v, o);
-					if ((threadIdx.x & 31) == 0)
+					if (lane == 0)
 						s_red[threadIdx.x >> 5][k] = v;
 				}
 				__syncthreads();
-				if (threadIdx.x == 0) {
-					double sums[20];
-					for (int k = 0; k < 20; ++k) {
-						double v = 0;
-						for (int w = 0; w < static_cast<int>(blockDim.x / 32); ++w)
-							v += s_red[w][k];
-						sums[k] = v;
+				if (warp0) {
+					if (lane < 20) {
+						float v = 0.f;
+						for (int w = 0; w < kTrackThreads / 32; ++w)
+							v += s_red[w][lane];
+						s_sum[lane] = v;
 					}
-					double tap_re[5], tap_im[5];
-					for (int t = 0; t < 5; ++t)
-						add_with_phase(sums[4 * t], sums[4 * t + 1], sums[4 * t + 2], sums[4 * t + 3], s_rel[t], tap_re[t], tap_im[t]);
-					// UpdatePhase (tracking_parameters.hpp:163-165) with the pre-update frequency
-					st->phase_fx += frac_to_fx(st->carrier_freq / 1000.0);
-					// Pll(prompt) (tracking_parameters.hpp:495-511)
-					const double pr = static_cast<float>(tap_re[2]), pi = static_cast<float>(tap_im[2]);
-					const double err = pr != 0.0 ? atan(pi / pr) / (kPi * 2.0) : 0.0;
-					const double cross = pr * st->prev_im - st->prev_re * pi;
-					const double dot = fabs(pr * st->prev_re + st->prev_im * pi);
-					const double ferr = atan2(cross, dot) / kPi;
-					st->carrier_freq += p.k1_pll * err - p.k2_pll * st->carrier_phase_error - p.k3_pll * ferr;
-					st->carrier_phase_error = err;
-					st->phase_fx += static_cast<unsigned long long>(llrint(err / 4.0 * kTwo64));
-					st->prev_re = pr;
-					st->prev_im = pi;
-					// Dll(early, late) (tracking_parameters.hpp:513-528)
-					const double er = static_cast<float>(tap_re[1]), ei = static_cast<float>(tap_im[1]);
-					const double lr = static_cast<float>(tap_re[3]), li = static_cast<float>(tap_im[3]);
-					const double ea = hypot(er, ei), la = hypot(lr, li);
-					double ce = 0.0;
-					if (ea + la != 0)
-						ce = (ea - la) / (ea + la);
-					st->code_nco += (p.k1_dll * (ce - st->code_error) + p.k2_dll * ce) * (st->base / 1.023e6);
-					st->code_error = ce;
-					st->code_freq = st->base - st->code_nco;
-					st->code_phase -= p.fs / 1000 / 2 * (st->code_freq / st->base - 1);
-					if (p.out) {
-						TrackOut o;
-						for (int t = 0; t < 5; ++t) {
-							o.taps[t][0] = static_cast<float>(tap_re[t]);
-							o.taps[t][1] = static_cast<float>(tap_im[t]);
+					__syncwarp();
+					// AddWithPhase per tap (lanes 0-4): the reference's comparison
+					// |l / rel + r / (1 - rel)| > |l / rel| multiplied through by
+					// rel (1 - rel) > 0; taps rounded to float as the reference's
+					float tap_re = 0.f, tap_im = 0.f;
+					if (lane < 5) {
+						float lr = s_sum[4 * lane], li = s_sum[4 * lane + 1], rr = s_sum[4 * lane + 2], ri = s_sum[4 * lane + 3];
+						const double rel = s_rel[lane];
+						if (rel < 0.5) {
+							float t0 = lr; lr = rr; rr = t0;
+							t0 = li; li = ri; ri = t0;
 						}
-						o.carrier_frequency = st->carrier_freq;
-						o.carrier_phase = static_cast<double>(st->phase_fx) / kTwo64 * 2 * kPi;
-						o.code_phase = st->code_phase;
-						o.code_frequency = st->code_freq;
-						o.phase_error = err;
-						o.code_error = ce;
-						p.out[static_cast<size_t>(ep) * p.n_channels + blockIdx.x] = o;
+						const double a = static_cast<double>(lr) * (1.0 - rel);
+						const bool plus = fabs(a + static_cast<double>(rr) * rel) > fabs(a);
+						tap_re = static_cast<float>(plus ? static_cast<double>(lr) + rr : static_cast<double>(lr) - rr);
+						tap_im = static_cast<float>(plus ? static_cast<double>(li) + ri : static_cast<double>(li) - ri);
 					}
-					++st->epoch;
+					float taps_re[5], taps_im[5];
+#pragma unroll
+					for (int t = 0; t < 5; ++t) {
+						taps_re[t] = __shfl_sync(0xffffffffu, tap_re, t);
+						taps_im[t] = __shfl_sync(0xffffffffu, tap_im, t);
+					}
+					const float pr = taps_re[2], pi = taps_im[2];
+					const float ppr = __shfl_sync(0xffffffffu, ls.prev_re, 0), ppi = __shfl_sync(0xffffffffu, ls.prev_im, 0);
+					// discriminators in the reference's float types, side by side:
+					// lane 0 PLL atan(imag / real), 1 FLL atan2(cross, dot), 2 |E|, 3 |L|
+					float part = 0.f;
+					if (lane == 0) {
+						part = pr != 0.f ? atanf(__fdiv_rn(pi, pr)) : 0.f;
+					}
+					else if (lane == 1) {
+						const float cross = __fsub_rn(__fmul_rn(pr, ppi), __fmul_rn(ppr, pi));
+						const float dot = fabsf(__fadd_rn(__fmul_rn(pr, ppr), __fmul_rn(ppi, pi)));
+						part = atan2f(cross, dot);
+					}
+					else if (lane == 2) {
+						part = hypotf(taps_re[1], taps_im[1]);
+					}
+					else if (lane == 3) {
+						part = hypotf(taps_re[3], taps_im[3]);
+					}
+					const float ferr_f = __shfl_sync(0xffffffffu, part, 1);
+					const float ea = __shfl_sync(0xffffffffu, part, 2);
+					const float la = __shfl_sync(0xffffffffu, part, 3);
+					if (lane == 0) {
+						const double err = static_cast<double>(part) / (kPi * 2.0);
+						const double ferr = static_cast<double>(ferr_f) / kPi;
+						// UpdatePhase (tracking_parameters.hpp:163-165) with the pre-update frequency
+						ls.phase_fx += frac_to_fx(ls.carrier_freq / 1000.0);
+						// Pll(prompt) (tracking_parameters.hpp:495-511), loop filter in FP64
+						ls.carrier_freq += p.k1_pll * err - p.k2_pll * ls.carrier_phase_error - p.k3_pll * ferr;
+						ls.carrier_phase_error = err;
+						ls.phase_fx += static_cast<unsigned long long>(llrint(err * (kTwo64 / 4.0)));
+						ls.prev_re = pr;
+						ls.prev_im = pi;
+						// Dll(early, late) (tracking_parameters.hpp:513-528)
+						double ce = 0.0;
+						if (ea + la != 0.f)
+							ce = __fdiv_rn(__fsub_rn(ea, la), __fadd_rn(ea, la));
+						ls.code_nco += (p.k1_dll * (ce - ls.code_error) + p.k2_dll * ce) * dll_scale;
+						ls.code_error = ce;
+						ls.code_freq = base_freq - ls.code_nco;
+						ls.code_phase -= p.fs / 1000 / 2 * (ls.code_freq / base_freq - 1);
+						if (p.out) {
+							TrackOut o;
+							for (int t = 0; t < 5; ++t) {
+								o.taps[t][0] = taps_re[t];
+								o.taps[t][1] = taps_im[t];
+							}
+							o.carrier_frequency = ls.carrier_freq;
+							o.carrier_phase = static_cast<double>(ls.phase_fx) / kTwo64 * 2 * kPi;
+							o.code_phase = ls.code_phase;
+							o.code_frequency = ls.code_freq;
+							o.phase_error = err;
+							o.code_error = ce;
+							p.out[static_cast<size_t>(ep) * p.n_channels + blockIdx.x] = o;
+						}
+						++ls.epoch;
+						nco_setup();
+					}
+					__syncwarp();
+					if (ep + 1 < p.n_epochs)
+						tap_setup();
 				}
 				__syncthreads();
+			}
+			if (threadIdx.x == 0) {
+				st->code_phase = ls.code_phase;
+				st->carrier_freq = ls.carrier_freq;
+				st->carrier_phase_error = ls.carrier_phase_error;
+				st->code_nco = ls.code_nco;
+				st->code_error = ls.code_error;
+				st->code_freq = ls.code_freq;
+				st->prev_re = ls.prev_re;
+				st->prev_im = ls.prev_im;
+				st->phase_fx = ls.phase_fx;
+				st->epoch = ls.epoch;
 			}
 		}
 	}
@@ -265,6 +409,60 @@ struct ugsdr_track_bank {
 	DevBuf chips, states, samples, out;
 };
 
+namespace {
+	// Enqueues n_epochs of the bank on the context stream; `dev_out` (device,
+	// or null) receives n_epochs x n_channels outputs.
+	void track_enqueue(ugsdr_track_bank* bank, const void* samples, int sample_type, int samples_on_device,
+		size_t samples_per_epoch, int n_epochs, TrackOut* dev_out) {
+		ugsdr_ctx* ctx = bank->ctx;
+		require(samples && n_epochs > 0, "null samples or no epochs");
+		require(samples_per_epoch == bank->spm, "samples_per_epoch must be sampling_rate / 1000");
+		require(sample_type >= 0 && sample_type <= 3, "unknown sample type");
+		const size_t per = sample_type == UGSDR_SAMPLES_CF32 ? 8 : sample_type == UGSDR_SAMPLES_CI8 ? 2 : sample_type == UGSDR_SAMPLES_CI16 ? 4 : 1;
+		const size_t n = bank->spm * static_cast<size_t>(n_epochs);
+		const void* dev = samples;
+		if (!samples_on_device) {
+			bank->samples.reserve(per * n);
+			UG_CUDA(cudaMemcpyAsync(bank->samples.ptr, samples, per * n, cudaMemcpyHostToDevice, ctx->stream));
+			dev = bank->samples.ptr;
+		}
+		TrackParams p{};
+		p.samples = dev;
+		p.spm = bank->spm;
+		p.n_epochs = n_epochs;
+		p.n_channels = bank->n_channels;
+		p.fs = bank->fs;
+		std::memcpy(p.offsets, bank->offsets, sizeof(p.offsets));
+		p.k1_pll = bank->k1_pll;
+		p.k2_pll = bank->k2_pll;
+		p.k3_pll = bank->k3_pll;
+		p.k1_dll = bank->k1_dll;
+		p.k2_dll = bank->k2_dll;
+		p.chips = bank->chips.as<float>();
+		p.len_max = bank->len_max;
+		p.lut = get_lut(ctx);
+		p.states = bank->states.as<TrackState>();
+		p.out = dev_out;
+		const size_t smem = 0;
+		KernelTimer timer(ctx, "track_bank");
+		switch (sample_type) {
+		case UGSDR_SAMPLES_CF32:
+			track_bank_kernel<UGSDR_SAMPLES_CF32><<<bank->n_channels, kTrackThreads, smem, ctx->stream>>>(p);
+			break;
+		case UGSDR_SAMPLES_CI8:
+			track_bank_kernel<UGSDR_SAMPLES_CI8><<<bank->n_channels, kTrackThreads, smem, ctx->stream>>>(p);
+			break;
+		case UGSDR_SAMPLES_CI16:
+			track_bank_kernel<UGSDR_SAMPLES_CI16><<<bank->n_channels, kTrackThreads, smem, ctx->stream>>>(p);
+			break;
+		default:
+			track_bank_kernel<UGSDR_SAMPLES_RI8><<<bank->n_channels, kTrackThreads, smem, ctx->stream>>>(p);
+			break;
+		}
+		note_launch(ctx);
+	}
+}
+
 extern "C" {
 
 int ugsdr_track_create(ugsdr_ctx* ctx, const ugsdr_track_config* cfg, const ugsdr_track_channel* channels, int n_channels,
@@ -276,7 +474,7 @@ int ugsdr_track_create(ugsdr_ctx* ctx, const ugsdr_track_config* cfg, const ugsd
 	return guarded(ctx, [&] {
 		require(cfg && channels && codes && code_lens && n_channels > 0 && n_codes > 0 && code_len_max > 0, "null or empty bank description");
 		require(std::fabs(cfg->integration_time - 1e-3) < 1e-12, "integration_time must be 0.001 s (one epoch)");
-		require(code_len_max * sizeof(float) <= 48 * 1024, "codes longer than 12288 chips are not supported");
+		require(code_len_max <= (1 << 20), "codes longer than 2^20 chips are not supported");
 		auto b = std::make_unique<ugsdr_track_bank>();
 		b->ctx = ctx;
 		b->n_channels = n_channels;
@@ -284,6 +482,8 @@ int ugsdr_track_create(ugsdr_ctx* ctx, const ugsdr_track_config* cfg, const ugsd
 		b->fs = channels[0].sampling_rate;
 		require(b->fs > 0 && std::fmod(b->fs, 1e3) == 0.0, "sampling rate must be a whole number of kHz");
 		b->spm = static_cast<size_t>(b->fs / 1e3);
+		require(b->spm >= 2 * kWinPad && b->spm <= static_cast<size_t>(kMaxChunks) * kWinChunk,
+			"sampling rate must be between 256 kHz and 131.072 MHz");
 		const double el = cfg->early_late_spacing, vel = cfg->very_early_late_spacing;
 		const double offs[5] = {vel, el, 0.0, -el, -vel};
 		std::memcpy(b->offsets, offs, sizeof(offs));
@@ -311,6 +511,9 @@ int ugsdr_track_create(ugsdr_ctx* ctx, const ugsdr_track_config* cfg, const ugsd
 			const double period = ch.code_length / ch.code_frequency * 1000.0;
 			const int period_ms = static_cast<int>(std::lround(period));
 			require(period_ms >= 1 && std::fabs(period - period_ms) < 1e-9, "code period must be a whole number of ms");
+			// every tap within kWinPad - 2 samples of the prompt (replica window margin)
+			require((std::fmax(std::fabs(el), std::fabs(vel)) * b->fs / ch.code_frequency) + 2 <= kWinPad,
+				"tap spacing too wide for the sampling rate (more than 126 samples from the prompt)");
 			TrackState s{};
 			s.code = ch.code;
 			s.len = len;
@@ -339,60 +542,28 @@ int ugsdr_track_run(ugsdr_track_bank* bank, const void* samples, int sample_type
 	ugsdr_ctx* ctx = bank->ctx;
 	std::lock_guard<std::mutex> lock(ctx->mutex);
 	return guarded(ctx, [&] {
-		require(samples && n_epochs > 0, "null samples or no epochs");
-		require(samples_per_epoch == bank->spm, "samples_per_epoch must be sampling_rate / 1000");
-		require(sample_type >= 0 && sample_type <= 3, "unknown sample type");
-		const size_t per = sample_type == UGSDR_SAMPLES_CF32 ? 8 : sample_type == UGSDR_SAMPLES_CI8 ? 2 : sample_type == UGSDR_SAMPLES_CI16 ? 4 : 1;
-		const size_t n = bank->spm * static_cast<size_t>(n_epochs);
-		const void* dev = samples;
-		if (!samples_on_device) {
-			bank->samples.reserve(per * n);
-			UG_CUDA(cudaMemcpyAsync(bank->samples.ptr, samples, per * n, cudaMemcpyHostToDevice, ctx->stream));
-			dev = bank->samples.ptr;
-		}
-		TrackParams p{};
-		p.samples = dev;
-		p.spm = bank->spm;
-		p.n_epochs = n_epochs;
-		p.n_channels = bank->n_channels;
-		p.fs = bank->fs;
-		std::memcpy(p.offsets, bank->offsets, sizeof(p.offsets));
-		p.k1_pll = bank->k1_pll;
-		p.k2_pll = bank->k2_pll;
-		p.k3_pll = bank->k3_pll;
-		p.k1_dll = bank->k1_dll;
-		p.k2_dll = bank->k2_dll;
-		p.chips = bank->chips.as<float>();
-		p.len_max = bank->len_max;
-		p.lut = get_lut(ctx);
-		p.states = bank->states.as<TrackState>();
+		TrackOut* dev_out = nullptr;
 		if (outputs) {
+			require(n_epochs > 0, "null samples or no epochs");
 			bank->out.reserve(sizeof(TrackOut) * static_cast<size_t>(n_epochs) * bank->n_channels);
-			p.out = bank->out.as<TrackOut>();
+			dev_out = bank->out.as<TrackOut>();
 		}
-		const size_t smem = sizeof(float) * bank->len_max;
-		{
-			KernelTimer timer(ctx, "track_bank");
-			switch (sample_type) {
-			case UGSDR_SAMPLES_CF32:
-				track_bank_kernel<UGSDR_SAMPLES_CF32><<<bank->n_channels, kTrackThreads, smem, ctx->stream>>>(p);
-				break;
-			case UGSDR_SAMPLES_CI8:
-				track_bank_kernel<UGSDR_SAMPLES_CI8><<<bank->n_channels, kTrackThreads, smem, ctx->stream>>>(p);
-				break;
-			case UGSDR_SAMPLES_CI16:
-				track_bank_kernel<UGSDR_SAMPLES_CI16><<<bank->n_channels, kTrackThreads, smem, ctx->stream>>>(p);
-				break;
-			default:
-				track_bank_kernel<UGSDR_SAMPLES_RI8><<<bank->n_channels, kTrackThreads, smem, ctx->stream>>>(p);
-				break;
-			}
-		}
-		note_launch(ctx);
+		track_enqueue(bank, samples, sample_type, samples_on_device, samples_per_epoch, n_epochs, dev_out);
 		if (outputs)
-			UG_CUDA(cudaMemcpyAsync(outputs, p.out, sizeof(TrackOut) * static_cast<size_t>(n_epochs) * bank->n_channels,
+			UG_CUDA(cudaMemcpyAsync(outputs, dev_out, sizeof(TrackOut) * static_cast<size_t>(n_epochs) * bank->n_channels,
 				cudaMemcpyDeviceToHost, ctx->stream));
 		UG_CUDA(cudaStreamSynchronize(ctx->stream));
+	});
+}
+
+int ugsdr_track_run_device(ugsdr_track_bank* bank, const void* samples, int sample_type, size_t samples_per_epoch,
+	int n_epochs, ugsdr_track_output* outputs) {
+	if (!bank)
+		return UGSDR_E_INVALID;
+	ugsdr_ctx* ctx = bank->ctx;
+	std::lock_guard<std::mutex> lock(ctx->mutex);
+	return guarded(ctx, [&] {
+		track_enqueue(bank, samples, sample_type, 1, samples_per_epoch, n_epochs, reinterpret_cast<TrackOut*>(outputs));
 	});
 }
 

@@ -27,6 +27,7 @@ class Emitter:
     data_rate: float = 50.0  # bits/s (0 = pilot)
     phase: float = 0.0
     tag: object = None
+    secondary: np.ndarray | None = None  # +-1 per primary code period (e.g. NH10), repeating
 
 
 def synthesize(emitters: list[Emitter], fs: float, n: int, noise_sigma: float, sample_type: str, seed: int,
@@ -41,6 +42,9 @@ def synthesize(emitters: list[Emitter], fs: float, n: int, noise_sigma: float, s
         amp = noise_sigma * np.sqrt(2.0 * 10 ** (e.cn0_dbhz / 10.0) / fs)
         pos = (t * e.chip_rate - e.code_phase) % len(e.chips)
         code = e.chips[np.floor(pos).astype(np.int64) % len(e.chips)]
+        if e.secondary is not None:
+            period = np.floor((t * e.chip_rate - e.code_phase) / len(e.chips)).astype(np.int64)
+            code = code * np.asarray(e.secondary, np.float64)[period % len(e.secondary)]
         if e.data_rate > 0:
             bit_off = rng.uniform(0, 1.0 / e.data_rate)
             nbits = int(np.ceil((t[-1] + bit_off) * e.data_rate)) + 2
@@ -86,3 +90,34 @@ def gps_l1_config(seed: int, codes: dict[int, np.ndarray], fs: float = 4.0e6, ms
                           cn0=e.cn0_dbhz))
     n = int(round(fs * ms / 1000))
     return synthesize(ems, fs, n, sigma, sample_type, seed + 1000), truth
+
+
+# Neuman-Hofman 10-bit secondary code of the GPS L5 I5 channel (IS-GPS-705,
+# first bit first): one bit per 1 ms primary period.
+NH10 = np.array([0, 0, 0, 0, 1, 1, 0, 1, 0, 1], np.int8)
+
+
+def nh10_mask() -> int:
+    """Sign mask of NH10 for ugsdr_code_put: bit s set = period s negated."""
+    return int(sum(1 << s for s, b in enumerate(NH10) if b))
+
+
+def l5_weak_config(seed: int, codes: dict[int, np.ndarray], fs: float = 40e6, if_hz: float = 10e6, ms: int = 200,
+                   visible: int = 8, cn0=(30.0, 38.0), max_doppler: float = 4500.0, sigma: float = 20.0):
+    """GPS L5I with NH10 at a real IF: real int8 samples at fs, carrier at if_hz
+    plus Doppler, code phase uniform over the 10 ms NH period.  Pilot-like
+    (no data symbols), so a 10 ms coherent block sees only the NH10 flips."""
+    rng = np.random.default_rng(seed)
+    prns = sorted(codes)
+    chosen = rng.choice(prns, size=visible, replace=False)
+    ems, truth = [], []
+    sec = 1.0 - 2.0 * NH10
+    for p in chosen:
+        delay = rng.uniform(0, 10 * 10230)  # chips within the NH period
+        dop = rng.uniform(-max_doppler, max_doppler)
+        e = Emitter(codes[int(p)], 10.23e6, delay, if_hz + dop, rng.uniform(*cn0), 0.0, rng.uniform(0, 2 * np.pi),
+                    tag=int(p), secondary=sec)
+        ems.append(e)
+        truth.append(dict(prn=int(p), doppler=dop, delay_chips=delay, cn0=e.cn0_dbhz))
+    n = int(round(fs * ms / 1000))
+    return synthesize(ems, fs, n, sigma, "ri8", seed + 1000, real_if=True), truth
