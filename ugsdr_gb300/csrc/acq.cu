@@ -141,6 +141,28 @@ namespace ugsdr_gpu {
 				most = std::max(most, batch * plan.n / plan.radix[s]);
 			return std::min(kBatchedThreads, std::max(64, (most + 31) / 32 * 32));
 		}
+		template <class F>
+		int threads_of(const FftPlanDev& plan, int batch) {
+			if constexpr (F::N > 0)
+				return std::min(kBatchedThreads, std::max(64, (F::most_butterflies(batch) + 31) / 32 * 32));
+			else
+				return threads_for(plan, batch);
+		}
+
+		// Compile-time sub-FFT plans for the N1 x N2 splits of the configured
+		// block sizes (get_large_plan's choice: the largest N1 <= sqrt(N)),
+		// odd radices first; other sizes run the runtime plan.
+		template <class Fn>
+		void with_large_ffts(int n1, int n2, Fn&& fn) {
+			if (n1 == 200 && n2 == 250)
+				fn(StaticFft<200, 25, 8>{}, StaticFft<250, 25, 10>{});          // 50,000: 1 ms at 50 MHz
+			else if (n1 == 400 && n2 == 500)
+				fn(StaticFft<400, 25, 16>{}, StaticFft<500, 25, 20>{});         // 200,000: 4 ms at 50 MHz
+			else if (n1 == 440 && n2 == 465)
+				fn(StaticFft<440, 11, 5, 8>{}, StaticFft<465, 31, 15>{});       // 204,600: 10 ms at 20.46 MHz
+			else
+				fn(RuntimeFft{}, RuntimeFft{});
+		}
 
 		// Sub-transforms per CTA: 8 columns/rows (64-byte runs per k1 row) unless
 		// the tiles would exceed a third of shared memory.
@@ -192,22 +214,27 @@ namespace ugsdr_gpu {
 		}
 
 		template <typename K>
-		void launch_fwd_cols(ugsdr_ctx* ctx, K kernel, const BatchedParams& p, int items) {
+		void launch_fwd_cols(ugsdr_ctx* ctx, K kernel, const BatchedParams& p, int items, int threads) {
 			const size_t smem = smem_cols(p, false);
 			set_smem(kernel, smem);
-			kernel<<<items * chunks_of(p.n2, p.cw), threads_for(p.p1, p.cw), smem, ctx->stream>>>(p);
+			kernel<<<items * chunks_of(p.n2, p.cw), threads, smem, ctx->stream>>>(p);
 		}
 
 		void launch_forward(ugsdr_ctx* ctx, int sample_type, const BatchedParams& p, int items) {
-			switch (sample_type) {
-			case UGSDR_SAMPLES_CF32: launch_fwd_cols(ctx, fwd_cols_kernel<UGSDR_SAMPLES_CF32>, p, items); break;
-			case UGSDR_SAMPLES_CI8: launch_fwd_cols(ctx, fwd_cols_kernel<UGSDR_SAMPLES_CI8>, p, items); break;
-			case UGSDR_SAMPLES_CI16: launch_fwd_cols(ctx, fwd_cols_kernel<UGSDR_SAMPLES_CI16>, p, items); break;
-			default: launch_fwd_cols(ctx, fwd_cols_kernel<UGSDR_SAMPLES_RI8>, p, items); break;
-			}
-			const size_t smem = smem_rows(p, false);
-			set_smem(fwd_rows_kernel, smem);
-			fwd_rows_kernel<<<items * chunks_of(p.n1, p.rw), threads_for(p.p2, p.rw), smem, ctx->stream>>>(p);
+			with_large_ffts(p.n1, p.n2, [&](auto f1, auto f2) {
+				using F1 = decltype(f1);
+				using F2 = decltype(f2);
+				const int t1 = threads_of<F1>(p.p1, p.cw);
+				switch (sample_type) {
+				case UGSDR_SAMPLES_CF32: launch_fwd_cols(ctx, fwd_cols_kernel<UGSDR_SAMPLES_CF32, F1>, p, items, t1); break;
+				case UGSDR_SAMPLES_CI8: launch_fwd_cols(ctx, fwd_cols_kernel<UGSDR_SAMPLES_CI8, F1>, p, items, t1); break;
+				case UGSDR_SAMPLES_CI16: launch_fwd_cols(ctx, fwd_cols_kernel<UGSDR_SAMPLES_CI16, F1>, p, items, t1); break;
+				default: launch_fwd_cols(ctx, fwd_cols_kernel<UGSDR_SAMPLES_RI8, F1>, p, items, t1); break;
+				}
+				const size_t smem = smem_rows(p, false);
+				set_smem(fwd_rows_kernel<F2>, smem);
+				fwd_rows_kernel<F2><<<items * chunks_of(p.n1, p.rw), threads_of<F2>(p.p2, p.rw), smem, ctx->stream>>>(p);
+			});
 			note_launch(ctx, 2);
 		}
 	}
@@ -278,26 +305,31 @@ namespace ugsdr_gpu {
 				p.zcg = reinterpret_cast<float2*>(carve(sizeof(float2) * static_cast<size_t>(r_max) * s.k * s.m));
 		}
 		const size_t smem_r = smem_rows(p, true), smem_c = smem_cols(p, true);
-		set_smem(inv_rows_kernel, smem_r);
-		set_smem(inv_cols_kernel, smem_c);
-		KernelTimer timer(ctx, "acq_inverse_large");
-		for (int row0 = 0; row0 < s.rows; row0 += r_max) {
-			p.row0 = row0;
-			p.rows = std::min(r_max, s.rows - row0);
-			UG_CUDA(cudaMemsetAsync(p.counters, 0, sizeof(unsigned int) * p.rows, ctx->stream));
-			if (s.fold_mode) {
-				UG_CUDA(cudaMemsetAsync(p.accg, 0, sizeof(float) * static_cast<size_t>(p.rows) * s.m, ctx->stream));
-				if (s.fold_mode == 2)
-					UG_CUDA(cudaMemsetAsync(p.zcg, 0, sizeof(float2) * static_cast<size_t>(p.rows) * s.k * s.m, ctx->stream));
+		with_large_ffts(p.n1, p.n2, [&](auto f1, auto f2) {
+			using F1 = decltype(f1);
+			using F2 = decltype(f2);
+			set_smem(inv_rows_kernel<F2>, smem_r);
+			set_smem(inv_cols_kernel<F1>, smem_c);
+			const int t_rows = threads_of<F2>(p.p2, p.rw), t_cols = threads_of<F1>(p.p1, p.cw);
+			KernelTimer timer(ctx, "acq_inverse_large");
+			for (int row0 = 0; row0 < s.rows; row0 += r_max) {
+				p.row0 = row0;
+				p.rows = std::min(r_max, s.rows - row0);
+				UG_CUDA(cudaMemsetAsync(p.counters, 0, sizeof(unsigned int) * p.rows, ctx->stream));
+				if (s.fold_mode) {
+					UG_CUDA(cudaMemsetAsync(p.accg, 0, sizeof(float) * static_cast<size_t>(p.rows) * s.m, ctx->stream));
+					if (s.fold_mode == 2)
+						UG_CUDA(cudaMemsetAsync(p.zcg, 0, sizeof(float2) * static_cast<size_t>(p.rows) * s.k * s.m, ctx->stream));
+				}
+				inv_rows_kernel<F2><<<p.rows * s.k * chunks_of(p.n1, p.rw), t_rows, smem_r, ctx->stream>>>(p);
+				inv_cols_kernel<F1><<<p.rows * chunks, t_cols, smem_c, ctx->stream>>>(p);
+				note_launch(ctx, 2);
+				if (s.fold_mode) {
+					fold_finish_kernel<<<p.rows, kBatchedThreads, 0, ctx->stream>>>(p);
+					note_launch(ctx);
+				}
 			}
-			inv_rows_kernel<<<p.rows * s.k * chunks_of(p.n1, p.rw), threads_for(p.p2, p.rw), smem_r, ctx->stream>>>(p);
-			inv_cols_kernel<<<p.rows * chunks, threads_for(p.p1, p.cw), smem_c, ctx->stream>>>(p);
-			note_launch(ctx, 2);
-			if (s.fold_mode) {
-				fold_finish_kernel<<<p.rows, kBatchedThreads, 0, ctx->stream>>>(p);
-				note_launch(ctx);
-			}
-		}
+		});
 	}
 
 	namespace {

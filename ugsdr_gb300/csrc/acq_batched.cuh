@@ -23,6 +23,7 @@
 #pragma once
 
 #include "acq_kernels.cuh"
+#include "fft_static.cuh"
 
 namespace ugsdr_gpu {
 
@@ -48,6 +49,32 @@ namespace ugsdr_gpu {
 			ns *= r;
 		}
 		return a;
+	}
+
+	// FFT policy of the runtime plan (any plannable size); StaticFft is the
+	// compile-time alternative for the configured sizes.
+	struct RuntimeFft {
+		static constexpr int N = 0;
+		template <bool INV>
+		__device__ static float2* run(float2* a, float2* b, const FftPlanDev& plan, int batch, int ld) {
+			return passes_batch<INV>(a, b, plan, batch, ld);
+		}
+	};
+
+	// sub-transform length and division by it: constants for a static plan
+	template <class F>
+	__device__ __forceinline__ int fft_n(int runtime_n) {
+		if constexpr (F::N > 0)
+			return F::N;
+		else
+			return runtime_n;
+	}
+	template <class F>
+	__device__ __forceinline__ int div_fft_n(int e, float inv_runtime_n) {
+		if constexpr (F::N > 0)
+			return e / F::N;
+		else
+			return fdiv(e, inv_runtime_n);
 	}
 
 	// W_N^e (conjugated when inv) for 0 <= e < N: sincospi of 2 e' / N with
@@ -108,14 +135,14 @@ namespace ugsdr_gpu {
 	}
 
 	// grid: items * ceil(N2 / cw)
-	template <int ST>
+	template <int ST, class F1>
 	__global__ void __launch_bounds__(256, 3) fwd_cols_kernel(BatchedParams p) {
 		extern __shared__ float2 smem[];
 		__shared__ float lut[80];
 		if (threadIdx.x < 80 && p.base.lut)
 			lut[threadIdx.x] = p.base.lut[threadIdx.x];
 		__syncthreads();
-		const int n1 = p.n1, n2 = p.n2;
+		const int n1 = fft_n<F1>(p.n1), n2 = p.n2;
 		const int chunks = (n2 + p.cw - 1) >> p.cw_shift;
 		const int item = blockIdx.x / chunks;
 		const int c0 = (blockIdx.x - item * chunks) << p.cw_shift;
@@ -131,7 +158,7 @@ namespace ugsdr_gpu {
 				a[f * ld + i1] = fwd_load<ST>(p, item, static_cast<int64_t>(n2) * i1 + c0 + f, lut);
 		}
 		__syncthreads();
-		const float2* y = passes_batch<false>(a, b, p.p1, cw, ld);
+		const float2* y = F1::template run<false>(a, b, p.p1, cw, ld);
 		float2* out = p.out + static_cast<size_t>(item) * p.base.n;
 		const float inv_n2 = 2.0f / static_cast<float>(p.base.n);
 		for (int e = threadIdx.x; e < p.cw * n1; e += blockDim.x) {
@@ -143,9 +170,10 @@ namespace ugsdr_gpu {
 	}
 
 	// grid: items * ceil(N1 / rw); code mode also conjugates and masks (conj(FFT(code)))
+	template <class F2>
 	__global__ void __launch_bounds__(256, 3) fwd_rows_kernel(BatchedParams p) {
 		extern __shared__ float2 smem[];
-		const int n1 = p.n1, n2 = p.n2;
+		const int n1 = p.n1, n2 = fft_n<F2>(p.n2);
 		const int chunks = (n1 + p.rw - 1) / p.rw;
 		const int item = blockIdx.x / chunks;
 		const int r0 = (blockIdx.x - item * chunks) * p.rw;
@@ -156,11 +184,11 @@ namespace ugsdr_gpu {
 		for (int e = threadIdx.x; e < rw * n2; e += blockDim.x)
 			a[e] = out[e];
 		__syncthreads();
-		const float2* y = passes_batch<false>(a, b, p.p2, rw, n2);
+		const float2* y = F2::template run<false>(a, b, p.p2, rw, n2);
 		const int half = p.base.n / 2;
 		const float inv_n2f = 1.0f / static_cast<float>(n2);
 		for (int e = threadIdx.x; e < rw * n2; e += blockDim.x) {
-			const int ri = fdiv(e, inv_n2f), k2 = e - ri * n2;
+			const int ri = div_fft_n<F2>(e, inv_n2f), k2 = e - ri * n2;
 			const int64_t k = (r0 + ri) + static_cast<int64_t>(n1) * k2;
 			const bool zero = p.base.one_sided && k > half;
 			if (p.code_mode) {
@@ -175,10 +203,11 @@ namespace ugsdr_gpu {
 
 	// ------------------------------------------------------------- inverse
 	// grid: rows * K * ceil(N1 / rw)
+	template <class F2>
 	__global__ void __launch_bounds__(256, 3) inv_rows_kernel(BatchedParams p) {
 		extern __shared__ float2 smem[];
 		const AcqParams& q = p.base;
-		const int n1 = p.n1, n2 = p.n2, n = q.n;
+		const int n1 = p.n1, n2 = fft_n<F2>(p.n2), n = q.n;
 		const int chunks = (n1 + p.rw - 1) / p.rw;
 		const int item = blockIdx.x / chunks;       // (local row, block)
 		const int r0 = (blockIdx.x - item * chunks) * p.rw;
@@ -195,28 +224,40 @@ namespace ugsdr_gpu {
 		const int half = n / 2;
 		const float inv_n2f = 1.0f / static_cast<float>(n2);
 		for (int e = threadIdx.x; e < rw * n2; e += blockDim.x) {
-			const int ri = fdiv(e, inv_n2f), k2 = e - ri * n2;
+			const int ri = div_fft_n<F2>(e, inv_n2f), k2 = e - ri * n2;
 			const int64_t k = (r0 + ri) + static_cast<int64_t>(n1) * k2;
 			a[e] = (q.one_sided && k > half) ? c2(0.f, 0.f) : cmul(__ldg(x + e), __ldg(code + e));
 		}
 		__syncthreads();
-		const float2* y = passes_batch<true>(a, b, p.p2, rw, n2);
+		const float2* y = F2::template run<true>(a, b, p.p2, rw, n2);
 		float2* out = p.bbuf + static_cast<size_t>(item) * n + static_cast<size_t>(r0) * n2;
 		const float inv_n2 = 2.0f / static_cast<float>(n);
-		for (int e = threadIdx.x; e < rw * n2; e += blockDim.x) {
-			const int ri = fdiv(e, inv_n2f), i2 = e - ri * n2;
-			out[e] = cmul(y[e], tw_n(static_cast<uint32_t>(i2) * static_cast<uint32_t>(r0 + ri), n, inv_n2, true));
+		// inter-step twiddle W_N^{-i2 k1}: one warp per row k1, lane l takes
+		// i2 = l, l + 32, ... and advances its twiddle by W_N^{-32 k1} (two
+		// sincospif per lane and row, at most n2 / 32 products in the chain)
+		const int lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+		for (int ri = threadIdx.x >> 5; ri < rw; ri += nwarps) {
+			const uint32_t k1 = static_cast<uint32_t>(r0 + ri);
+			float2 w = tw_n((static_cast<uint32_t>(lane) * k1) % static_cast<uint32_t>(n), n, inv_n2, true);
+			const float2 step = tw_n((32u * k1) % static_cast<uint32_t>(n), n, inv_n2, true);
+			const float2* yr = y + ri * n2;
+			float2* orow = out + ri * n2;
+			for (int i2 = lane; i2 < n2; i2 += 32) {
+				orow[i2] = cmul(yr[i2], w);
+				w = cmul(w, step);
+			}
 		}
 	}
 
 	// grid: rows * ceil(N2 / cw); shared: 3 * cw * ld1 float2 (input, work, prefetch) + cw * ld1 float
+	template <class F1>
 	__global__ void __launch_bounds__(256, 2) inv_cols_kernel(BatchedParams p) {
 		extern __shared__ float2 smem[];
 		__shared__ MaxIdx s_max[8];
 		__shared__ double s_sum[8], s_sq[8];
 		__shared__ bool s_last;
 		const AcqParams& q = p.base;
-		const int n1 = p.n1, n2 = p.n2, n = q.n, m = q.m;
+		const int n1 = fft_n<F1>(p.n1), n2 = p.n2, n = q.n, m = q.m;
 		const int chunks = (n2 + p.cw - 1) >> p.cw_shift;
 		const int lrow = blockIdx.x / chunks;
 		const int chunk = blockIdx.x - lrow * chunks;
@@ -249,17 +290,17 @@ namespace ugsdr_gpu {
 			__syncthreads();
 			if (blk + 1 < q.k_blocks)
 				prefetch(pre, blk + 1);
-			const float2* y = passes_batch<true>(in, work, p.p1, cw, ld);
+			const float2* y = F1::template run<true>(in, work, p.p1, cw, ld);
 			if (q.fold_mode == 0) {
 				for (int e = threadIdx.x; e < cw * n1; e += blockDim.x) {
-					const int f = fdiv(e, inv_n1), i1 = e - f * n1;
+					const int f = div_fft_n<F1>(e, inv_n1), i1 = e - f * n1;
 					acc[f * ld + i1] += stat_of(cscale(cscale(y[f * ld + i1], inv_n), post), q.stat);
 				}
 			}
 			else if (q.fold_mode == 1) {
 				float* ag = p.accg + static_cast<size_t>(lrow) * m;
 				for (int e = threadIdx.x; e < cw * n1; e += blockDim.x) {
-					const int f = fdiv(e, inv_n1), i1 = e - f * n1;
+					const int f = div_fft_n<F1>(e, inv_n1), i1 = e - f * n1;
 					const uint32_t tau = static_cast<uint32_t>(n2) * i1 + c0 + f;
 					atomicAdd(ag + tau % static_cast<uint32_t>(m), stat_of(cscale(cscale(y[f * ld + i1], inv_n), post), q.stat));
 				}
@@ -267,7 +308,7 @@ namespace ugsdr_gpu {
 			else {
 				float2* zg = p.zcg + (static_cast<size_t>(lrow) * q.k_blocks + blk) * m;
 				for (int e = threadIdx.x; e < cw * n1; e += blockDim.x) {
-					const int f = fdiv(e, inv_n1), i1 = e - f * n1;
+					const int f = div_fft_n<F1>(e, inv_n1), i1 = e - f * n1;
 					const uint32_t tau = static_cast<uint32_t>(n2) * i1 + c0 + f;
 					const float2 v = cscale(cscale(y[f * ld + i1], inv_n), post);
 					float2* z = zg + tau % static_cast<uint32_t>(m);
@@ -286,7 +327,7 @@ namespace ugsdr_gpu {
 		MaxIdx best{-1.0f, 0xFFFFFFFFu};
 		float sum = 0.f, sq = 0.f;
 		for (int e = threadIdx.x; e < cw * n1; e += blockDim.x) {
-			const int f = fdiv(e, inv_n1), i1 = e - f * n1;
+			const int f = div_fft_n<F1>(e, inv_n1), i1 = e - f * n1;
 			const float v = acc[f * ld + i1];
 			const MaxIdx cand{v, static_cast<uint32_t>(n2) * i1 + c0 + f};
 			best = better(best, cand);
