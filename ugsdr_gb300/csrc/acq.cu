@@ -112,8 +112,11 @@ namespace ugsdr_gpu {
 			const int b = n / a;
 			if (!plan_radices(a, r) || !plan_radices(b, r))
 				continue;
-			// both tiles must fit with at least 4 columns / 1 row
-			if (2 * sizeof(float2) * 4 * static_cast<size_t>(a) > budget || 2 * sizeof(float2) * static_cast<size_t>(b) > budget)
+			// both kernels' tiles and twiddle tables must fit with at least
+			// 4 columns (inverse: 3 tiles + accumulator) and 1 row (2 tiles)
+			const size_t cols = (3 * sizeof(float2) + sizeof(float)) * 4 * static_cast<size_t>(a | 1) + sizeof(float2) * a + 16;
+			const size_t rows = 3 * sizeof(float2) * static_cast<size_t>(b) + 16;
+			if (cols > budget || rows > budget)
 				continue;
 			best1 = a;  // increasing a -> closest to sqrt(n) last
 		}
@@ -172,10 +175,10 @@ namespace ugsdr_gpu {
 		void tile_shape(ugsdr_ctx* ctx, const LargePlan& lp, int& cw, int& rw) {
 			const size_t ld = static_cast<size_t>(lp.n1 | 1);
 			cw = 8;
-			while (cw > 1 && (3 * sizeof(float2) + sizeof(float)) * cw * ld > (ctx->smem_optin - 2048) / 2)
+			while (cw > 1 && (3 * sizeof(float2) + sizeof(float)) * cw * ld + sizeof(float2) * lp.n1 + 16 > (ctx->smem_optin - 2048) / 2)
 				cw /= 2;
 			rw = 8;
-			while (rw > 1 && 2 * sizeof(float2) * rw * static_cast<size_t>(lp.n2) > (ctx->smem_optin - 2048) / 3)
+			while (rw > 1 && 2 * sizeof(float2) * rw * static_cast<size_t>(lp.n2) + sizeof(float2) * lp.n2 + 16 > (ctx->smem_optin - 2048) / 3)
 				rw /= 2;
 		}
 
@@ -197,11 +200,12 @@ namespace ugsdr_gpu {
 
 		// fwd_cols: two tiles; inv_cols: input, work and prefetch tiles + accumulator
 		size_t smem_cols(const BatchedParams& p, bool inverse) {
-			return (inverse ? 3 * sizeof(float2) + sizeof(float) : 2 * sizeof(float2)) * static_cast<size_t>(p.cw) * p.ld1;
+			return (inverse ? 3 * sizeof(float2) + sizeof(float) : 2 * sizeof(float2)) * static_cast<size_t>(p.cw) * p.ld1
+				+ sizeof(float2) * p.n1 + 16;  // + the N1-point twiddle table
 		}
-		// row kernels: two tiles
+		// row kernels: two tiles + the N2-point twiddle table
 		size_t smem_rows(const BatchedParams& p, bool) {
-			return 2 * sizeof(float2) * static_cast<size_t>(p.rw) * p.n2;
+			return 2 * sizeof(float2) * static_cast<size_t>(p.rw) * p.n2 + sizeof(float2) * p.n2 + 16;
 		}
 
 		int chunks_of(int total, int per) { return (total + per - 1) / per; }

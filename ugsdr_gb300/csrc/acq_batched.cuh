@@ -61,6 +61,18 @@ namespace ugsdr_gpu {
 		}
 	};
 
+	// The plan's twiddle table copied into shared memory at `dst` (16-byte
+	// aligned, n entries); returns the plan pointing at the copy.  Call before
+	// the CTA's first __syncthreads.
+	__device__ __forceinline__ FftPlanDev plan_in_smem(const FftPlanDev& plan, void* dst, int n) {
+		float2* t = reinterpret_cast<float2*>((reinterpret_cast<uintptr_t>(dst) + 15) & ~static_cast<uintptr_t>(15));
+		for (int i = threadIdx.x; i < n; i += blockDim.x)
+			t[i] = __ldg(plan.tw + i);
+		FftPlanDev out = plan;
+		out.tw = t;
+		return out;
+	}
+
 	// sub-transform length and division by it: constants for a static plan
 	template <class F>
 	__device__ __forceinline__ int fft_n(int runtime_n) {
@@ -151,6 +163,7 @@ namespace ugsdr_gpu {
 		const int mask = p.cw - 1;
 		float2* a = smem;
 		float2* b = smem + p.cw * ld;
+		const FftPlanDev p1 = plan_in_smem(p.p1, smem + 2 * p.cw * ld, n1);
 		// consecutive threads take consecutive columns of one n1 row: coalesced reads
 		for (int e = threadIdx.x; e < p.cw * n1; e += blockDim.x) {
 			const int f = e & mask, i1 = e >> p.cw_shift;
@@ -158,7 +171,7 @@ namespace ugsdr_gpu {
 				a[f * ld + i1] = fwd_load<ST>(p, item, static_cast<int64_t>(n2) * i1 + c0 + f, lut);
 		}
 		__syncthreads();
-		const float2* y = F1::template run<false>(a, b, p.p1, cw, ld);
+		const float2* y = F1::template run<false>(a, b, p1, cw, ld);
 		float2* out = p.out + static_cast<size_t>(item) * p.base.n;
 		const float inv_n2 = 2.0f / static_cast<float>(p.base.n);
 		for (int e = threadIdx.x; e < p.cw * n1; e += blockDim.x) {
@@ -180,11 +193,12 @@ namespace ugsdr_gpu {
 		const int rw = min(p.rw, n1 - r0);
 		float2* a = smem;
 		float2* b = smem + p.rw * n2;
+		const FftPlanDev p2 = plan_in_smem(p.p2, smem + 2 * p.rw * n2, n2);
 		float2* out = p.out + static_cast<size_t>(item) * p.base.n + static_cast<size_t>(r0) * n2;
 		for (int e = threadIdx.x; e < rw * n2; e += blockDim.x)
 			a[e] = out[e];
 		__syncthreads();
-		const float2* y = F2::template run<false>(a, b, p.p2, rw, n2);
+		const float2* y = F2::template run<false>(a, b, p2, rw, n2);
 		const int half = p.base.n / 2;
 		const float inv_n2f = 1.0f / static_cast<float>(n2);
 		for (int e = threadIdx.x; e < rw * n2; e += blockDim.x) {
@@ -221,15 +235,33 @@ namespace ugsdr_gpu {
 		const float2* code = q.codes[c] + static_cast<size_t>(r0) * n2;
 		float2* a = smem;
 		float2* b = smem + p.rw * n2;
+		const FftPlanDev p2 = plan_in_smem(p.p2, smem + 2 * p.rw * n2, n2);
 		const int half = n / 2;
 		const float inv_n2f = 1.0f / static_cast<float>(n2);
-		for (int e = threadIdx.x; e < rw * n2; e += blockDim.x) {
-			const int ri = div_fft_n<F2>(e, inv_n2f), k2 = e - ri * n2;
-			const int64_t k = (r0 + ri) + static_cast<int64_t>(n1) * k2;
-			a[e] = (q.one_sided && k > half) ? c2(0.f, 0.f) : cmul(__ldg(x + e), __ldg(code + e));
+		// Z = X * C, four element pairs in flight per thread
+		const int total = rw * n2;
+		for (int e0 = threadIdx.x; e0 < total; e0 += 4 * blockDim.x) {
+			float2 xv[4], cv[4];
+#pragma unroll
+			for (int u = 0; u < 4; ++u) {
+				const int e = e0 + u * blockDim.x;
+				if (e < total) {
+					xv[u] = __ldg(x + e);
+					cv[u] = __ldg(code + e);
+				}
+			}
+#pragma unroll
+			for (int u = 0; u < 4; ++u) {
+				const int e = e0 + u * blockDim.x;
+				if (e < total) {
+					const int ri = div_fft_n<F2>(e, inv_n2f), k2 = e - ri * n2;
+					const int64_t k = (r0 + ri) + static_cast<int64_t>(n1) * k2;
+					a[e] = (q.one_sided && k > half) ? c2(0.f, 0.f) : cmul(xv[u], cv[u]);
+				}
+			}
 		}
 		__syncthreads();
-		const float2* y = F2::template run<true>(a, b, p.p2, rw, n2);
+		const float2* y = F2::template run<true>(a, b, p2, rw, n2);
 		float2* out = p.bbuf + static_cast<size_t>(item) * n + static_cast<size_t>(r0) * n2;
 		const float inv_n2 = 2.0f / static_cast<float>(n);
 		// inter-step twiddle W_N^{-i2 k1}: one warp per row k1, lane l takes
@@ -270,6 +302,7 @@ namespace ugsdr_gpu {
 		float2* work = smem + tile;
 		float2* pre = smem + 2 * tile;
 		float* acc = reinterpret_cast<float*>(smem + 3 * tile);
+		const FftPlanDev p1 = plan_in_smem(p.p1, acc + tile, n1);
 		const float inv_n = 1.0f / static_cast<float>(n);
 		const float post = q.one_sided ? 2.0f : 1.0f;
 		const float inv_n1 = 1.0f / static_cast<float>(n1);
@@ -290,7 +323,7 @@ namespace ugsdr_gpu {
 			__syncthreads();
 			if (blk + 1 < q.k_blocks)
 				prefetch(pre, blk + 1);
-			const float2* y = F1::template run<true>(in, work, p.p1, cw, ld);
+			const float2* y = F1::template run<true>(in, work, p1, cw, ld);
 			if (q.fold_mode == 0) {
 				for (int e = threadIdx.x; e < cw * n1; e += blockDim.x) {
 					const int f = div_fft_n<F1>(e, inv_n1), i1 = e - f * n1;

@@ -34,7 +34,7 @@ namespace ugsdr_gpu {
 				const int step = TW_STEP * k;
 #pragma unroll
 				for (int r = 1; r < R; ++r) {
-					const float2 w = __ldg(tw + r * step);
+					const float2 w = tw[r * step];  // generic load: the table may sit in shared memory
 					v[r] = INV ? cmulc(v[r], w) : cmul(v[r], w);
 				}
 			}
