@@ -161,8 +161,8 @@ namespace ugsdr_gpu {
 				fn(StaticFft<200, 25, 8>{}, StaticFft<250, 25, 10>{});          // 50,000: 1 ms at 50 MHz
 			else if (n1 == 400 && n2 == 500)
 				fn(StaticFft<400, 25, 16>{}, StaticFft<500, 25, 20>{});         // 200,000: 4 ms at 50 MHz
-			else if (n1 == 440 && n2 == 465)
-				fn(StaticFft<440, 11, 5, 8>{}, StaticFft<465, 31, 15>{});       // 204,600: 10 ms at 20.46 MHz
+			else if (n1 == 440 && n2 == 465)  // 204,600: 10 ms at 20.46 MHz; fusing the radix-31 rows spills
+				fn(StaticFft<440, 11, 5, 8>{}, StaticFftPlain<465, 31, 15>{});
 			else
 				fn(RuntimeFft{}, RuntimeFft{});
 		}

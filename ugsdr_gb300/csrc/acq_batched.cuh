@@ -55,6 +55,7 @@ namespace ugsdr_gpu {
 	// compile-time alternative for the configured sizes.
 	struct RuntimeFft {
 		static constexpr int N = 0;
+		static constexpr bool kHooked = false;
 		template <bool INV>
 		__device__ static float2* run(float2* a, float2* b, const FftPlanDev& plan, int batch, int ld) {
 			return passes_batch<INV>(a, b, plan, batch, ld);
@@ -216,6 +217,73 @@ namespace ugsdr_gpu {
 	}
 
 	// ------------------------------------------------------------- inverse
+	// Hooks of the static inverse plans.  Row stage: pass 0 gathers Z = X * C
+	// straight from the spectra (bins above N/2 are zero one-sided), the last
+	// pass applies W_N^{-i2 k1} (per-butterfly recurrence over its outputs,
+	// i2 = base + r NS) and stores B.
+	struct InvRowsLoad {
+		const float2* x;
+		const float2* code;
+		int n1, n2, r0, half, one_sided;
+		__device__ __forceinline__ float2 operator()(int f, int k2) const {
+			if (one_sided && (r0 + f) + n1 * k2 > half)
+				return c2(0.f, 0.f);
+			const size_t off = static_cast<size_t>(f) * n2 + k2;
+			return cmul(__ldg(x + off), __ldg(code + off));
+		}
+	};
+	struct InvRowsEmit {
+		float2* out;
+		int n2, r0;
+		uint32_t n;
+		float inv_n2;  // 2 / N
+		template <int R, int NS>
+		__device__ __forceinline__ void put(int f, int base, const float2 (&v)[R]) const {
+			const uint32_t k1 = static_cast<uint32_t>(r0 + f);
+			float2 w = tw_n((static_cast<uint32_t>(base) * k1) % n, n, inv_n2, true);
+			const float2 step = tw_n((static_cast<uint32_t>(NS) * k1) % n, n, inv_n2, true);
+			float2* o = out + static_cast<size_t>(f) * n2 + base;
+#pragma unroll
+			for (int r = 0; r < R; ++r) {
+				o[r * NS] = cmul(v[r], w);
+				w = cmul(w, step);
+			}
+		}
+	};
+	// Column stage: the last pass scales each output (1/N, x2 one-sided),
+	// takes |.| or |.|^2 and accumulates it (or, folded, adds it to the row's
+	// fold buffer) instead of storing the transform.
+	struct InvColsEmit {
+		float* acc;
+		int ld, stat, fold_mode, n2, c0, m;
+		float scale;
+		float* ag;
+		float2* zg;
+		template <int R, int NS>
+		__device__ __forceinline__ void put(int f, int base, const float2 (&v)[R]) const {
+			if (fold_mode == 0) {
+				float* a = acc + f * ld + base;
+#pragma unroll
+				for (int r = 0; r < R; ++r)
+					a[r * NS] += stat_of(cscale(v[r], scale), stat);
+				return;
+			}
+#pragma unroll
+			for (int r = 0; r < R; ++r) {
+				const uint32_t tau = static_cast<uint32_t>(n2) * static_cast<uint32_t>(base + r * NS) + c0 + f;
+				const float2 y = cscale(v[r], scale);
+				if (fold_mode == 1) {
+					atomicAdd(ag + tau % static_cast<uint32_t>(m), stat_of(y, stat));
+				}
+				else {
+					float2* z = zg + tau % static_cast<uint32_t>(m);
+					atomicAdd(&z->x, y.x);
+					atomicAdd(&z->y, y.y);
+				}
+			}
+		}
+	};
+
 	// grid: rows * K * ceil(N1 / rw)
 	template <class F2>
 	__global__ void __launch_bounds__(256, 3) inv_rows_kernel(BatchedParams p) {
@@ -238,6 +306,14 @@ namespace ugsdr_gpu {
 		const FftPlanDev p2 = plan_in_smem(p.p2, smem + 2 * p.rw * n2, n2);
 		const int half = n / 2;
 		const float inv_n2f = 1.0f / static_cast<float>(n2);
+		if constexpr (F2::kHooked) {
+			float2* out = p.bbuf + static_cast<size_t>(item) * n + static_cast<size_t>(r0) * n2;
+			const InvRowsLoad load{x, code, n1, n2, r0, half, q.one_sided};
+			const InvRowsEmit emit{out, n2, r0, static_cast<uint32_t>(n), 2.0f / static_cast<float>(n)};
+			__syncthreads();  // twiddle table in shared memory
+			F2::template run_hooked<true, true>(a, b, p2, rw, n2, load, emit);
+			return;
+		}
 		// Z = X * C, four element pairs in flight per thread
 		const int total = rw * n2;
 		for (int e0 = threadIdx.x; e0 < total; e0 += 4 * blockDim.x) {
@@ -323,6 +399,18 @@ namespace ugsdr_gpu {
 			__syncthreads();
 			if (blk + 1 < q.k_blocks)
 				prefetch(pre, blk + 1);
+			if constexpr (F1::kHooked) {
+				float2* zg = q.fold_mode == 2 ? p.zcg + (static_cast<size_t>(lrow) * q.k_blocks + blk) * m : nullptr;
+				const InvColsEmit emit{acc, ld, q.stat, q.fold_mode, n2, c0, m, inv_n * post,
+					q.fold_mode == 1 ? p.accg + static_cast<size_t>(lrow) * m : nullptr, zg};
+				const NoLoad none{};
+				F1::template run_hooked<true, false>(in, work, p1, cw, ld, none, emit);
+				__syncthreads();
+				float2* t = in;
+				in = pre;
+				pre = t;
+				continue;
+			}
 			const float2* y = F1::template run<true>(in, work, p1, cw, ld);
 			if (q.fold_mode == 0) {
 				for (int e = threadIdx.x; e < cw * n1; e += blockDim.x) {

@@ -65,6 +65,70 @@ namespace ugsdr_gpu {
 		}
 	};
 
+	// Hooked pass: when FIRST, inputs come from load(f, i) (element i of
+	// transform f) instead of `in`; when LAST, each butterfly's outputs go to
+	// emit.put<R, NS>(f, base, v) — v[r] is output element base + r * NS —
+	// instead of `out`.  Fusing the producer and consumer into the first and
+	// last passes saves a shared-memory round trip and a barrier each.
+	template <int N, int R, int NS, bool INV, bool FIRST, bool LAST, class Load, class Emit>
+	__device__ __forceinline__ void hooked_pass(const float2* __restrict__ in, float2* __restrict__ out,
+		const float2* __restrict__ tw, int batch, int ld, Load& load, Emit& emit) {
+		constexpr int NB = N / R;
+		constexpr int TW_STEP = N / (NS * R);
+		const int total = NB * batch;
+		for (int u = threadIdx.x; u < total; u += blockDim.x) {
+			const int f = u / NB;
+			const int j = u - f * NB;
+			const int k = NS == 1 ? 0 : j % NS;
+			float2 v[R];
+			if constexpr (FIRST) {
+#pragma unroll
+				for (int r = 0; r < R; ++r)
+					v[r] = load(f, j + r * NB);
+			}
+			else {
+				const float2* src = in + f * ld + j;
+#pragma unroll
+				for (int r = 0; r < R; ++r)
+					v[r] = src[r * NB];
+			}
+			if constexpr (NS > 1) {
+				const int step = TW_STEP * k;
+#pragma unroll
+				for (int r = 1; r < R; ++r) {
+					const float2 w = tw[r * step];
+					v[r] = INV ? cmulc(v[r], w) : cmul(v[r], w);
+				}
+			}
+			Dft<R, INV>::run(v);
+			if constexpr (LAST) {
+				emit.template put<R, NS>(f, (j - k) * R + k, v);
+			}
+			else {
+				float2* dst = out + f * ld + (j - k) * R + k;
+#pragma unroll
+				for (int r = 0; r < R; ++r)
+					dst[r * NS] = v[r];
+			}
+		}
+	}
+
+	template <int N, int NS, bool INV, bool FIRST, int... Rs>
+	struct HookedPasses;
+
+	template <int N, int NS, bool INV, bool FIRST, int R, int... Rest>
+	struct HookedPasses<N, NS, INV, FIRST, R, Rest...> {
+		template <class Load, class Emit>
+		__device__ static void run(float2* a, float2* b, const float2* tw, int batch, int ld, Load& load, Emit& emit) {
+			constexpr bool LAST = sizeof...(Rest) == 0;
+			hooked_pass<N, R, NS, INV, FIRST, LAST>(a, b, tw, batch, ld, load, emit);
+			if constexpr (!LAST) {
+				__syncthreads();
+				HookedPasses<N, NS * R, INV, false, Rest...>::run(b, a, tw, batch, ld, load, emit);
+			}
+		}
+	};
+
 	template <int... Rs>
 	constexpr int radix_product() {
 		return (1 * ... * Rs);
@@ -83,11 +147,31 @@ namespace ugsdr_gpu {
 	struct StaticFft {
 		static_assert(radix_product<Rs...>() == N_, "radices must multiply to N");
 		static constexpr int N = N_;
+		static constexpr bool kHooked = true;  // kernels fuse their producer/consumer into the first/last pass
 		// most butterflies of one pass over `batch` transforms
 		static constexpr int most_butterflies(int batch) { return batch * (N_ / radix_min<Rs...>()); }
 		template <bool INV>
 		__device__ static float2* run(float2* a, float2* b, const FftPlanDev& plan, int batch, int ld) {
 			return StaticPasses<N_, 1, INV, Rs...>::run(a, b, plan.tw, batch, ld);
 		}
+		// Pass 0 reads `a` (or gathers through `load` when FIRST), intermediate
+		// passes ping-pong between the tiles, the last pass emits.  With FIRST and
+		// two radices only one tile (`b`) is used.
+		template <bool INV, bool FIRST, class Load, class Emit>
+		__device__ static void run_hooked(float2* a, float2* b, const FftPlanDev& plan, int batch, int ld, Load& load, Emit& emit) {
+			HookedPasses<N_, 1, INV, FIRST, Rs...>::run(a, b, plan.tw, batch, ld, load, emit);
+		}
+	};
+
+	// The same plan with the kernels' separate load / epilogue loops (for
+	// plans whose fused first pass would hold too many registers).
+	template <int N_, int... Rs>
+	struct StaticFftPlain : StaticFft<N_, Rs...> {
+		static constexpr bool kHooked = false;
+	};
+
+	// a load hook for plans that read their first pass from shared memory
+	struct NoLoad {
+		__device__ float2 operator()(int, int) const { return c2(0.f, 0.f); }
 	};
 }
