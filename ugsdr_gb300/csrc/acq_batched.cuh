@@ -51,17 +51,6 @@ namespace ugsdr_gpu {
 		return a;
 	}
 
-	// FFT policy of the runtime plan (any plannable size); StaticFft is the
-	// compile-time alternative for the configured sizes.
-	struct RuntimeFft {
-		static constexpr int N = 0;
-		static constexpr bool kHooked = false;
-		template <bool INV>
-		__device__ static float2* run(float2* a, float2* b, const FftPlanDev& plan, int batch, int ld) {
-			return passes_batch<INV>(a, b, plan, batch, ld);
-		}
-	};
-
 	// The plan's twiddle table copied into shared memory at `dst` (16-byte
 	// aligned, n entries); returns the plan pointing at the copy.  Call before
 	// the CTA's first __syncthreads.
@@ -73,6 +62,18 @@ namespace ugsdr_gpu {
 		out.tw = t;
 		return out;
 	}
+
+	// FFT policy of the runtime plan (any plannable size); StaticFft is the
+	// compile-time alternative for the configured sizes.
+	struct RuntimeFft {
+		static constexpr int N = 0;
+		static constexpr bool kHooked = false;
+		__device__ static FftPlanDev prepare(const FftPlanDev& plan, void* dst) { return plan_in_smem(plan, dst, plan.n); }
+		template <bool INV>
+		__device__ static float2* run(float2* a, float2* b, const FftPlanDev& plan, int batch, int ld) {
+			return passes_batch<INV>(a, b, plan, batch, ld);
+		}
+	};
 
 	// sub-transform length and division by it: constants for a static plan
 	template <class F>
@@ -164,7 +165,7 @@ namespace ugsdr_gpu {
 		const int mask = p.cw - 1;
 		float2* a = smem;
 		float2* b = smem + p.cw * ld;
-		const FftPlanDev p1 = plan_in_smem(p.p1, smem + 2 * p.cw * ld, n1);
+		const FftPlanDev p1 = F1::prepare(p.p1, smem + 2 * p.cw * ld);
 		// consecutive threads take consecutive columns of one n1 row: coalesced reads
 		for (int e = threadIdx.x; e < p.cw * n1; e += blockDim.x) {
 			const int f = e & mask, i1 = e >> p.cw_shift;
@@ -194,7 +195,7 @@ namespace ugsdr_gpu {
 		const int rw = min(p.rw, n1 - r0);
 		float2* a = smem;
 		float2* b = smem + p.rw * n2;
-		const FftPlanDev p2 = plan_in_smem(p.p2, smem + 2 * p.rw * n2, n2);
+		const FftPlanDev p2 = F2::prepare(p.p2, smem + 2 * p.rw * n2);
 		float2* out = p.out + static_cast<size_t>(item) * p.base.n + static_cast<size_t>(r0) * n2;
 		for (int e = threadIdx.x; e < rw * n2; e += blockDim.x)
 			a[e] = out[e];
@@ -303,7 +304,7 @@ namespace ugsdr_gpu {
 		const float2* code = q.codes[c] + static_cast<size_t>(r0) * n2;
 		float2* a = smem;
 		float2* b = smem + p.rw * n2;
-		const FftPlanDev p2 = plan_in_smem(p.p2, smem + 2 * p.rw * n2, n2);
+		const FftPlanDev p2 = F2::prepare(p.p2, smem + 2 * p.rw * n2);
 		const int half = n / 2;
 		const float inv_n2f = 1.0f / static_cast<float>(n2);
 		if constexpr (F2::kHooked) {
@@ -378,7 +379,7 @@ namespace ugsdr_gpu {
 		float2* work = smem + tile;
 		float2* pre = smem + 2 * tile;
 		float* acc = reinterpret_cast<float*>(smem + 3 * tile);
-		const FftPlanDev p1 = plan_in_smem(p.p1, acc + tile, n1);
+		const FftPlanDev p1 = F1::prepare(p.p1, acc + tile);
 		const float inv_n = 1.0f / static_cast<float>(n);
 		const float post = q.one_sided ? 2.0f : 1.0f;
 		const float inv_n1 = 1.0f / static_cast<float>(n1);

@@ -19,7 +19,6 @@ namespace ugsdr_gpu {
 	__device__ __forceinline__ void static_pass(const float2* __restrict__ in, float2* __restrict__ out, const float2* __restrict__ tw,
 		int batch, int ld) {
 		constexpr int NB = N / R;           // butterflies per transform
-		constexpr int TW_STEP = N / (NS * R);
 		const int total = NB * batch;
 		for (int u = threadIdx.x; u < total; u += blockDim.x) {
 			const int f = u / NB;
@@ -31,10 +30,10 @@ namespace ugsdr_gpu {
 			for (int r = 0; r < R; ++r)
 				v[r] = src[r * NB];
 			if constexpr (NS > 1) {
-				const int step = TW_STEP * k;
+				const float2* wk = tw + k * (R - 1) - 1;  // this pass's table, [k][r - 1]
 #pragma unroll
 				for (int r = 1; r < R; ++r) {
-					const float2 w = tw[r * step];  // generic load: the table may sit in shared memory
+					const float2 w = wk[r];
 					v[r] = INV ? cmulc(v[r], w) : cmul(v[r], w);
 				}
 			}
@@ -56,12 +55,18 @@ namespace ugsdr_gpu {
 		__device__ static float2* run(float2* a, float2*, const float2*, int, int) { return a; }
 	};
 
+	// twiddle entries of a pass: W_N^{r k N / (NS R)} for k < NS, 1 <= r < R
+	template <int NS, int R>
+	constexpr int pass_table_size() {
+		return NS > 1 ? NS * (R - 1) : 0;
+	}
+
 	template <int N, int NS, bool INV, int R, int... Rest>
 	struct StaticPasses<N, NS, INV, R, Rest...> {
 		__device__ static float2* run(float2* a, float2* b, const float2* tw, int batch, int ld) {
 			static_pass<N, R, NS, INV>(a, b, tw, batch, ld);
 			__syncthreads();
-			return StaticPasses<N, NS * R, INV, Rest...>::run(b, a, tw, batch, ld);
+			return StaticPasses<N, NS * R, INV, Rest...>::run(b, a, tw + pass_table_size<NS, R>(), batch, ld);
 		}
 	};
 
@@ -74,7 +79,6 @@ namespace ugsdr_gpu {
 	__device__ __forceinline__ void hooked_pass(const float2* __restrict__ in, float2* __restrict__ out,
 		const float2* __restrict__ tw, int batch, int ld, Load& load, Emit& emit) {
 		constexpr int NB = N / R;
-		constexpr int TW_STEP = N / (NS * R);
 		const int total = NB * batch;
 		for (int u = threadIdx.x; u < total; u += blockDim.x) {
 			const int f = u / NB;
@@ -93,10 +97,10 @@ namespace ugsdr_gpu {
 					v[r] = src[r * NB];
 			}
 			if constexpr (NS > 1) {
-				const int step = TW_STEP * k;
+				const float2* wk = tw + k * (R - 1) - 1;  // this pass's table, [k][r - 1]
 #pragma unroll
 				for (int r = 1; r < R; ++r) {
-					const float2 w = tw[r * step];
+					const float2 w = wk[r];
 					v[r] = INV ? cmulc(v[r], w) : cmul(v[r], w);
 				}
 			}
@@ -124,7 +128,7 @@ namespace ugsdr_gpu {
 			hooked_pass<N, R, NS, INV, FIRST, LAST>(a, b, tw, batch, ld, load, emit);
 			if constexpr (!LAST) {
 				__syncthreads();
-				HookedPasses<N, NS * R, INV, false, Rest...>::run(b, a, tw, batch, ld, load, emit);
+				HookedPasses<N, NS * R, INV, false, Rest...>::run(b, a, tw + pass_table_size<NS, R>(), batch, ld, load, emit);
 			}
 		}
 	};
@@ -132,6 +136,31 @@ namespace ugsdr_gpu {
 	template <int... Rs>
 	constexpr int radix_product() {
 		return (1 * ... * Rs);
+	}
+
+	// Per-pass twiddle tables, pass after pass, entry [k][r - 1] = tw[r k N / (NS R)]
+	// (tw: the N-point table exp(-2 pi i m / N)); a fixed r is a stride-(R - 1)
+	// read across lanes, free of the bank conflicts of tw[r k] itself.
+	template <int N, int NS, int R, int... Rest>
+	__device__ __forceinline__ void build_pass_tables(float2* dst, const float2* __restrict__ tw) {
+		if constexpr (NS > 1) {
+			constexpr int STEP = N / (NS * R);
+			for (int e = threadIdx.x; e < NS * (R - 1); e += blockDim.x) {
+				const int k = e / (R - 1);
+				const int r = e - k * (R - 1) + 1;
+				dst[e] = __ldg(tw + r * k * STEP);
+			}
+		}
+		if constexpr (sizeof...(Rest) > 0)
+			build_pass_tables<N, NS * R, Rest...>(dst + pass_table_size<NS, R>(), tw);
+	}
+
+	template <int NS, int R, int... Rest>
+	constexpr int tables_size() {
+		if constexpr (sizeof...(Rest) > 0)
+			return pass_table_size<NS, R>() + tables_size<NS * R, Rest...>();
+		else
+			return pass_table_size<NS, R>();
 	}
 
 	template <int... Rs>
@@ -150,6 +179,17 @@ namespace ugsdr_gpu {
 		static constexpr bool kHooked = true;  // kernels fuse their producer/consumer into the first/last pass
 		// most butterflies of one pass over `batch` transforms
 		static constexpr int most_butterflies(int batch) { return batch * (N_ / radix_min<Rs...>()); }
+		static_assert(tables_size<1, Rs...>() <= N_, "pass tables fit the N-entry table space");
+		// Builds the pass tables at `dst` (16-byte aligned, room for N entries)
+		// from the plan's N-point table (global memory); returns the plan
+		// pointing at them.  Call before the CTA's first barrier.
+		__device__ static FftPlanDev prepare(const FftPlanDev& plan, void* dst) {
+			float2* t = reinterpret_cast<float2*>((reinterpret_cast<uintptr_t>(dst) + 15) & ~static_cast<uintptr_t>(15));
+			build_pass_tables<N_, 1, Rs...>(t, plan.tw);
+			FftPlanDev out = plan;
+			out.tw = t;
+			return out;
+		}
 		template <bool INV>
 		__device__ static float2* run(float2* a, float2* b, const FftPlanDev& plan, int batch, int ld) {
 			return StaticPasses<N_, 1, INV, Rs...>::run(a, b, plan.tw, batch, ld);
