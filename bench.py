@@ -92,6 +92,16 @@ def gal_small_workload(seed: int = 2):
     return [gal], raw
 
 
+def gps_small_workload(seed: int = 2):
+    """Profiling case for the 50,000-point kernels: the GPS job of the
+    multi-constellation capture cut to 4 codes x 5 Doppler bins (K = 40)."""
+    jobs, raw = multi_workload(seed)
+    gps = dict(jobs[0])
+    gps["codes"] = gps["codes"][:4]
+    gps["step"] = 2500.0
+    return [gps], raw
+
+
 def gps_4mhz_workload(seed: int = 1):
     from ugsdr_gb300 import _lib as L
     from ugsdr_gb300 import api, signals
@@ -118,12 +128,13 @@ def l5_weak_workload(seed: int = 5):
 
 
 WORKLOADS = {"multi": multi_workload, "gps_l1_4mhz": gps_4mhz_workload, "gal_small": gal_small_workload,
-             "l5_weak": l5_weak_workload}
+             "gps_small": gps_small_workload, "l5_weak": l5_weak_workload}
 WORKLOAD_DESC = {
     "multi": "multi-constellation batch: int16 I/Q 50 MHz 40 ms; GPS L1 C/A 32x41x50000x40, "
              "GLONASS L1OF 14ch x41x50000x40, Galileo E1B 36x161x200000x10",
     "gps_l1_4mhz": "GPS L1 C/A int8 4 MHz 10 ms; 32 PRN x 21 Doppler x 4000 x 10",
     "gal_small": "Galileo E1B 4 codes x 5 Doppler x 200000 x 10 (profiling case)",
+    "gps_small": "GPS L1 C/A 4 codes x 5 Doppler x 50000 x 40 (profiling case)",
     "l5_weak": "GPS L5I weak-signal: real int8 IF 40 MHz 200 ms -> 20.46 MHz complex on device; "
                "63 PRN x 401 Doppler x 204600 (10 ms, NH10 wiped) x 20",
 }
@@ -165,6 +176,16 @@ def inverse_flops(j):
     N-point IFFT (5 N log2 N) + conj-multiply and |.| accumulate (10 N)."""
     n = j["n"]
     return len(j["codes"]) * n_doppler(j["step"]) * j["k"] * (5 * n * log2(n) + 10 * n)
+
+
+# DRAM bytes per inverse-transform point of the four-step kernels (inv_rows +
+# inv_cols), measured with ncu on the 200,000- and 50,000-point profiling cases
+# (15.6 and 15.7; the intermediate B buffer is 14.5 of it); see profiles/.
+TRAFFIC_BYTES_PER_INVERSE_POINT = 15.6
+
+
+def inverse_points(j):
+    return len(j["codes"]) * n_doppler(j["step"]) * j["k"] * j["n"]
 
 
 def inverse_bytes(j):
@@ -297,6 +318,9 @@ def run_ours(args, world, rank):
     n_fwd, ms_fwd = ctx.kernel_time(inv_name.replace("inverse", "forward"))
     flops_inv = sum(inverse_flops(j) for j in jobs) * args.steps
     bytes_inv = sum(inverse_bytes(j) for j in jobs) * args.steps
+    large = all(j["n"] > 12000 for j in jobs)  # four-step kernels (the measured traffic applies)
+    traffic = (TRAFFIC_BYTES_PER_INVERSE_POINT * sum(inverse_points(j) for j in jobs) * args.steps / max(n_inv, 1)
+               if large else None)
 
     # end to end through the C ABI with pinned host samples
     e2e_times, _ = timed(host_jobs, max(2, args.steps // 2), False)
@@ -333,7 +357,10 @@ def run_ours(args, world, rank):
                 "ms_per_step": t_e2e * 1e3},
         "gpu_launches": launches,
         "roofline": {"bound": "fp32", "kernel": inv_name, "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
-                     "frac": achieved / fp32_peak if achieved else None, "traffic": None,
+                     "frac": achieved / fp32_peak if achieved else None, "traffic": traffic,
+                     "traffic_source": "ncu dram__bytes_read+write per inverse point (15.6 B, 200k/50k profiling "
+                                       "cases) x points per launch" if traffic else None,
+                     "algorithmic_bytes_per_launch": bytes_inv / max(n_inv, 1),
                      "peak_source": f"{n_sm} SMs x 128 FP32 lanes x 2 x sm_max_mhz {sm_max} (MEASURED_PEAKS.json)",
                      "launches": n_inv, "avg_launch_ms": ms_inv / max(n_inv, 1),
                      "hbm": {"achieved": hbm_ach, "peak": hbm_peak, "unit": "GB/s",
