@@ -25,7 +25,26 @@ namespace ugsdr_gpu {
 		constexpr int kTrackThreads = 256;
 		constexpr int kWinChunk = 8192;   // samples per replica window (a multiple of kTrackThreads)
 		constexpr int kWinPad = 128;      // window margin: taps within +-kWinPad samples of the prompt
-		constexpr int kMaxChunks = 16;    // samples per epoch up to kMaxChunks * kWinChunk
+		constexpr int kMaxChunks = 32;    // chunks per epoch
+		constexpr int kStageBytes = 32768;  // one staged sample chunk (two buffers, double-buffered)
+
+		template <int ST>
+		constexpr int sample_size() {
+			return ST == UGSDR_SAMPLES_CF32 ? 8 : ST == UGSDR_SAMPLES_CI16 ? 4 : ST == UGSDR_SAMPLES_CI8 ? 2 : 1;
+		}
+		// samples per chunk: the window's 8192, or fewer so a chunk fits one stage buffer
+		template <int ST>
+		constexpr int chunk_samples() {
+			return kStageBytes / sample_size<ST>() < kWinChunk ? kStageBytes / sample_size<ST>() : kWinChunk;
+		}
+
+		template <int G>
+		__device__ __forceinline__ void cp_async_g(void* smem, const void* gmem) {
+			const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+			asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(d), "l"(gmem), "n"(G));
+		}
+		__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+		__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 		constexpr double kTwo64 = 18446744073709551616.0;
 		constexpr double kPi = 3.14159265358979323846;
 
@@ -59,6 +78,7 @@ namespace ugsdr_gpu {
 			const float* lut;
 			TrackState* states;
 			TrackOut* out;          // [epoch][channel] or null
+			int stage_g;            // cp.async size (16/8/4) when staged: it divides the epoch and chunk byte offsets and the base alignment
 		};
 
 		__device__ __forceinline__ unsigned long long frac_to_fx(double cycles) {
@@ -112,13 +132,19 @@ namespace ugsdr_gpu {
 			return {static_cast<int>((num / S3) % static_cast<unsigned long long>(len)), static_cast<unsigned int>(num % S3)};
 		}
 
-		template <int ST>
+		template <int ST, bool STAGED>
 		__global__ void __launch_bounds__(kTrackThreads, 2) track_bank_kernel(TrackParams p) {
-			// The epoch is correlated in chunks of kWinChunk samples.  For each chunk
-			// the code replica is written once to s_win, from kWinPad samples before
-			// the prompt's first index; every tap reads it at its own offset (the
+			// The epoch is correlated in chunks of CH samples.  For each chunk the
+			// code replica is written once to s_win, from kWinPad samples before the
+			// prompt's first index; every tap reads it at its own offset (the
 			// replica is periodic in the code period, so a tap across the period
-			// boundary reads the same values).
+			// boundary reads the same values).  STAGED: the chunk's samples are
+			// copied into one of two shared buffers by cp.async while the previous
+			// chunk (or the previous epoch's loop update) runs — the samples do not
+			// depend on the loop state, so the copies run one chunk ahead.
+			constexpr int CH = chunk_samples<ST>();
+			constexpr int SB = sample_size<ST>();
+			extern __shared__ __align__(16) unsigned char s_stage[];  // STAGED: 2 x kStageBytes
 			__shared__ float s_win[kWinChunk + 2 * kWinPad];
 			__shared__ float s_lut[80];
 			__shared__ float s_red[kTrackThreads / 32][20];
@@ -146,11 +172,11 @@ namespace ugsdr_gpu {
 			const unsigned int s3 = static_cast<unsigned int>(S3);
 			const ChipPos tid_pos = chip_of(threadIdx.x, L3, S3, len);
 			const ChipPos step_pos = chip_of(blockDim.x, L3, S3, len);
-			const int n_chunks = (spm + kWinChunk - 1) / kWinChunk;
+			const int n_chunks = (spm + CH - 1) / CH;
 			if (threadIdx.x < n_chunks)
-				s_cpos[threadIdx.x] = chip_of(static_cast<unsigned long long>(threadIdx.x) * kWinChunk, L3, S3, len);
+				s_cpos[threadIdx.x] = chip_of(static_cast<unsigned long long>(threadIdx.x) * CH, L3, S3, len);
 			const double spc = p.fs / st->base;
-			const double base_freq = st->base, dll_scale = st->base / 1.023e6;
+			const double base_freq = st->base, inv_base = 1.0 / st->base, dll_scale = st->base / 1.023e6;
 			const int lane = threadIdx.x & 31;
 			const bool warp0 = threadIdx.x < 32;
 
@@ -208,6 +234,30 @@ namespace ugsdr_gpu {
 					nco_setup();
 				tap_setup();
 			}
+			// copy of global chunk gi = epoch * n_chunks + chunk into stage buffer gi & 1
+			const int total_chunks = p.n_epochs * n_chunks;
+			auto stage = [&](int gi) {
+				const int e = gi / n_chunks;
+				const int c = (gi - e * n_chunks) * CH;
+				const int bytes = min(CH, spm - c) * SB;
+				const char* src = static_cast<const char*>(p.samples) + (static_cast<size_t>(e) * spm + c) * SB;
+				unsigned char* dst = s_stage + (gi & 1) * kStageBytes;
+				if (p.stage_g == 16) {
+					for (int o = threadIdx.x * 16; o < bytes; o += blockDim.x * 16)
+						cp_async_g<16>(dst + o, src + o);
+				}
+				else if (p.stage_g == 8) {
+					for (int o = threadIdx.x * 8; o < bytes; o += blockDim.x * 8)
+						cp_async_g<8>(dst + o, src + o);
+				}
+				else {
+					for (int o = threadIdx.x * 4; o < bytes; o += blockDim.x * 4)
+						cp_async_g<4>(dst + o, src + o);
+				}
+				cp_async_commit();
+			};
+			if constexpr (STAGED)
+				stage(0);
 			__syncthreads();
 
 			for (int ep = 0; ep < p.n_epochs; ++ep) {
@@ -228,22 +278,33 @@ namespace ugsdr_gpu {
 				const bool mix = s_mix;
 				const size_t base = static_cast<size_t>(ep) * spm;
 				for (int k = 0; k < n_chunks; ++k) {
-					const int c0 = k * kWinChunk;
-					const int n_c = min(kWinChunk, spm - c0);
+					const int c0 = k * CH;
+					const int n_c = min(CH, spm - c0);
+					const int gi = ep * n_chunks + k;
+					const void* stage_buf = s_stage + (gi & 1) * kStageBytes;
 					// replica window of this chunk: entries j < n_c + 2 kWinPad
 					ChipPos pos = chip_add(chip_add(wpos, s_cpos[k], s3, len), tid_pos, s3, len);
 					for (int j = threadIdx.x; j < n_c + 2 * kWinPad; j += blockDim.x) {
 						s_win[j] = __ldg(chips + pos.chip);
 						pos = chip_add(pos, step_pos, s3, len);
 					}
+					if constexpr (STAGED)
+						cp_async_wait_all();  // this chunk's samples (issued one chunk earlier)
 					__syncthreads();
+					if constexpr (STAGED) {
+						if (gi + 1 < total_chunks)
+							stage(gi + 1);  // its buffer was last read by chunk gi - 1, before the barrier
+					}
 					// correlate: four samples in flight per thread
 					for (int i0 = threadIdx.x; i0 < n_c; i0 += 4 * kTrackThreads) {
 						float2 xs[4];
 #pragma unroll
 						for (int u = 0; u < 4; ++u) {
 							const int i = i0 + u * kTrackThreads;
-							xs[u] = i < n_c ? load_sample<ST>(p.samples, base + c0 + i) : c2(0.f, 0.f);
+							if constexpr (STAGED)
+								xs[u] = i < n_c ? load_sample<ST>(stage_buf, i) : c2(0.f, 0.f);
+							else
+								xs[u] = i < n_c ? load_sample<ST>(p.samples, base + c0 + i) : c2(0.f, 0.f);
 						}
 #pragma unroll
 						for (int u = 0; u < 4; ++u) {
@@ -342,7 +403,7 @@ namespace ugsdr_gpu {
 						const double err = static_cast<double>(part) / (kPi * 2.0);
 						const double ferr = static_cast<double>(ferr_f) / kPi;
 						// UpdatePhase (tracking_parameters.hpp:163-165) with the pre-update frequency
-						ls.phase_fx += frac_to_fx(ls.carrier_freq / 1000.0);
+						ls.phase_fx += frac_to_fx(ls.carrier_freq * 1e-3);
 						// Pll(prompt) (tracking_parameters.hpp:495-511), loop filter in FP64
 						ls.carrier_freq += p.k1_pll * err - p.k2_pll * ls.carrier_phase_error - p.k3_pll * ferr;
 						ls.carrier_phase_error = err;
@@ -356,7 +417,7 @@ namespace ugsdr_gpu {
 						ls.code_nco += (p.k1_dll * (ce - ls.code_error) + p.k2_dll * ce) * dll_scale;
 						ls.code_error = ce;
 						ls.code_freq = base_freq - ls.code_nco;
-						ls.code_phase -= p.fs / 1000 / 2 * (ls.code_freq / base_freq - 1);
+						ls.code_phase -= p.fs / 1000 / 2 * (ls.code_freq * inv_base - 1);
 						if (p.out) {
 							TrackOut o;
 							for (int t = 0; t < 5; ++t) {
@@ -443,20 +504,40 @@ namespace {
 		p.lut = get_lut(ctx);
 		p.states = bank->states.as<TrackState>();
 		p.out = dev_out;
-		const size_t smem = 0;
+		// stage the samples through shared memory when a 16/8/4-byte cp.async
+		// divides the epoch size and the base address (chunks are 32 KiB or 8192
+		// samples, multiples of 16 bytes)
+		const uintptr_t addr = reinterpret_cast<uintptr_t>(dev);
+		p.stage_g = 0;
+		for (int g : {16, 8, 4})
+			if ((per * bank->spm) % g == 0 && addr % g == 0) {
+				p.stage_g = g;
+				break;
+			}
+		const dim3 grid(bank->n_channels), block(kTrackThreads);
+		const size_t smem = p.stage_g ? 2 * kStageBytes : 0;
 		KernelTimer timer(ctx, "track_bank");
+		auto launch = [&](auto staged_kernel, auto direct_kernel) {
+			if (p.stage_g) {
+				UG_CUDA(cudaFuncSetAttribute(staged_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+				staged_kernel<<<grid, block, smem, ctx->stream>>>(p);
+			}
+			else {
+				direct_kernel<<<grid, block, 0, ctx->stream>>>(p);
+			}
+		};
 		switch (sample_type) {
 		case UGSDR_SAMPLES_CF32:
-			track_bank_kernel<UGSDR_SAMPLES_CF32><<<bank->n_channels, kTrackThreads, smem, ctx->stream>>>(p);
+			launch(track_bank_kernel<UGSDR_SAMPLES_CF32, true>, track_bank_kernel<UGSDR_SAMPLES_CF32, false>);
 			break;
 		case UGSDR_SAMPLES_CI8:
-			track_bank_kernel<UGSDR_SAMPLES_CI8><<<bank->n_channels, kTrackThreads, smem, ctx->stream>>>(p);
+			launch(track_bank_kernel<UGSDR_SAMPLES_CI8, true>, track_bank_kernel<UGSDR_SAMPLES_CI8, false>);
 			break;
 		case UGSDR_SAMPLES_CI16:
-			track_bank_kernel<UGSDR_SAMPLES_CI16><<<bank->n_channels, kTrackThreads, smem, ctx->stream>>>(p);
+			launch(track_bank_kernel<UGSDR_SAMPLES_CI16, true>, track_bank_kernel<UGSDR_SAMPLES_CI16, false>);
 			break;
 		default:
-			track_bank_kernel<UGSDR_SAMPLES_RI8><<<bank->n_channels, kTrackThreads, smem, ctx->stream>>>(p);
+			launch(track_bank_kernel<UGSDR_SAMPLES_RI8, true>, track_bank_kernel<UGSDR_SAMPLES_RI8, false>);
 			break;
 		}
 		note_launch(ctx);
@@ -482,7 +563,7 @@ int ugsdr_track_create(ugsdr_ctx* ctx, const ugsdr_track_config* cfg, const ugsd
 		b->fs = channels[0].sampling_rate;
 		require(b->fs > 0 && std::fmod(b->fs, 1e3) == 0.0, "sampling rate must be a whole number of kHz");
 		b->spm = static_cast<size_t>(b->fs / 1e3);
-		require(b->spm >= 2 * kWinPad && b->spm <= static_cast<size_t>(kMaxChunks) * kWinChunk,
+		require(b->spm >= 2 * kWinPad && b->spm <= static_cast<size_t>(kMaxChunks) * (kStageBytes / 8),
 			"sampling rate must be between 256 kHz and 131.072 MHz");
 		const double el = cfg->early_late_spacing, vel = cfg->very_early_late_spacing;
 		const double offs[5] = {vel, el, 0.0, -el, -vel};
