@@ -284,7 +284,25 @@ namespace ugsdr_gpu {
 					const void* stage_buf = s_stage + (gi & 1) * kStageBytes;
 					// replica window of this chunk: entries j < n_c + 2 kWinPad
 					ChipPos pos = chip_add(chip_add(wpos, s_cpos[k], s3, len), tid_pos, s3, len);
-					for (int j = threadIdx.x; j < n_c + 2 * kWinPad; j += blockDim.x) {
+					const int n_win = n_c + 2 * kWinPad;
+					int j = threadIdx.x;
+					// eight chip-table loads in flight per thread: positions first, then loads
+					for (; j + 7 * static_cast<int>(blockDim.x) < n_win; j += 8 * blockDim.x) {
+						int cj[8];
+#pragma unroll
+						for (int u = 0; u < 8; ++u) {
+							cj[u] = pos.chip;
+							pos = chip_add(pos, step_pos, s3, len);
+						}
+						float vj[8];
+#pragma unroll
+						for (int u = 0; u < 8; ++u)
+							vj[u] = __ldg(chips + cj[u]);
+#pragma unroll
+						for (int u = 0; u < 8; ++u)
+							s_win[j + u * blockDim.x] = vj[u];
+					}
+					for (; j < n_win; j += blockDim.x) {
 						s_win[j] = __ldg(chips + pos.chip);
 						pos = chip_add(pos, step_pos, s3, len);
 					}
