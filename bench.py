@@ -447,12 +447,13 @@ def run_served(args):
         cells.append(len(hs) * n_doppler(r["step"]) * n)
 
     # served: Poisson arrivals into the continuous-batching server
-    srv = api.Server(ctx, max_inflight=args.inflight)
+    policy = {"fifo": L.SERVE_FIFO, "response_ratio": L.SERVE_RESPONSE_RATIO}[args.policy]
+    srv = api.Server(ctx, max_inflight=args.inflight, policy=policy)
     warm = srv.submit(jobs[0])
     srv.drain()
     srv.poll(warm)
     t0 = time.perf_counter()
-    tickets, done_at = [], {}
+    tickets, done_at, failures = [], {}, []
     i = 0
     while len(done_at) < len(jobs):
         now = time.perf_counter() - t0
@@ -460,7 +461,14 @@ def run_served(args):
             tickets.append(srv.submit(jobs[i]))
             i += 1
         for k, t in enumerate(tickets):
-            if k not in done_at and srv.poll(t) is not None:
+            if k in done_at:
+                continue
+            try:
+                finished = srv.poll(t) is not None
+            except L.UgsdrError as e:  # a failed request still completes (with its error)
+                failures.append({"request": k, "error": str(e)})
+                finished = True
+            if finished:
                 done_at[k] = time.perf_counter() - t0
         time.sleep(0.0002)
     t_total = max(done_at.values()) - reqs[0]["arrival"]
@@ -504,11 +512,15 @@ def run_served(args):
         "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
         "offered_rate_req_s": args.rate, "wall_s": t_total, "max_inflight_seen": stats["max_inflight_seen"],
         "offered_load": args.rate * float(np.mean(cells)) / (sum(cells) / t_seq),
+        "failed_requests": failures,
+        "per_request": [{"arrival_ms": round(reqs[k]["arrival"] * 1e3, 2), "cell_blocks": int(cells[k] * reqs[k]["k"]),
+                         "latency_ms": round(float(lat[k]), 1)} for k in range(len(jobs))],
         "sequential_cells_s": sum(cells) / t_seq, "plain_cells_s": plain, "served_over_plain": served / plain,
         "served_over_sequential": served / (sum(cells) / t_seq),
         "plain_sample": f"{rows} (code, Doppler) rows of a {n}-sample x {req['k']}-block request, per-op entries",
         "config": {"workload": f"served stream: Poisson {args.rate:g} req/s, fs {{2.046,4,10.23,20.46,50}} MHz, Tcoh 1-20 ms, "
                                "K 1-40, 1-63 codes of L1 C/A / L5I / E1B, int8/int16", "inflight": args.inflight,
+                   "policy": args.policy,
                    "cells_total": int(sum(cells))},
     }
 
@@ -829,6 +841,8 @@ def main():
     ap.add_argument("--requests", type=int, default=24, help="requests in the served stream")
     ap.add_argument("--inflight", type=int, default=4, help="server slots for the served stream")
     ap.add_argument("--rate", type=float, default=2000.0, help="Poisson arrival rate of the served stream (req/s)")
+    ap.add_argument("--policy", choices=["fifo", "response_ratio"], default="response_ratio",
+                    help="server admission order for the served stream")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", 1))
     rank = int(os.environ.get("RANK", 0))

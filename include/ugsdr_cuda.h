@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define UGSDR_CUDA_ABI_VERSION 2
+#define UGSDR_CUDA_ABI_VERSION 3
 
 enum ugsdr_status {
 	UGSDR_OK = 0,
@@ -345,10 +345,23 @@ int ugsdr_track_destroy(ugsdr_track_bank* bank);
  * keep arriving.  Code spectra (ugsdr_code_put handles) stay resident across
  * requests; do not release a handle that a pending job uses. */
 typedef struct ugsdr_server ugsdr_server;
+/* Admission order of pending requests. */
+enum ugsdr_serve_policy {
+	UGSDR_SERVE_FIFO = 0,       /* oldest first */
+	/* highest response ratio next: (wait + estimated service) / estimated
+	 * service, the service estimated from the request's cell-blocks (codes x
+	 * Doppler bins x block samples x blocks) and the server's measured
+	 * throughput — short searches go first, long ones age to the front; a
+	 * search estimated below 0.5 s runs on its slot's highest-priority CUDA
+	 * stream, so its blocks are dispatched ahead of running long searches */
+	UGSDR_SERVE_RESPONSE_RATIO = 1
+};
+
 typedef struct ugsdr_server_config {
 	int max_inflight;          /* concurrent jobs on the device (0 = 4) */
 	size_t memory_budget;      /* device bytes the slots' scratch may hold (0 = 80 % of free memory) */
 	int queue_capacity;        /* pending requests before UGSDR_E_QUEUE_FULL (0 = 1024) */
+	int policy;                /* ugsdr_serve_policy */
 } ugsdr_server_config;
 
 typedef struct ugsdr_server_stats {

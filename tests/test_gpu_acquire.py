@@ -242,3 +242,25 @@ def test_doppler_chunking_same_results(ctx, acq_golden, golden_codes, monkeypatc
     finally:
         for h in hs + hl:
             ctx.code_release(h)
+
+
+def test_large_368280_runtime_plan(ctx, oracle, golden_codes):
+    """GPS L1 at 20.46 MHz, 18 ms coherent: N = 368,280 = 594 x 620 runs the
+    runtime-planned four-step kernels, and its scratch regions are not
+    multiples of 256 bytes (the layout must round every region the same way
+    when sizing and when carving)."""
+    ca = unpack_codes(golden_codes, "gps_l1ca")
+    em = signals.Emitter(ca[2], 1.023e6, 321.5, 300.0, 50.0, data_rate=0.0)
+    raw = signals.synthesize([em], 20.46e6, 368280, 20.0, "ci16", seed=15)
+    x = to_complex(raw)
+    res, _ = run_engine(ctx, raw, 20.46e6, 368280, 1, [ca[2]], 18, 300, 300)
+    code = oracle.upsample(np.tile(ca[2], 18), 368280)
+    o32 = oracle.acquire(x, 368280, 1, code, 20.46e6, 300, 300)
+    o64 = oracle.acquire(x, 368280, 1, code, 20.46e6, 300, 300, double=True)
+    # 18 repetitions of a 1 ms code without data: 18 equal peaks, one per
+    # period, so rounding may pick any of them; the peak is exact modulo 1 ms
+    r = res[0]
+    assert r.index % 20460 == int(o32["index"]) % 20460 and r.doppler_bin == int(o32["doppler_bin"])
+    for f in ("level", "mean", "std", "snr", "sigma"):
+        assert abs(getattr(r, f) - o64[f]) <= RTOL * abs(o64[f]), (f, getattr(r, f), o64[f])
+    assert abs(r.index % 20460 - 321.5 * 20) <= 2

@@ -80,3 +80,39 @@ def test_queue_full_and_budget(ctx, golden_codes):
         for hs in handles:
             for h in hs:
                 ctx.code_release(h)
+
+
+@pytest.mark.parametrize("policy", [L.SERVE_FIFO, L.SERVE_RESPONSE_RATIO])
+def test_admission_order(ctx, golden_codes, policy):
+    """One slot: while a long search runs, a long and a short one queue.  FIFO
+    admits them in arrival order; the response-ratio policy admits the short
+    one first (its (wait + service) / service is larger)."""
+    ca = unpack_codes(golden_codes, "gps_l1ca")
+    raw, _ = signals.gps_l1_config(seed=77, codes={p: ca[p] for p in range(8)}, fs=50e6, ms=8, visible=2,
+                                   sample_type="ci16")
+    long_h = [ctx.code_put(ca[p], 50000) for p in range(24)]
+    short_h = [ctx.code_put(ca[0], 50000)]
+    try:
+        long_job = ctx.make_job(raw, L.SAMPLES_CI16, 50e6, 50000, 8, long_h, 5000.0, 250.0)
+        short_job = ctx.make_job(raw, L.SAMPLES_CI16, 50e6, 50000, 1, short_h, 500.0, 500.0)
+        srv = Server(ctx, max_inflight=1, policy=policy)
+        first = srv.submit(long_job)
+        time.sleep(0.002)
+        t_long = srv.submit(long_job)
+        t_short = srv.submit(short_job)
+        done = {}
+        t0 = time.perf_counter()
+        while len(done) < 3 and time.perf_counter() - t0 < 120:
+            for t in (first, t_long, t_short):
+                if t not in done and srv.poll(t) is not None:
+                    done[t] = time.perf_counter()
+            time.sleep(0.0005)
+        srv.close()
+        assert len(done) == 3
+        if policy == L.SERVE_FIFO:
+            assert done[t_long] < done[t_short]
+        else:
+            assert done[t_short] < done[t_long]
+    finally:
+        for h in long_h + short_h:
+            ctx.code_release(h)

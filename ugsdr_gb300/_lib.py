@@ -10,7 +10,7 @@ from pathlib import Path
 
 LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libugsdr_cuda.so"
 
-ABI_VERSION = 2  # UGSDR_CUDA_ABI_VERSION the structs below mirror
+ABI_VERSION = 3  # UGSDR_CUDA_ABI_VERSION the structs below mirror
 
 OK = 0
 E_INVALID = -1
@@ -107,8 +107,12 @@ class TrackOutput(C.Structure):
     ]
 
 
+SERVE_FIFO, SERVE_RESPONSE_RATIO = 0, 1
+
+
 class ServerConfig(C.Structure):
-    _fields_ = [("max_inflight", C.c_int), ("memory_budget", C.c_size_t), ("queue_capacity", C.c_int)]
+    _fields_ = [("max_inflight", C.c_int), ("memory_budget", C.c_size_t), ("queue_capacity", C.c_int),
+                ("policy", C.c_int)]
 
 
 # exported symbols and their signatures (restype, argtypes)

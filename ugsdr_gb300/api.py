@@ -342,9 +342,10 @@ class TrackBank:
 class Server:
     """Continuous-batching acquisition server (ugsdr_server_*)."""
 
-    def __init__(self, ctx: Context, max_inflight: int = 4, memory_budget: int = 0, queue_capacity: int = 1024):
+    def __init__(self, ctx: Context, max_inflight: int = 4, memory_budget: int = 0, queue_capacity: int = 1024,
+                 policy: int = L.SERVE_FIFO):
         self.ctx = ctx
-        cfg = L.ServerConfig(max_inflight, memory_budget, queue_capacity)
+        cfg = L.ServerConfig(max_inflight, memory_budget, queue_capacity, policy)
         h = C.c_void_p()
         ctx._check(ctx.lib.ugsdr_server_create(ctx.h, C.byref(cfg), C.byref(h)))
         self.h = h

@@ -210,10 +210,12 @@ namespace ugsdr_gpu {
 
 		int chunks_of(int total, int per) { return (total + per - 1) / per; }
 
-		// rows per inverse batch: B (rows x K x N complex) within the budget
+		// rows per inverse batch: B (rows x K x N complex) within 8 GiB — large
+		// enough that a batch is thousands of CTAs and a search a few hundred
+		// launches at most (the host then never waits on a full launch queue)
 		int batch_rows(const JobLaunchShape& s) {
 			const size_t per_row = sizeof(float2) * static_cast<size_t>(s.n) * s.k;
-			const size_t budget = static_cast<size_t>(512) << 20;
+			const size_t budget = static_cast<size_t>(8) << 30;
 			return static_cast<int>(std::max<size_t>(1, std::min<size_t>(s.rows, budget / per_row)));
 		}
 
@@ -243,21 +245,37 @@ namespace ugsdr_gpu {
 		}
 	}
 
+	namespace {
+		// Scratch layout of one large-path launch (B, partials, sums, counters,
+		// fold buffers), each region 256-byte aligned; sizing and carving both
+		// walk it, so they agree byte for byte.
+		struct ScratchLayout {
+			size_t bbuf = 0, partials = 0, sums = 0, counters = 0, accg = 0, zcg = 0, total = 0;
+			ScratchLayout(const JobLaunchShape& s, int r_max, int chunks) {
+				auto region = [&](size_t bytes) {
+					const size_t at = total;
+					total += (bytes + 255) / 256 * 256;
+					return at;
+				};
+				const size_t r = static_cast<size_t>(r_max);
+				bbuf = region(sizeof(float2) * r * s.k * s.n);
+				partials = region(sizeof(float4) * r * chunks);
+				sums = region(sizeof(double2) * r * chunks);
+				counters = region(sizeof(unsigned int) * r);
+				if (s.fold_mode) {
+					accg = region(sizeof(float) * r * s.m);
+					if (s.fold_mode == 2)
+						zcg = region(sizeof(float2) * r * s.k * s.m);
+				}
+			}
+		};
+	}
+
 	size_t batched_scratch_bytes(ugsdr_ctx* ctx, const JobLaunchShape& s) {
 		AcqParams base{};
 		base.n = s.n;
 		const BatchedParams p = batched_params(ctx, base, s.n);
-		const size_t r = batch_rows(s);
-		const size_t chunks = chunks_of(p.n2, p.cw);
-		size_t bytes = sizeof(float2) * r * s.k * s.n;                     // B
-		bytes += (sizeof(float4) + sizeof(double2)) * r * chunks + 256;   // partials, sums
-		bytes += sizeof(unsigned int) * r + 256;                          // counters
-		if (s.fold_mode) {
-			bytes += sizeof(float) * r * s.m + 256;                       // accg
-			if (s.fold_mode == 2)
-				bytes += sizeof(float2) * r * s.k * s.m + 256;            // zcg
-		}
-		return bytes;
+		return ScratchLayout(s, batch_rows(s), chunks_of(p.n2, p.cw)).total;
 	}
 
 	void large_code_spectrum(ugsdr_ctx* ctx, CodeEntry& e, const float* chips_dev, size_t n_chips, size_t repeats,
@@ -293,20 +311,15 @@ namespace ugsdr_gpu {
 		}
 		const int r_max = batch_rows(s);
 		const int chunks = chunks_of(p.n2, p.cw);
-		char* at = scratch;
-		auto carve = [&](size_t bytes) {
-			char* q = at;
-			at += (bytes + 255) / 256 * 256;
-			return q;
-		};
-		p.bbuf = reinterpret_cast<float2*>(carve(sizeof(float2) * static_cast<size_t>(r_max) * s.k * s.n));
-		p.partials = reinterpret_cast<float4*>(carve(sizeof(float4) * static_cast<size_t>(r_max) * chunks));
-		p.sums = reinterpret_cast<double2*>(carve(sizeof(double2) * static_cast<size_t>(r_max) * chunks));
-		p.counters = reinterpret_cast<unsigned int*>(carve(sizeof(unsigned int) * r_max));
+		const ScratchLayout lay(s, r_max, chunks);
+		p.bbuf = reinterpret_cast<float2*>(scratch + lay.bbuf);
+		p.partials = reinterpret_cast<float4*>(scratch + lay.partials);
+		p.sums = reinterpret_cast<double2*>(scratch + lay.sums);
+		p.counters = reinterpret_cast<unsigned int*>(scratch + lay.counters);
 		if (s.fold_mode) {
-			p.accg = reinterpret_cast<float*>(carve(sizeof(float) * static_cast<size_t>(r_max) * s.m));
+			p.accg = reinterpret_cast<float*>(scratch + lay.accg);
 			if (s.fold_mode == 2)
-				p.zcg = reinterpret_cast<float2*>(carve(sizeof(float2) * static_cast<size_t>(r_max) * s.k * s.m));
+				p.zcg = reinterpret_cast<float2*>(scratch + lay.zcg);
 		}
 		const size_t smem_r = smem_rows(p, true), smem_c = smem_cols(p, true);
 		with_large_ffts(p.n1, p.n2, [&](auto f1, auto f2) {

@@ -1,17 +1,24 @@
 // Continuous-batching acquisition server (ugsdr_server_*).
 //
-// A worker thread owns `max_inflight` slots, each a CUDA stream with its own
-// scratch workspace and pinned host staging.  Requests queue on submit; the
-// worker admits the oldest pending request whenever a slot is free and the
-// request's device-memory estimate fits the budget (releasing idle slots'
-// scratch first if needed), enqueues it asynchronously on the slot's stream,
-// and retires slots whose completion event fired.  Admitted jobs therefore
-// overlap on the device while new requests keep arriving.  Code spectra are
-// the context's resident cache, shared by every request.
+// `max_inflight` slots, each with two CUDA streams (normal and highest
+// priority), its own scratch workspace and pinned host staging.  Requests
+// queue on submit.  The admission thread picks a pending request (the oldest,
+// or under the response-ratio policy the one with the largest
+// (wait + service) / service), reserves a free slot if the request's
+// device-memory estimate fits the budget (releasing idle slots' scratch first
+// if needed), and launches it on the slot's stream — short searches on the
+// high-priority one — with the server lock released.  The retirement thread
+// polls the slots' completion events and turns finished cells into results.
+// Admitted searches therefore overlap on the device while new requests keep
+// arriving, and completions are seen while long searches are still being
+// launched.  Code spectra are the context's resident cache, shared by every
+// request.
 #include "internal.hpp"
 
 #include <chrono>
 #include <condition_variable>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
 #include <list>
@@ -20,6 +27,9 @@
 using namespace ugsdr_gpu;
 
 namespace {
+	// estimated service below which a search runs on a slot's high-priority stream
+	constexpr double kUrgentSeconds = 0.5;
+
 	// Pinned host staging that grows without freeing while the server runs
 	// (cudaFreeHost waits for the device); outgrown buffers are freed at exit.
 	struct PinnedBuf {
@@ -53,7 +63,9 @@ namespace {
 		ugsdr_acq_job job{};
 		std::vector<int> codes;
 		std::vector<char> samples;  // host copy (empty for device-resident samples)
-		size_t estimate = 0;
+		size_t estimate = 0;   // device bytes
+		double work = 0;       // cell-blocks: codes x Doppler bins x N x K
+		std::chrono::steady_clock::time_point queued;
 		std::vector<ugsdr_acq_result> results;
 		bool done = false;
 		int status = UGSDR_OK;
@@ -61,11 +73,14 @@ namespace {
 	};
 
 	struct Slot {
-		cudaStream_t stream = nullptr;
+		cudaStream_t stream = nullptr;   // normal priority
+		cudaStream_t urgent = nullptr;   // highest priority (short searches under the response-ratio policy)
+		cudaStream_t active = nullptr;   // the one the current job runs on
 		cudaEvent_t event = nullptr;
 		Workspace ws;
 		PinnedBuf samples, cells;
 		Request* req = nullptr;
+		bool enqueuing = false;  // the worker is launching req's work (server lock released)
 		EnqueuedBatch batch;
 	};
 
@@ -87,12 +102,40 @@ struct ugsdr_server {
 	std::map<uint64_t, std::unique_ptr<Request>> requests;
 	uint64_t next_ticket = 1;
 	std::mutex mu;
-	std::condition_variable cv_work, cv_done;
-	std::thread worker;
+	std::condition_variable cv_work, cv_done, cv_reap;
+	std::thread worker, reaper;
 	bool stop = false;
 	size_t budget = 0;
 	ugsdr_server_stats stats{};
 	std::chrono::steady_clock::time_point busy_since;
+	double done_work = 0;  // cell-blocks completed (throughput estimate with stats.busy_seconds)
+	// UGSDR_SERVER_TRACE=1: one stderr line per admission and retirement (times in ms since creation)
+	bool trace = std::getenv("UGSDR_SERVER_TRACE") != nullptr;
+	std::chrono::steady_clock::time_point created = std::chrono::steady_clock::now();
+	double since() const { return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - created).count(); }
+
+	// measured cell-blocks per second (a first guess until work has completed)
+	double rate() const { return stats.busy_seconds > 0.05 && done_work > 0 ? done_work / stats.busy_seconds : 5e10; }
+
+	// the pending request to admit next under cfg.policy
+	std::deque<Request*>::iterator pick() {
+		if (cfg.policy != UGSDR_SERVE_RESPONSE_RATIO || pending.size() < 2)
+			return pending.begin();
+		const double rate = this->rate();
+		const auto now = std::chrono::steady_clock::now();
+		auto best = pending.begin();
+		double best_ratio = -1;
+		for (auto it = pending.begin(); it != pending.end(); ++it) {
+			const double service = std::max((*it)->work / rate, 1e-4);
+			const double wait = std::chrono::duration<double>(now - (*it)->queued).count();
+			const double ratio = (wait + service) / service;
+			if (ratio > best_ratio) {  // ties keep arrival order
+				best_ratio = ratio;
+				best = it;
+			}
+		}
+		return best;
+	}
 
 	size_t held() const {
 		size_t s = 0;
@@ -113,7 +156,7 @@ struct ugsdr_server {
 	bool retire() {
 		bool any = false;
 		for (auto& sl : slots) {
-			if (!sl.req)
+			if (!sl.req || sl.enqueuing)
 				continue;
 			const cudaError_t q = cudaEventQuery(sl.event);
 			if (q == cudaErrorNotReady)
@@ -133,6 +176,9 @@ struct ugsdr_server {
 			ugsdr_acq_result* rp = r->results.data();
 			finish_jobs(sl.batch, &r->job, 1, sl.cells.ptr, &rp, nullptr);
 			r->done = true;
+			done_work += r->work;
+			if (trace)
+				std::fprintf(stderr, "[serve] %.1f retire ticket %llu\n", since(), static_cast<unsigned long long>(r->ticket));
 			++stats.completed;
 			cv_done.notify_all();
 		}
@@ -140,7 +186,10 @@ struct ugsdr_server {
 	}
 
 	// admit the oldest pending request if a slot and memory allow; true if admitted
-	bool admit() {
+	// Admits one request if a slot and memory allow; true if one was admitted
+	// (or failed).  The launches run with the server lock released: polls,
+	// submissions and retirement proceed while a long search is enqueued.
+	bool admit(std::unique_lock<std::mutex>& lock) {
 		if (pending.empty())
 			return false;
 		Slot* free_slot = nullptr;
@@ -151,7 +200,8 @@ struct ugsdr_server {
 			}
 		if (!free_slot)
 			return false;
-		Request* r = pending.front();
+		const auto pos = pick();
+		Request* r = *pos;
 		const size_t grow = r->estimate > free_slot->ws.reserved() ? r->estimate - free_slot->ws.reserved() : 0;
 		if (held() + grow > budget) {
 			// give back scratch of idle slots before waiting
@@ -160,14 +210,26 @@ struct ugsdr_server {
 					sl.ws.release();
 			if (held() + grow > budget) {
 				if (stats.inflight == 0) {
-					pending.pop_front();
+					pending.erase(pos);
 					fail(r, UGSDR_E_NOMEM, "job needs " + std::to_string(r->estimate) + " device bytes, budget " + std::to_string(budget));
 					return true;
 				}
 				return false;  // wait for running jobs to finish
 			}
 		}
-		pending.pop_front();
+		pending.erase(pos);
+		const double t_admit = trace ? since() : 0.0;
+		// reserve the slot, then launch without the server lock
+		free_slot->req = r;
+		free_slot->enqueuing = true;
+		if (stats.inflight == 0)
+			busy_since = std::chrono::steady_clock::now();
+		++stats.inflight;
+		stats.max_inflight_seen = std::max(stats.max_inflight_seen, stats.inflight);
+		const bool urgent = cfg.policy == UGSDR_SERVE_RESPONSE_RATIO && r->work / rate() < kUrgentSeconds;
+		lock.unlock();
+		int fail_status = UGSDR_OK;
+		std::string fail_msg;
 		try {
 			ugsdr_acq_job job = r->job;
 			job.codes = r->codes.data();
@@ -178,43 +240,70 @@ struct ugsdr_server {
 			}
 			size_t n_cells = 0;
 			{
-				std::lock_guard<std::mutex> lock(ctx->mutex);
+				std::lock_guard<std::mutex> ctx_lock(ctx->mutex);
 				// cells: one record per (code, Doppler bin)
 				n_cells = static_cast<size_t>(job.n_codes) * doppler_grid(job.doppler_range, job.doppler_step).size();
 				free_slot->cells.reserve(16 * std::max<size_t>(n_cells, 1));
-				free_slot->batch = enqueue_jobs(ctx, free_slot->ws, free_slot->stream, &job, 1, free_slot->cells.ptr);
-				UG_CUDA(cudaEventRecord(free_slot->event, free_slot->stream));
+				// short searches run on the high-priority stream: the device
+				// dispatches their CTAs ahead of the long jobs' (kUrgentSeconds of
+				// estimated service); the slot's scratch follows the stream
+				free_slot->active = urgent ? free_slot->urgent : free_slot->stream;
+				free_slot->ws.set_stream(free_slot->active);
+				free_slot->batch = enqueue_jobs(ctx, free_slot->ws, free_slot->active, &job, 1, free_slot->cells.ptr);
+				UG_CUDA(cudaEventRecord(free_slot->event, free_slot->active));
+				if (trace)
+					std::fprintf(stderr, "[serve] %.1f admit ticket %llu work %.3g urgent %d enqueue %.1f ms\n", t_admit,
+						static_cast<unsigned long long>(r->ticket), r->work, urgent ? 1 : 0, since() - t_admit);
 			}
 			r->job.codes = r->codes.data();
-			free_slot->req = r;
-			if (stats.inflight == 0)
-				busy_since = std::chrono::steady_clock::now();
-			++stats.inflight;
-			stats.max_inflight_seen = std::max(stats.max_inflight_seen, stats.inflight);
 		}
 		catch (const Error& e) {
-			fail(r, e.status, e.what());
+			fail_status = e.status;
+			fail_msg = e.what();
 		}
 		catch (const std::exception& e) {
-			fail(r, UGSDR_E_INVALID, e.what());
+			fail_status = UGSDR_E_INVALID;
+			fail_msg = e.what();
+		}
+		lock.lock();
+		free_slot->enqueuing = false;
+		if (fail_status != UGSDR_OK) {
+			free_slot->req = nullptr;
+			if (--stats.inflight == 0)
+				stats.busy_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - busy_since).count();
+			fail(r, fail_status, fail_msg);
 		}
 		return true;
 	}
 
+	// Admission thread: admits and launches while a slot and memory allow,
+	// otherwise sleeps until a submission or a retirement.
 	void run() {
 		cudaSetDevice(ctx->device);
 		std::unique_lock<std::mutex> lock(mu);
 		while (!stop) {
-			bool progress = retire();
-			while (admit())
+			bool progress = false;
+			while (!stop && admit(lock))
 				progress = true;
 			stats.device_bytes = held();
-			if (!progress) {
-				if (stats.inflight > 0)
-					cv_work.wait_for(lock, std::chrono::microseconds(50));
-				else
-					cv_work.wait(lock, [&] { return stop || !pending.empty(); });
-			}
+			if (!progress)
+				cv_work.wait_for(lock, std::chrono::milliseconds(5));
+		}
+	}
+
+	// Retirement thread: polls the slots' completion events (every 50 us while
+	// work is in flight), so completions are seen while the admission thread
+	// is still launching a long search.
+	void reap() {
+		cudaSetDevice(ctx->device);
+		std::unique_lock<std::mutex> lock(mu);
+		while (!stop) {
+			if (retire())
+				cv_work.notify_all();
+			if (stats.inflight > 0)
+				cv_reap.wait_for(lock, std::chrono::microseconds(50));
+			else
+				cv_reap.wait_for(lock, std::chrono::milliseconds(5));
 		}
 	}
 };
@@ -234,6 +323,7 @@ int ugsdr_server_create(ugsdr_ctx* ctx, const ugsdr_server_config* cfg, ugsdr_se
 			s->cfg.max_inflight = 4;
 		if (s->cfg.queue_capacity <= 0)
 			s->cfg.queue_capacity = 1024;
+		require(s->cfg.policy == UGSDR_SERVE_FIFO || s->cfg.policy == UGSDR_SERVE_RESPONSE_RATIO, "unknown serving policy");
 		require(s->cfg.max_inflight <= 64, "max_inflight above 64");
 		UG_CUDA(cudaSetDevice(ctx->device));
 		if (s->cfg.memory_budget) {
@@ -246,13 +336,18 @@ int ugsdr_server_create(ugsdr_ctx* ctx, const ugsdr_server_config* cfg, ugsdr_se
 		}
 		for (int i = 0; i < s->cfg.max_inflight; ++i)
 			s->slots.emplace_back();
+		int least = 0, greatest = 0;
+		UG_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
 		for (auto& sl : s->slots) {
-			UG_CUDA(cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking));
+			UG_CUDA(cudaStreamCreateWithPriority(&sl.stream, cudaStreamNonBlocking, least));
+			UG_CUDA(cudaStreamCreateWithPriority(&sl.urgent, cudaStreamNonBlocking, greatest));
 			UG_CUDA(cudaEventCreateWithFlags(&sl.event, cudaEventDisableTiming));
+			sl.active = sl.stream;
 			sl.ws.set_stream(sl.stream);  // scratch grows stream-ordered, without a device-wide wait
 		}
 		ugsdr_server* raw = s.get();
 		s->worker = std::thread([raw] { raw->run(); });
+		s->reaper = std::thread([raw] { raw->reap(); });
 		*server = s.release();
 	});
 }
@@ -274,6 +369,8 @@ int ugsdr_server_submit(ugsdr_server* server, const ugsdr_acq_job* job, uint64_t
 		}
 		std::lock_guard<std::mutex> lock(ctx->mutex);
 		r->estimate = jobs_device_bytes(ctx, &r->job, 1);  // validates the job too
+		r->work = static_cast<double>(r->job.n_codes) * doppler_grid(r->job.doppler_range, r->job.doppler_step).size() *
+			static_cast<double>(r->job.block_samples) * static_cast<double>(r->job.n_blocks);
 	});
 	if (st != UGSDR_OK)
 		return st;
@@ -283,6 +380,7 @@ int ugsdr_server_submit(ugsdr_server* server, const ugsdr_acq_job* job, uint64_t
 		return UGSDR_E_QUEUE_FULL;
 	}
 	r->ticket = server->next_ticket++;
+	r->queued = std::chrono::steady_clock::now();
 	*ticket = r->ticket;
 	server->pending.push_back(r.get());
 	server->requests[r->ticket] = std::move(r);
@@ -342,17 +440,22 @@ int ugsdr_server_destroy(ugsdr_server* server) {
 		server->stop = true;
 		server->cv_work.notify_all();
 	}
+	server->cv_reap.notify_all();
 	if (server->worker.joinable())
 		server->worker.join();
+	if (server->reaper.joinable())
+		server->reaper.join();
 	for (auto& sl : server->slots) {
-		sl.ws.release();  // stream-ordered frees, before the stream goes
-		if (sl.stream)
-			cudaStreamSynchronize(sl.stream);
+		sl.ws.release();  // stream-ordered frees, before the streams go
+		for (cudaStream_t st : {sl.stream, sl.urgent})
+			if (st)
+				cudaStreamSynchronize(st);
 		sl.ws.set_stream(nullptr);
 		if (sl.event)
 			cudaEventDestroy(sl.event);
-		if (sl.stream)
-			cudaStreamDestroy(sl.stream);
+		for (cudaStream_t st : {sl.stream, sl.urgent})
+			if (st)
+				cudaStreamDestroy(st);
 	}
 	delete server;
 	return UGSDR_OK;
