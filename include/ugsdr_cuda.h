@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define UGSDR_CUDA_ABI_VERSION 3
+#define UGSDR_CUDA_ABI_VERSION 4
 
 enum ugsdr_status {
 	UGSDR_OK = 0,
@@ -58,8 +58,28 @@ enum ugsdr_sample_type {
 	UGSDR_SAMPLES_CF32 = 0, /* interleaved float I/Q (std::complex<float>) */
 	UGSDR_SAMPLES_CI8 = 1,  /* interleaved int8 I/Q  (FileType::Iq_8_plus_8) */
 	UGSDR_SAMPLES_CI16 = 2, /* interleaved int16 I/Q (FileType::Iq_16_plus_16) */
-	UGSDR_SAMPLES_RI8 = 3   /* real int8, imag = 0   (FileType::Real_8) */
+	UGSDR_SAMPLES_RI8 = 3,  /* real int8, imag = 0   (FileType::Real_8) */
+	/* Packed front-end captures, decoded on the device as the reference's
+	 * readers decode them (signal_parameters.hpp:78-85, 186-246):
+	 * BBP DDC: 1 ms epochs of an 8-byte header and fs/1e3 complex samples,
+	 * two per byte (bits 0-3 and 4-7: imag then real 2-bit fields, each
+	 * read as (field | 1), i.e. +-1; helpers/BbpPackedSpan.hpp), the epoch
+	 * padded to an even count of 64-bit words; sample counts are whole epochs. */
+	UGSDR_SAMPLES_BBP_DDC = 4,
+	/* NT1065 grabber: one byte per sample carrying four channels, 2 bits each
+	 * (sign, magnitude) -> (2 sign - 1)(1 + 2 magnitude), real
+	 * (helpers/NtlabPackedSpan.hpp); _1 .. _4 = FileType::Nt1065GrabberFirst ..
+	 * Fourth, bit offsets 6, 4, 2, 0 */
+	UGSDR_SAMPLES_NT1065_1 = 5,
+	UGSDR_SAMPLES_NT1065_2 = 6,
+	UGSDR_SAMPLES_NT1065_3 = 7,
+	UGSDR_SAMPLES_NT1065_4 = 8
 };
+
+/* Bytes a capture of n_samples samples of sample_type occupies at
+ * sampling_rate (BBP DDC: whole 1 ms epochs with their headers and padding,
+ * as SignalParametersBase::OpenFile sizes them, signal_parameters.hpp:78-85). */
+int ugsdr_sample_bytes(int sample_type, double sampling_rate, size_t n_samples, size_t* bytes);
 
 /* Matched-filter spectrum convention. */
 enum ugsdr_spectrum_mode {
@@ -276,6 +296,12 @@ int ugsdr_correlate(ugsdr_ctx* ctx, const float* iq, const float* code, size_t n
 /* SignalParametersBase::GetPartialSignal int -> complex<float> conversion
  * (src/signal_parameters.hpp:150-183). */
 int ugsdr_convert_samples(ugsdr_ctx* ctx, const void* in, int sample_type, size_t n, float* out_iq);
+/* SignalParametersBase::GetSeveralMs for any sample type (signal_parameters.hpp:
+ * 150-246, 262-273): decodes n_samples samples (whole epochs for BBP DDC) of
+ * `in` (in_bytes bytes, host) captured at sampling_rate into out_iq
+ * (n_samples complex floats, host). */
+int ugsdr_unpack_samples(ugsdr_ctx* ctx, const void* in, size_t in_bytes, int sample_type, double sampling_rate,
+	size_t n_samples, float* out_iq);
 
 /* ------------------------------------------------------ tracking bank */
 /* Correlator bank for many channels per 1 ms epoch (Tracker::Track,

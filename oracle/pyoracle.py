@@ -174,3 +174,33 @@ def track_taps(iq_epoch: np.ndarray, chips: np.ndarray, fs: float, code_frequenc
     fn(x.ctypes.data, x.size, c.ctypes.data, len(c), fs, code_frequency, float(len(c)), code_phase, carrier_frequency,
        carrier_phase, early_late, very_early_late, out.ctypes.data)
     return out
+
+
+def bbp_epoch_bytes(fs: float) -> int:
+    """Bytes per 1 ms BBP DDC epoch (signal_parameters.hpp:78-85)."""
+    words = fs / 1e3 * 4 / 64 + 1
+    b = int(words / 2) * 2
+    if words % 2:
+        b += 2
+    return b * 8
+
+
+def unpack_bbp(raw: np.ndarray, fs: float) -> np.ndarray:
+    """BBP DDC epochs -> complex (helpers/BbpPackedSpan.hpp, signal_parameters.hpp:234-246):
+    skip each epoch's 8-byte header; byte s/2 holds sample s, imag in bits
+    0-1 / 4-5 and real in bits 2-3 / 6-7, each 2-bit field read as (f | 1)."""
+    spm = int(fs / 1e3)
+    eb = bbp_epoch_bytes(fs)
+    ep = raw.reshape(-1, eb)[:, 8:8 + spm // 2].astype(np.uint8)
+    out = np.empty((ep.shape[0], spm), np.complex64)
+    for half, sh in ((0, 0), (1, 4)):
+        im = np.where((ep >> (sh + 1)) & 1, -1.0, 1.0)
+        re = np.where((ep >> (sh + 3)) & 1, -1.0, 1.0)
+        out[:, half::2] = re + 1j * im
+    return out.reshape(-1)
+
+
+def unpack_nt1065(raw: np.ndarray, channel: int) -> np.ndarray:
+    """NT1065 bytes -> real samples (helpers/NtlabPackedSpan.hpp), channel 0..3 at bit offsets 6, 4, 2, 0."""
+    b = raw.astype(np.int32) >> (6 - 2 * channel)
+    return ((2 * (b & 1) - 1) * (1 + 2 * ((b >> 1) & 1))).astype(np.complex64)

@@ -29,6 +29,8 @@
 #include "mixer/table_mixer.hpp"
 #include "resample/resampler.hpp"
 #include "resample/upsampler.hpp"
+#include "helpers/NtlabPackedSpan.hpp"
+#include "signal_parameters.hpp"
 
 #include <complex>
 #include <cstdint>
@@ -258,4 +260,41 @@ void ref_acquire_f64(const double* iq, std::size_t n_total, std::size_t n, std::
 	Acquire<double>(iq, n_total, n, k_blocks, code, fs, range, step, if_freq, ratio, reshape, coherent, nullptr, rec, best_output);
 }
 
+
+// Packed front-end formats (golden vectors for the GPU decoders).
+// BbpDdc file through the reference's own reader: SignalParametersBase::
+// GetSeveralMs (signal_parameters.hpp:262-273) -> OpenFile's epoch framing
+// (78-85), VerifyHeaders (48-57) and PackedSpan (helpers/BbpPackedSpan.hpp).
+// Returns the number of decoded samples (ms * fs / 1e3) or -1 on error.
+long ref_bbp_read(const char* path, double central, double fs, std::size_t ms, float* out_iq) {
+	try {
+		auto sp = ugsdr::SignalParametersBase<float>(path, ugsdr::FileType::BbpDdc, central, fs);
+		// PackedSpan::Iterator::operator- (helpers/BbpPackedSpan.hpp:63-67) is
+		// off by one, so the reader's std::copy (signal_parameters.hpp:244)
+		// stops two samples past each epoch: harmless between epochs (the next
+		// one overwrites them), past the end of the last one.  The slack here
+		// keeps those two writes inside this vector.
+		const std::size_t n = ms * static_cast<std::size_t>(fs / 1e3);
+		std::vector<std::complex<float>> v(n + 64);
+		sp.GetSeveralMs(0, ms, v);
+		std::memcpy(out_iq, v.data(), n * sizeof(std::complex<float>));
+		return static_cast<long>(n);
+	}
+	catch (...) {
+		return -1;
+	}
+}
+
+// NT1065 grabber bytes through NtlabPackedSpan<offset> (helpers/NtlabPackedSpan.hpp),
+// channel 0..3 = First..Fourth (bit offsets 6, 4, 2, 0).
+void ref_nt1065_decode(const unsigned char* bytes, std::size_t n, int channel, float* out_iq) {
+	auto* dst = reinterpret_cast<std::complex<float>*>(out_iq);
+	const auto* src = reinterpret_cast<const std::byte*>(bytes);
+	switch (channel) {
+	case 0: { auto s = ugsdr::NtlabPackedSpan<6, float>(src, n); std::copy(s.begin(), s.end(), dst); break; }
+	case 1: { auto s = ugsdr::NtlabPackedSpan<4, float>(src, n); std::copy(s.begin(), s.end(), dst); break; }
+	case 2: { auto s = ugsdr::NtlabPackedSpan<2, float>(src, n); std::copy(s.begin(), s.end(), dst); break; }
+	default: { auto s = ugsdr::NtlabPackedSpan<0, float>(src, n); std::copy(s.begin(), s.end(), dst); break; }
+	}
+}
 }

@@ -55,6 +55,9 @@ def ref_lib(ref_dir: str) -> C.CDLL:
     lib.ref_correlate_f32.argtypes = [vp, vp, sz, vp]
     lib.ref_acquire_f32.argtypes = [vp, sz, sz, sz, vp, d, d, d, d, d, i, i, vp, vp]
     lib.ref_acquire_f64.argtypes = [vp, sz, sz, sz, vp, d, d, d, d, d, i, i, vp, vp]
+    lib.ref_bbp_read.argtypes = [C.c_char_p, d, d, sz, vp]
+    lib.ref_bbp_read.restype = C.c_long
+    lib.ref_nt1065_decode.argtypes = [vp, sz, i, vp]
     return lib
 
 
@@ -202,6 +205,41 @@ def acquisition(lib, code_fix) -> dict[str, np.ndarray]:
                 acq_truth=np.array([[t["prn"], t["doppler"], t["code_phase_samples"], t["cn0"]] for t in truth]))
 
 
+def bbp_epoch_bytes(fs: float) -> int:
+    """Bytes per 1 ms BbpDdc epoch (signal_parameters.hpp:78-85): 4 bits per
+    complex sample in 64-bit words plus a header word, padded to an even count."""
+    words = fs / 1e3 * 4 / 64 + 1
+    b = int(words / 2) * 2
+    if words % 2:
+        b += 2
+    return b * 8
+
+
+def packed(lib, ref_dir: str) -> dict[str, np.ndarray]:
+    """Packed front-end formats: the first 10 ms of the reference's real
+    BbpDdc capture (GPS L1, 33.25 MHz; fs and centre frequency as in
+    benchmark/benchmark.cpp:82) decoded by the reference's own reader, and
+    every NT1065 byte value decoded for each of the four channels."""
+    out = {}
+    path = Path(ref_dir) / "data" / "bbp_ddc_gps_L1.dat"
+    fs, ms = 33.25e6, 10
+    eb = bbp_epoch_bytes(fs)
+    raw = np.fromfile(path, np.uint8, count=eb * ms)
+    dec = np.zeros(int(fs / 1e3) * ms * 2, np.float32)
+    n = lib.ref_bbp_read(str(path).encode(), 1575.42e6, fs, ms, p(dec))
+    assert n == int(fs / 1e3) * ms
+    out["bbp_raw"] = raw
+    out["bbp_fs"] = np.array(fs)
+    out["bbp_epoch_bytes"] = np.array(eb)
+    out["bbp_decoded"] = dec.reshape(-1, 2).astype(np.int8)  # values are +-1
+    nt = np.arange(256, dtype=np.uint8)
+    for ch in range(4):
+        d = np.zeros(512, np.float32)
+        lib.ref_nt1065_decode(p(nt), nt.size, ch, p(d))
+        out[f"nt1065_{ch}"] = d.reshape(-1, 2).astype(np.int8)  # values -3, -1, 1, 3 (imag 0)
+    return out
+
+
 def main() -> None:
     ref_dir = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     lib = ref_lib(ref_dir)
@@ -211,6 +249,7 @@ def main() -> None:
     np.savez_compressed(HERE / "kats.npz", **k)
     a = acquisition(lib, c)
     np.savez_compressed(HERE / "acq_gps_l1_4mhz.npz", **a)
+    np.savez_compressed(HERE / "packed.npz", **packed(lib, ref_dir))
     for f in sorted(HERE.glob("*.npz")):
         print(f.name, f.stat().st_size)
 

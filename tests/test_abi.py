@@ -28,7 +28,7 @@ def test_exports_every_header_symbol(lib):
 
 
 def test_abi_version(lib):
-    assert lib.ugsdr_abi_version() == 3  # ugsdr_server_config gained policy
+    assert lib.ugsdr_abi_version() == 4  # packed sample types
 
 
 @pytest.mark.parametrize("name,signal,count", [("gps_l1ca", L.GPS_L1CA, 37), ("gps_l5i", L.GPS_L5I, 32),
@@ -75,3 +75,15 @@ def test_galileo_codes_are_boc(golden_codes):
         c = unpack_codes(golden_codes, name)
         assert c.shape == (50, 8184)
         np.testing.assert_array_equal(c[:, 0::2], -c[:, 1::2])  # DecodeBoc [c, -c]
+
+
+def test_capture_sizes(lib):
+    """ugsdr_sample_bytes: BBP DDC epochs as SignalParametersBase::OpenFile sizes
+    them (33.25 MHz: 16,640 bytes per 1 ms), one byte per NT1065 sample."""
+    import ctypes as C
+    b = C.c_size_t()
+    assert lib.ugsdr_sample_bytes(4, 33.25e6, 33250 * 10, C.byref(b)) == 0 and b.value == 166400
+    assert lib.ugsdr_sample_bytes(5, 50e6, 1000, C.byref(b)) == 0 and b.value == 1000
+    assert lib.ugsdr_sample_bytes(2, 4e6, 1000, C.byref(b)) == 0 and b.value == 4000
+    assert lib.ugsdr_sample_bytes(4, 33.25e6, 33250 + 1, C.byref(b)) != 0  # not whole epochs
+    assert lib.ugsdr_sample_bytes(4, 33.2505e6, 33250, C.byref(b)) != 0    # not a whole-kHz rate

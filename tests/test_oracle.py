@@ -2,6 +2,7 @@
 primitives: every golden vector in tests/golden/ was produced by the
 reference sources compiled into oracle/_ref (tests/golden/make_golden.py)."""
 import numpy as np
+from pathlib import Path
 import pytest
 
 from conftest import unpack_codes
@@ -117,3 +118,16 @@ def test_acquisition_matches_reference(oracle, acq_golden, golden_codes):
         assert r64["index"] == rec64[4] and r64["doppler_bin"] == rec64[5]
         assert abs(r64["level"] - rec64[0]) <= 1e-9 * rec64[0]
         assert abs(r64["snr"] - rec64[6]) <= 1e-9 * rec64[6]
+
+
+def test_packed_decoders(oracle):
+    """The oracle's BBP DDC / NT1065 decoders against the reference's own
+    readers (SignalParametersBase::GetSeveralMs on the real BBP capture,
+    NtlabPackedSpan on every byte value)."""
+    z = np.load(Path(__file__).parent / "golden" / "packed.npz")
+    g = z["bbp_decoded"].astype(np.float32)
+    np.testing.assert_array_equal(oracle.unpack_bbp(z["bbp_raw"], float(z["bbp_fs"])), g[:, 0] + 1j * g[:, 1])
+    assert oracle.bbp_epoch_bytes(float(z["bbp_fs"])) == int(z["bbp_epoch_bytes"])
+    for ch in range(4):
+        g = z[f"nt1065_{ch}"].astype(np.float32)
+        np.testing.assert_array_equal(oracle.unpack_nt1065(np.arange(256, dtype=np.uint8), ch), g[:, 0] + 1j * g[:, 1])

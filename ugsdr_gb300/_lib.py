@@ -10,7 +10,7 @@ from pathlib import Path
 
 LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libugsdr_cuda.so"
 
-ABI_VERSION = 3  # UGSDR_CUDA_ABI_VERSION the structs below mirror
+ABI_VERSION = 4  # UGSDR_CUDA_ABI_VERSION the structs below mirror
 
 OK = 0
 E_INVALID = -1
@@ -23,6 +23,7 @@ E_TIMEOUT = -7
 
 GPS_L1CA, GPS_L2CM, GPS_L5I, GPS_L5Q, GLONASS_L1OF, GLONASS_L2OF, GALILEO_E1B, GALILEO_E1C = range(8)
 SAMPLES_CF32, SAMPLES_CI8, SAMPLES_CI16, SAMPLES_RI8 = range(4)
+SAMPLES_BBP_DDC, SAMPLES_NT1065_1, SAMPLES_NT1065_2, SAMPLES_NT1065_3, SAMPLES_NT1065_4 = range(4, 9)
 SPECTRUM_ONE_SIDED, SPECTRUM_TWO_SIDED = 0, 1
 STAT_ABS, STAT_ABS2 = 0, 1
 
@@ -148,6 +149,8 @@ SIGNATURES = {
     "ugsdr_resample": (_i, [_vp, _vp, _sz, _u64, _u64, _vp, _sz, C.POINTER(_sz)]),
     "ugsdr_correlate": (_i, [_vp, _vp, _vp, _sz, _vp]),
     "ugsdr_convert_samples": (_i, [_vp, _vp, _i, _sz, _vp]),
+    "ugsdr_sample_bytes": (_i, [_i, _d, _sz, C.POINTER(_sz)]),
+    "ugsdr_unpack_samples": (_i, [_vp, _vp, _sz, _i, _d, _sz, _vp]),
     "ugsdr_track_create": (_i, [_vp, C.POINTER(TrackConfig), C.POINTER(TrackChannel), _i, _vp, C.POINTER(_i), _i, _i,
                                 C.POINTER(_vp)]),
     "ugsdr_track_run": (_i, [_vp, _vp, _i, _i, _sz, _i, C.POINTER(TrackOutput)]),

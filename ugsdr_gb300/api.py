@@ -103,8 +103,8 @@ class Context:
         else:
             arr = np.ascontiguousarray(samples)
             ptr = _ptr(arr)
-            per = {L.SAMPLES_CF32: 8, L.SAMPLES_CI8: 2, L.SAMPLES_CI16: 4, L.SAMPLES_RI8: 1}[sample_type]
-            n_samples = arr.nbytes // per
+            if n_samples is None:
+                n_samples = self.samples_in(sample_type, input_sampling_rate or fs, arr.nbytes)
             samples = arr
         job = L.AcqJob(ptr, sample_type, 1 if on_device else 0, n_samples, fs, intermediate_frequency, frontend_frequency,
                        code_offset_ratio,
@@ -134,7 +134,25 @@ class Context:
         self._check(self.lib.ugsdr_acquire_batch(self.h, arr, len(jobs), ptrs))
         return [[AcqResult.from_c(x) for x in r] for r in res]
 
+    def samples_in(self, sample_type: int, fs: float, nbytes: int) -> int:
+        """Samples held by `nbytes` bytes of a capture (BBP DDC: whole epochs)."""
+        if sample_type == L.SAMPLES_BBP_DDC:
+            one = C.c_size_t()
+            self._check(self.lib.ugsdr_sample_bytes(sample_type, fs, int(fs // 1000), C.byref(one)))
+            return nbytes // one.value * int(fs // 1000)
+        per = {L.SAMPLES_CF32: 8, L.SAMPLES_CI8: 2, L.SAMPLES_CI16: 4}.get(sample_type, 1)
+        return nbytes // per
+
     # ------------------------------------------------------------ per-op
+    def unpack_samples(self, raw: np.ndarray, sample_type: int, fs: float, n_samples: int | None = None) -> np.ndarray:
+        """SignalParametersBase::GetSeveralMs decoding of any capture format
+        (packed BBP DDC / NT1065 included) to complex64."""
+        raw = np.ascontiguousarray(raw)
+        n = n_samples if n_samples is not None else self.samples_in(sample_type, fs, raw.nbytes)
+        out = np.empty(n, np.complex64)
+        self._check(self.lib.ugsdr_unpack_samples(self.h, _ptr(raw), raw.nbytes, sample_type, fs, n, _ptr(out)))
+        return out
+
     def mix(self, iq: np.ndarray, fs: float, frequency: float, phase: float = 0.0) -> np.ndarray:
         """Mixer<TableMixer>::Translate(src_dst, fs, f, phase), in place (complex64)."""
         assert iq.dtype == np.complex64 and iq.flags.c_contiguous

@@ -403,12 +403,18 @@ namespace ugsdr_gpu {
 		JobLaunch validate(ugsdr_ctx* ctx, const ugsdr_acq_job& job) {
 			JobLaunch L;
 			require(job.samples != nullptr, "null samples");
-			require(job.sample_type >= 0 && job.sample_type <= 3, "unknown sample type");
+			require(job.sample_type >= 0 && job.sample_type <= UGSDR_SAMPLES_NT1065_4, "unknown sample type");
 			require(job.block_samples >= 2 && job.block_samples <= (1u << 24), "block size out of range");
 			require(job.n_blocks >= 1, "n_blocks must be >= 1");
 			require(job.sampling_rate > 0, "sampling rate must be positive");
 			L.front = job.input_sampling_rate != 0.0 && job.input_sampling_rate != job.sampling_rate;
-			if (L.front) {
+			if (!L.front && is_packed(job.sample_type)) {
+				// packed captures are decoded by the front end, at the same rate
+				L.front = true;
+				L.rs = ResamplePlan{1, 1, job.n_samples, job.n_samples};
+				require(job.n_samples >= job.block_samples * job.n_blocks, "not enough samples for n_blocks blocks");
+			}
+			else if (L.front) {
 				const double fi = job.input_sampling_rate, fo = job.sampling_rate;
 				require(fi > 0 && fi == std::floor(fi) && fo == std::floor(fo) && fi < 1e15 && fo < 1e15,
 					"resampling needs positive integer rates in Hz");
@@ -451,17 +457,17 @@ namespace ugsdr_gpu {
 				require(it->second->n == job.block_samples, "code length differs from block_samples");
 				require(it->second->spectrum_mode == job.spectrum_mode, "code spectrum mode differs from the job's");
 			}
+			if (is_packed(job.sample_type))
+				require(capture_bytes(job.sample_type, job.input_sampling_rate != 0.0 ? job.input_sampling_rate : job.sampling_rate,
+					job.n_samples) > 0, "BBP DDC captures need a whole-kHz rate and whole 1 ms epochs");
 			L.large = !fits_single_cta(ctx, L.n);
 			return L;
 		}
 
-		size_t sample_bytes(int type) {
-			switch (type) {
-			case UGSDR_SAMPLES_CF32: return 8;
-			case UGSDR_SAMPLES_CI8: return 2;
-			case UGSDR_SAMPLES_CI16: return 4;
-			default: return 1;
-			}
+		// bytes of the job's capture (packed formats: with their framing)
+		size_t job_bytes(const ugsdr_acq_job& job) {
+			return capture_bytes(job.sample_type, job.input_sampling_rate != 0.0 ? job.input_sampling_rate : job.sampling_rate,
+				job.n_samples);
 		}
 	}
 
@@ -556,9 +562,12 @@ namespace ugsdr_gpu {
 		FrontEndParams f{};
 		f.samples = samples;
 		f.n_in = job.n_samples;
+		const double fs_in = job.input_sampling_rate != 0.0 ? job.input_sampling_rate : job.sampling_rate;
+		f.layout.spm = static_cast<uint32_t>(fs_in / 1e3);
+		f.layout.epoch_bytes = static_cast<uint32_t>(bbp_epoch_bytes(fs_in));
 		f.rs = L.rs;
 		f.fe_on = job.frontend_frequency != 0.0;
-		f.fe_adder = f.fe_on ? nco_adder(job.input_sampling_rate, job.frontend_frequency) : 0u;
+		f.fe_adder = f.fe_on ? nco_adder(fs_in, job.frontend_frequency) : 0u;
 		f.lut = get_lut(ctx);
 		f.out = out;
 		f.n = static_cast<uint64_t>(L.n) * L.k;
@@ -568,7 +577,12 @@ namespace ugsdr_gpu {
 		case UGSDR_SAMPLES_CF32: front_end_kernel<UGSDR_SAMPLES_CF32><<<blocks, 256, 0, ctx->stream>>>(f); break;
 		case UGSDR_SAMPLES_CI8: front_end_kernel<UGSDR_SAMPLES_CI8><<<blocks, 256, 0, ctx->stream>>>(f); break;
 		case UGSDR_SAMPLES_CI16: front_end_kernel<UGSDR_SAMPLES_CI16><<<blocks, 256, 0, ctx->stream>>>(f); break;
-		default: front_end_kernel<UGSDR_SAMPLES_RI8><<<blocks, 256, 0, ctx->stream>>>(f); break;
+		case UGSDR_SAMPLES_RI8: front_end_kernel<UGSDR_SAMPLES_RI8><<<blocks, 256, 0, ctx->stream>>>(f); break;
+		case UGSDR_SAMPLES_BBP_DDC: front_end_kernel<UGSDR_SAMPLES_BBP_DDC><<<blocks, 256, 0, ctx->stream>>>(f); break;
+		case UGSDR_SAMPLES_NT1065_1: front_end_kernel<UGSDR_SAMPLES_NT1065_1><<<blocks, 256, 0, ctx->stream>>>(f); break;
+		case UGSDR_SAMPLES_NT1065_2: front_end_kernel<UGSDR_SAMPLES_NT1065_2><<<blocks, 256, 0, ctx->stream>>>(f); break;
+		case UGSDR_SAMPLES_NT1065_3: front_end_kernel<UGSDR_SAMPLES_NT1065_3><<<blocks, 256, 0, ctx->stream>>>(f); break;
+		default: front_end_kernel<UGSDR_SAMPLES_NT1065_4><<<blocks, 256, 0, ctx->stream>>>(f); break;
 		}
 		note_launch(ctx);
 	}
@@ -595,7 +609,7 @@ namespace ugsdr_gpu {
 				s.launches.push_back(validate(ctx, jobs[j]));
 				const auto& L = s.launches.back();
 				if (!jobs[j].samples_on_device) {
-					const size_t bytes = sample_bytes(jobs[j].sample_type) * jobs[j].n_samples;
+					const size_t bytes = job_bytes(jobs[j]);
 					if (!seen[{jobs[j].samples, bytes}])
 						s.samples += (bytes + 255) / 256 * 256;
 					seen[{jobs[j].samples, bytes}] = true;
@@ -652,7 +666,7 @@ namespace ugsdr_gpu {
 				dev_samples[j] = job.samples;
 			}
 			else {
-				const size_t bytes = sample_bytes(job.sample_type) * job.n_samples;
+				const size_t bytes = job_bytes(job);
 				auto key = std::make_pair(job.samples, bytes);
 				auto it = staged.find(key);
 				if (it != staged.end()) {

@@ -173,3 +173,39 @@ int ugsdr_doppler_bins(double range, double step, uint32_t* n) {
 
 int ugsdr_abi_version(void) { return UGSDR_CUDA_ABI_VERSION; }
 }
+
+namespace ugsdr_gpu {
+	// SignalParametersBase::OpenFile, FileType::BbpDdc (signal_parameters.hpp:78-85):
+	// 4 bits per complex sample in 64-bit words plus a header word, padded to
+	// an even number of words
+	size_t bbp_epoch_bytes(double fs) {
+		if (!(fs > 0) || std::fmod(fs, 1e3) != 0.0)
+			return 0;
+		const double words = fs / 1e3 * 4 / 64 + 1;
+		size_t b = static_cast<size_t>(words / 2) * 2;
+		if (std::fmod(words, 2.0) != 0.0)
+			b += 2;
+		return b * 8;
+	}
+
+	size_t capture_bytes(int sample_type, double fs, size_t n) {
+		switch (sample_type) {
+		case UGSDR_SAMPLES_CF32: return 8 * n;
+		case UGSDR_SAMPLES_CI8: return 2 * n;
+		case UGSDR_SAMPLES_CI16: return 4 * n;
+		case UGSDR_SAMPLES_BBP_DDC: {
+			const size_t eb = bbp_epoch_bytes(fs);
+			const size_t spm = eb ? static_cast<size_t>(fs / 1e3) : 0;
+			return spm && n % spm == 0 ? n / spm * eb : 0;
+		}
+		default: return n;  // RI8 and NT1065: one byte per sample
+		}
+	}
+}
+
+extern "C" int ugsdr_sample_bytes(int sample_type, double sampling_rate, size_t n_samples, size_t* bytes) {
+	if (!bytes || sample_type < 0 || sample_type > UGSDR_SAMPLES_NT1065_4)
+		return UGSDR_E_INVALID;
+	*bytes = ugsdr_gpu::capture_bytes(sample_type, sampling_rate, n_samples);
+	return *bytes || n_samples == 0 ? UGSDR_OK : UGSDR_E_INVALID;
+}

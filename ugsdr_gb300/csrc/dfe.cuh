@@ -2,7 +2,7 @@
 // by SequentialResampler, with the reference's float rounding.
 #pragma once
 
-#include "acq_kernels.cuh"
+#include "packed.cuh"
 
 namespace ugsdr_gpu {
 
@@ -48,7 +48,8 @@ namespace ugsdr_gpu {
 	}
 
 	struct FrontEndParams {
-		const void* samples;   // n_in input samples
+		const void* samples;   // n_in input samples of the job's sample type
+		PackedLayout layout;   // packed types: framing
 		uint64_t n_in;
 		ResamplePlan rs;
 		uint32_t fe_adder;     // Translate(signal, fs_in, f) adder
@@ -58,14 +59,15 @@ namespace ugsdr_gpu {
 		uint64_t n;
 	};
 
-	// Translate at the input rate (fse.hpp:289, 312: phase 0 at input sample 0)
-	// then resample (fse.hpp:290-291, 313-314), for the first p.n outputs.
+	// Decode (packed formats), Translate at the input rate (fse.hpp:289, 312:
+	// phase 0 at input sample 0), then resample (fse.hpp:290-291, 313-314),
+	// for the first p.n outputs.
 	template <int ST>
 	__global__ void __launch_bounds__(256) front_end_kernel(FrontEndParams p) {
 		const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
 		for (uint64_t k = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; k < p.n; k += stride) {
 			p.out[k] = resample_point(k, p.rs, [&](uint64_t j) {
-				float2 v = load_sample<ST>(p.samples, j);
+				float2 v = load_any<ST>(p.samples, j, p.layout);
 				if (p.fe_on)
 					v = table_mix(v, j, p.fe_adder, 0u, p.lut);
 				return v;

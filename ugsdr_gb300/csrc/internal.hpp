@@ -227,6 +227,13 @@ namespace ugsdr_gpu {
 	// Device bytes a batch needs beyond what `ws` already holds (admission control).
 	size_t jobs_device_bytes(ugsdr_ctx* ctx, const ugsdr_acq_job* jobs, int n_jobs);
 
+	// capture framing (codes.cpp): bytes of a BBP DDC epoch at fs (0 if fs is not
+	// a whole number of kHz), bytes of n samples of any sample type (0 if the
+	// count is not whole BBP epochs), whether the type is a packed format
+	size_t bbp_epoch_bytes(double fs);
+	size_t capture_bytes(int sample_type, double fs, size_t n);
+	inline bool is_packed(int sample_type) { return sample_type >= UGSDR_SAMPLES_BBP_DDC && sample_type <= UGSDR_SAMPLES_NT1065_4; }
+
 	// shared host helpers (codes.cpp)
 	int prn_code(int signal, int sv, float* out, size_t cap, size_t* len);
 	// TableMixer adder for Translate(signal, fs, f): f < 0 -> fs + f (mixer.hpp:46-47)

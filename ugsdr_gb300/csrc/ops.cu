@@ -6,6 +6,7 @@
 #include "acq_kernels.cuh"
 #include "four_step.cuh"
 #include "dfe.cuh"
+#include "packed.cuh"
 #include "fft_plan.hpp"
 
 #include <algorithm>
@@ -661,6 +662,28 @@ int ugsdr_convert_samples(ugsdr_ctx* ctx, const void* in, int sample_type, size_
 		}
 		note_launch(ctx);
 		d2h(ctx, out_iq, ctx->op_b.ptr, sizeof(float2) * n);
+	});
+}
+
+int ugsdr_unpack_samples(ugsdr_ctx* ctx, const void* in, size_t in_bytes, int sample_type, double sampling_rate,
+	size_t n_samples, float* out_iq) {
+	UG_ENTRY(ctx) {
+		require(in && out_iq, "null buffer");
+		require(sample_type >= 0 && sample_type <= UGSDR_SAMPLES_NT1065_4, "unknown sample type");
+		const size_t bytes = capture_bytes(sample_type, sampling_rate, n_samples);
+		require(bytes > 0 || n_samples == 0, "BBP DDC captures need a whole-kHz rate and whole 1 ms epochs");
+		require(in_bytes >= bytes, "input holds fewer bytes than n_samples need");
+		if (n_samples == 0)
+			return;
+		PackedLayout l;
+		l.spm = static_cast<uint32_t>(sampling_rate / 1e3);
+		l.epoch_bytes = static_cast<uint32_t>(bbp_epoch_bytes(sampling_rate));
+		ctx->op_a.reserve(bytes + 16);
+		ctx->op_b.reserve(sizeof(float2) * n_samples);
+		h2d(ctx, ctx->op_a.ptr, in, bytes);
+		unpack_kernel<<<blocks_for(n_samples), kT, 0, ctx->stream>>>(ctx->op_a.ptr, sample_type, l, n_samples, ctx->op_b.as<float2>());
+		note_launch(ctx);
+		d2h(ctx, out_iq, ctx->op_b.ptr, sizeof(float2) * n_samples);
 	});
 }
 }

@@ -16,7 +16,9 @@
 // per-sample division), then thread 0 runs the FP64 loop update.
 #include "internal.hpp"
 #include "acq_kernels.cuh"
+#include "packed.cuh"
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 
@@ -485,7 +487,7 @@ struct ugsdr_track_bank {
 	size_t spm = 0;
 	double offsets[5] = {};
 	double k1_pll = 0, k2_pll = 0, k3_pll = 0, k1_dll = 0, k2_dll = 0;
-	DevBuf chips, states, samples, out;
+	DevBuf chips, states, samples, out, unpacked;
 };
 
 namespace {
@@ -496,15 +498,28 @@ namespace {
 		ugsdr_ctx* ctx = bank->ctx;
 		require(samples && n_epochs > 0, "null samples or no epochs");
 		require(samples_per_epoch == bank->spm, "samples_per_epoch must be sampling_rate / 1000");
-		require(sample_type >= 0 && sample_type <= 3, "unknown sample type");
-		const size_t per = sample_type == UGSDR_SAMPLES_CF32 ? 8 : sample_type == UGSDR_SAMPLES_CI8 ? 2 : sample_type == UGSDR_SAMPLES_CI16 ? 4 : 1;
+		require(sample_type >= 0 && sample_type <= UGSDR_SAMPLES_NT1065_4, "unknown sample type");
 		const size_t n = bank->spm * static_cast<size_t>(n_epochs);
+		const size_t bytes = capture_bytes(sample_type, bank->fs, n);
 		const void* dev = samples;
 		if (!samples_on_device) {
-			bank->samples.reserve(per * n);
-			UG_CUDA(cudaMemcpyAsync(bank->samples.ptr, samples, per * n, cudaMemcpyHostToDevice, ctx->stream));
+			bank->samples.reserve(bytes);
+			UG_CUDA(cudaMemcpyAsync(bank->samples.ptr, samples, bytes, cudaMemcpyHostToDevice, ctx->stream));
 			dev = bank->samples.ptr;
 		}
+		if (is_packed(sample_type)) {
+			// packed captures (BBP DDC, NT1065) are decoded to complex float first
+			PackedLayout l;
+			l.spm = static_cast<uint32_t>(bank->spm);
+			l.epoch_bytes = static_cast<uint32_t>(bbp_epoch_bytes(bank->fs));
+			bank->unpacked.reserve(sizeof(float2) * n);
+			const int blocks = static_cast<int>(std::min<size_t>((n + 255) / 256, static_cast<size_t>(ctx->sm_count) * 8));
+			unpack_kernel<<<blocks, 256, 0, ctx->stream>>>(dev, sample_type, l, n, bank->unpacked.as<float2>());
+			note_launch(ctx);
+			dev = bank->unpacked.ptr;
+			sample_type = UGSDR_SAMPLES_CF32;
+		}
+		const size_t per = capture_bytes(sample_type, bank->fs, n) / n;  // bytes per sample the kernel reads
 		TrackParams p{};
 		p.samples = dev;
 		p.spm = bank->spm;
