@@ -363,6 +363,24 @@ int ugsdr_track_run_device(ugsdr_track_bank* bank, const void* samples, int samp
 	int n_epochs, ugsdr_track_output* outputs);
 int ugsdr_track_destroy(ugsdr_track_bank* bank);
 
+/* Acquisition -> tracking hand-off: TrackingParameters::AddSignalImpl's
+ * code-phase refinement (src/tracking/tracking_parameters.hpp:297-357) for
+ * n_channels channels at once, on the device.  Per channel: the first three
+ * code periods of `samples` (n_samples >= 3 periods at the channel's rate),
+ * translated by -carrier_frequency, matched-filtered against one code period
+ * upsampled, zero-padded to three periods and rotated right by
+ * (integer) code_phase; |.| folded to one period; the first maximum's offset
+ * (wrapped to +-period / 2) goes to offsets[c] (may be NULL), and when it is
+ * within 1e-6 fs samples of a whole number of ms, accepted[c] = 1 and the
+ * channel's code_phase += offset (else accepted[c] = 0, code_phase kept).
+ * codes: n_codes x code_len_max chips as for ugsdr_track_create.  All
+ * channels' filters run as one batch of one-row acquisition jobs.  (An
+ * arbitrary replica given as samples is ugsdr_code_put with repeats 1 and
+ * samples = its length.) */
+int ugsdr_track_refine(ugsdr_ctx* ctx, ugsdr_track_channel* channels, int n_channels, const float* codes,
+	const int* code_lens, int n_codes, int code_len_max, const void* samples, int sample_type, int samples_on_device,
+	size_t n_samples, int* accepted, int* offsets);
+
 /* ------------------------------------------------------------ serving */
 /* Continuous-batching acquisition server.  A worker thread admits queued jobs
  * into `max_inflight` slots, each with its own CUDA stream and scratch, as

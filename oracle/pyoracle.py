@@ -204,3 +204,35 @@ def unpack_nt1065(raw: np.ndarray, channel: int) -> np.ndarray:
     """NT1065 bytes -> real samples (helpers/NtlabPackedSpan.hpp), channel 0..3 at bit offsets 6, 4, 2, 0."""
     b = raw.astype(np.int32) >> (6 - 2 * channel)
     return ((2 * (b & 1) - 1) * (1 + 2 * ((b >> 1) & 1))).astype(np.complex64)
+
+
+def track_refine(x: np.ndarray, channels: list[dict], codes: list[np.ndarray]):
+    """TrackingParameters::AddSignalImpl's refinement (tracking_parameters.hpp:
+    297-357) with the oracle's primitives, for channels whose code period is
+    1 ms (the oracle's fold block is one ms): returns (accepted, offsets,
+    refined code phases, peak levels)."""
+    acc, offs, phases, levels = [], [], [], []
+    for ch in channels:
+        fs = ch["fs"]
+        spm = int(fs / 1e3)
+        chips = np.asarray(codes[ch["code"]], np.float32)
+        period = spm * int(round(len(chips) / ch["code_frequency"] * 1000))
+        assert period == spm
+        n = 3 * period
+        y = table_mix(np.ascontiguousarray(x[:n], np.complex64), fs, -ch["carrier_frequency"])
+        replica = np.zeros(n, np.float32)
+        replica[:period] = upsample(chips, period)
+        replica = np.roll(replica, int(ch["code_phase"]))          # std::rotate right by (ptrdiff_t)code_phase
+        rec = acquire(y, n, 1, replica, fs, 0.0, 1.0, reshape=True, coherent=True)
+        off = int(rec["index"])
+        if off > period // 2:
+            off -= period
+        mod = (off + period) % spm
+        if mod > spm // 2:
+            mod -= spm
+        ok = abs(mod) < 1e-6 * fs
+        acc.append(1 if ok else 0)
+        offs.append(off)
+        phases.append(ch["code_phase"] + off if ok else ch["code_phase"])
+        levels.append(rec["level"])
+    return acc, offs, phases, levels

@@ -105,3 +105,28 @@ def test_bank_rejects_bad_configs(ctx, golden_codes):
         TrackBank(ctx, [dict(code=0, fs=4.0005e6, code_frequency=1.023e6, code_phase=0.0, carrier_frequency=0.0)], [ca[0]])
     with pytest.raises(L.UgsdrError):  # code index out of range
         TrackBank(ctx, [dict(code=3, fs=4e6, code_frequency=1.023e6, code_phase=0.0, carrier_frequency=0.0)], [ca[0]])
+
+
+def test_refine_handoff_vs_oracle(ctx, oracle, golden_codes):
+    """ugsdr_track_refine (AddSignalImpl's code-phase refinement): channels
+    started 2-3 samples off find the offset and are accepted; one started half
+    a millisecond off is rejected; offsets and acceptance equal the oracle's."""
+    from ugsdr_gb300.api import track_refine
+    ca = unpack_codes(golden_codes, "gps_l1ca")
+    codes = {p: ca[p] for p in range(8)}
+    raw, truth = signals.gps_l1_config(seed=31, codes=codes, fs=4e6, ms=6, visible=3, cn0=(46, 50), max_doppler=3000)
+    x = to_complex(raw)
+    chips, chans = [], []
+    for i, t in enumerate(truth):
+        chips.append(ca[t["prn"]])
+        cp = float(round(t["code_phase_samples"]))
+        chans.append(dict(code=i, fs=4e6, code_frequency=1.023e6, code_phase=(cp + (2.0, -3.0, 2000.0)[i]) % 4000,
+                          carrier_frequency=round(t["doppler"] / 50) * 50.0))
+    acc, offs, refined = track_refine(ctx, chans, chips, raw, L.SAMPLES_CI8)
+    o_acc, o_offs, o_phases, _ = oracle.track_refine(x, chans, chips)
+    assert acc == o_acc and offs == o_offs, (acc, offs, o_acc, o_offs)
+    assert acc == [1, 1, 0]
+    assert [r["code_phase"] for r in refined] == o_phases
+    for i in range(2):
+        true_cp = float(round(truth[i]["code_phase_samples"]))
+        assert abs((refined[i]["code_phase"] - true_cp + 2000) % 4000 - 2000) <= 1

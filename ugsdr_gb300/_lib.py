@@ -156,6 +156,8 @@ SIGNATURES = {
     "ugsdr_track_run": (_i, [_vp, _vp, _i, _i, _sz, _i, C.POINTER(TrackOutput)]),
     "ugsdr_track_run_device": (_i, [_vp, _vp, _i, _sz, _i, _vp]),
     "ugsdr_track_destroy": (_i, [_vp]),
+    "ugsdr_track_refine": (_i, [_vp, C.POINTER(TrackChannel), _i, _vp, C.POINTER(_i), _i, _i, _vp, _i, _i, _sz,
+                                C.POINTER(_i), C.POINTER(_i)]),
     "ugsdr_server_create": (_i, [_vp, C.POINTER(ServerConfig), C.POINTER(_vp)]),
     "ugsdr_server_submit": (_i, [_vp, C.POINTER(AcqJob), C.POINTER(_u64)]),
     "ugsdr_server_poll": (_i, [_vp, _u64, C.POINTER(AcqResult), C.POINTER(_i)]),

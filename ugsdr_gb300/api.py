@@ -357,6 +357,31 @@ class TrackBank:
             pass
 
 
+def track_refine(ctx: Context, channels: list[dict], codes: list[np.ndarray], samples, sample_type: int):
+    """ugsdr_track_refine: TrackingParameters::AddSignalImpl's code-phase
+    refinement of acquired channels.  Returns (accepted, offsets, channels
+    with refined code_phase)."""
+    lens = [len(c) for c in codes]
+    lmax = max(lens)
+    table = np.zeros((len(codes), lmax), np.float32)
+    for i, c in enumerate(codes):
+        table[i, : len(c)] = c
+    chs = (L.TrackChannel * len(channels))()
+    for i, ch in enumerate(channels):
+        code_len = lens[ch["code"]] if 0 <= ch["code"] < len(lens) else 0
+        chs[i] = L.TrackChannel(ch["code"], ch["fs"], ch["code_frequency"], code_len, ch["code_phase"],
+                                ch["carrier_frequency"], ch.get("carrier_phase", 0.0), ch.get("boc", 0))
+    raw = np.ascontiguousarray(samples)
+    n = ctx.samples_in(sample_type, channels[0]["fs"], raw.nbytes)
+    acc = (C.c_int * len(channels))()
+    off = (C.c_int * len(channels))()
+    lens_arr = (C.c_int * len(lens))(*lens)
+    ctx._check(ctx.lib.ugsdr_track_refine(ctx.h, chs, len(channels), _ptr(table), lens_arr, len(codes), lmax, _ptr(raw),
+                                          sample_type, 0, n, acc, off))
+    out = [dict(ch, code_phase=chs[i].code_phase) for i, ch in enumerate(channels)]
+    return list(acc), list(off), out
+
+
 class Server:
     """Continuous-batching acquisition server (ugsdr_server_*)."""
 
