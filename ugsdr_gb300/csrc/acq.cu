@@ -207,6 +207,10 @@ namespace ugsdr_gpu {
 		size_t smem_rows(const BatchedParams& p, bool) {
 			return 2 * sizeof(float2) * static_cast<size_t>(p.rw) * p.n2 + sizeof(float2) * p.n2 + 16;
 		}
+		template <class F>
+		size_t smem_inv_rows(const BatchedParams& p) {
+			return (rows_one_tile<F>() ? 1 : 2) * sizeof(float2) * static_cast<size_t>(p.rw) * p.n2 + sizeof(float2) * p.n2 + 16;
+		}
 
 		int chunks_of(int total, int per) { return (total + per - 1) / per; }
 
@@ -321,13 +325,15 @@ namespace ugsdr_gpu {
 			if (s.fold_mode == 2)
 				p.zcg = reinterpret_cast<float2*>(scratch + lay.zcg);
 		}
-		const size_t smem_r = smem_rows(p, true), smem_c = smem_cols(p, true);
+		const size_t smem_c = smem_cols(p, true);
 		with_large_ffts(p.n1, p.n2, [&](auto f1, auto f2) {
 			using F1 = decltype(f1);
 			using F2 = decltype(f2);
+			const size_t smem_r = smem_inv_rows<F2>(p);
 			set_smem(inv_rows_kernel<F2>, smem_r);
 			set_smem(inv_cols_kernel<F1>, smem_c);
 			const int t_rows = threads_of<F2>(p.p2, p.rw), t_cols = threads_of<F1>(p.p1, p.cw);
+			require(t_rows <= F2::kRowsMaxThreads, "row kernel needs more threads than its launch bound");
 			KernelTimer timer(ctx, "acq_inverse_large");
 			for (int row0 = 0; row0 < s.rows; row0 += r_max) {
 				p.row0 = row0;

@@ -68,6 +68,10 @@ namespace ugsdr_gpu {
 	struct RuntimeFft {
 		static constexpr int N = 0;
 		static constexpr bool kHooked = false;
+		static constexpr int kPasses = 0;
+		static constexpr bool kRowsCompact = false;
+		static constexpr int kRowsMaxThreads = 256;
+		static constexpr int kRowsMinBlocks = 3;
 		__device__ static FftPlanDev prepare(const FftPlanDev& plan, void* dst) { return plan_in_smem(plan, dst, plan.n); }
 		template <bool INV>
 		__device__ static float2* run(float2* a, float2* b, const FftPlanDev& plan, int batch, int ld) {
@@ -286,8 +290,13 @@ namespace ugsdr_gpu {
 	};
 
 	// grid: rows * K * ceil(N1 / rw)
+	// a compact plan (hooked, two passes) gathers pass 0 from global memory:
+	// one shared tile, and more CTAs per SM to hide the gathers' latency
+	template <class F>
+	constexpr bool rows_one_tile() { return F::kRowsCompact; }
+
 	template <class F2>
-	__global__ void __launch_bounds__(256, 3) inv_rows_kernel(BatchedParams p) {
+	__global__ void __launch_bounds__(F2::kRowsMaxThreads, F2::kRowsMinBlocks) inv_rows_kernel(BatchedParams p) {
 		extern __shared__ float2 smem[];
 		const AcqParams& q = p.base;
 		const int n1 = p.n1, n2 = fft_n<F2>(p.n2), n = q.n;
@@ -303,8 +312,8 @@ namespace ugsdr_gpu {
 		const float2* x = q.spectra + (static_cast<size_t>(d) * q.k_blocks + blk) * n + static_cast<size_t>(r0) * n2;
 		const float2* code = q.codes[c] + static_cast<size_t>(r0) * n2;
 		float2* a = smem;
-		float2* b = smem + p.rw * n2;
-		const FftPlanDev p2 = F2::prepare(p.p2, smem + 2 * p.rw * n2);
+		float2* b = rows_one_tile<F2>() ? smem : smem + p.rw * n2;
+		const FftPlanDev p2 = F2::prepare(p.p2, smem + (rows_one_tile<F2>() ? 1 : 2) * p.rw * n2);
 		const int half = n / 2;
 		const float inv_n2f = 1.0f / static_cast<float>(n2);
 		if constexpr (F2::kHooked) {

@@ -177,6 +177,13 @@ namespace ugsdr_gpu {
 		static_assert(radix_product<Rs...>() == N_, "radices must multiply to N");
 		static constexpr int N = N_;
 		static constexpr bool kHooked = true;  // kernels fuse their producer/consumer into the first/last pass
+		static constexpr int kPasses = sizeof...(Rs);
+		// inverse row kernel launch bounds: a hooked two-pass plan whose widest
+		// pass over 8 rows fits 224 threads runs one shared tile and four CTAs
+		// per SM (72 registers), other plans two tiles and three CTAs
+		static constexpr bool kRowsCompact = kPasses == 2 && 8 * (N_ / radix_min<Rs...>()) <= 224;
+		static constexpr int kRowsMaxThreads = kRowsCompact ? 224 : 256;
+		static constexpr int kRowsMinBlocks = kRowsCompact ? 4 : 3;
 		// most butterflies of one pass over `batch` transforms
 		static constexpr int most_butterflies(int batch) { return batch * (N_ / radix_min<Rs...>()); }
 		static_assert(tables_size<1, Rs...>() <= N_, "pass tables fit the N-entry table space");
@@ -208,6 +215,9 @@ namespace ugsdr_gpu {
 	template <int N_, int... Rs>
 	struct StaticFftPlain : StaticFft<N_, Rs...> {
 		static constexpr bool kHooked = false;
+		static constexpr bool kRowsCompact = false;
+		static constexpr int kRowsMaxThreads = 256;
+		static constexpr int kRowsMinBlocks = 3;
 	};
 
 	// a load hook for plans that read their first pass from shared memory
