@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define UGSDR_CUDA_ABI_VERSION 4
+#define UGSDR_CUDA_ABI_VERSION 5
 
 enum ugsdr_status {
 	UGSDR_OK = 0,
@@ -380,6 +380,60 @@ int ugsdr_track_destroy(ugsdr_track_bank* bank);
 int ugsdr_track_refine(ugsdr_ctx* ctx, ugsdr_track_channel* channels, int n_channels, const float* codes,
 	const int* code_lens, int n_codes, int code_len_max, const void* samples, int sample_type, int samples_on_device,
 	size_t n_samples, int* accepted, int* offsets);
+
+/* --------------------------------------------- interference mitigation */
+/* The antijamming stage the digital front end runs after resampling when
+ * mitigation is enabled (src/dfe/dfe.hpp:199-202). */
+
+/* ShortTimeFourierTransform<SequentialStft>::Transform(src, window_length,
+ * overlap_length) (src/math/stft.hpp:19-21, 42-61): column i is samples
+ * [i * hop, i * hop + window_length), hop = window_length - overlap_length,
+ * times the periodic Hann window 0.5 (1 - cos(2 pi j / window_length)),
+ * forward unnormalised DFT; n_columns = (n - overlap_length) / hop.
+ * out_iq (may be NULL: count only) receives n_columns x window_length
+ * complex.  Needs n >= window_length > overlap_length >= 0.  The reference's
+ * defaults are 128 and 96. */
+int ugsdr_stft(ugsdr_ctx* ctx, const float* in_iq, size_t n, int window_length, int overlap_length, float* out_iq,
+	size_t* n_columns);
+/* The container-of-containers overload, OverlapAndAdd (stft.hpp:63-75):
+ * each column's inverse DFT scaled 2 / window_length (the reference's FFTW
+ * inverse) added at i * hop into window_length + (n_columns - 1) * hop
+ * samples, in column order. */
+int ugsdr_istft(ugsdr_ctx* ctx, const float* in_iq, size_t n_columns, int window_length, int overlap_length,
+	float* out_iq);
+
+/* JammingDetector::DetectionResult::InterferenceType
+ * (src/antijamming/jamming_detection.hpp:30-34) */
+enum ugsdr_interference_type {
+	UGSDR_INTERFERENCE_NONE = 0,
+	UGSDR_INTERFERENCE_NARROWBAND = 1,
+	UGSDR_INTERFERENCE_WIDEBAND = 2
+};
+/* JammingDetector::DetectionResult (jamming_detection.hpp:29-48) */
+typedef struct ugsdr_jamming_detection {
+	int type;                /* ugsdr_interference_type */
+	int frequency_bin;       /* STFT bin (of 128) */
+	double frequency;        /* Hz: frequency_bin * fs / 128 */
+	double jammer_to_noise;  /* candidate peak / sigma, averaged over the columns */
+} ugsdr_jamming_detection;
+
+/* JammingDetector(fs).Process(src) (jamming_detection.hpp:196-201): STFT
+ * (128 / 96), per column the 8 strongest bins (each nulled +-3 bins after it
+ * is taken) kept when peak / sigma of the nulled magnitudes >= 6, then the
+ * occupation analysis (AnalyzeStftData, 130-189).  iq: n complex samples,
+ * host or (samples_on_device) device memory.  Up to `cap` detections go to
+ * `out`; *n_detections receives their count. */
+int ugsdr_jamming_detect(ugsdr_ctx* ctx, const float* iq, size_t n, double fs, int samples_on_device,
+	ugsdr_jamming_detection* out, int cap, int* n_detections);
+/* JammingSuppressionEngine<complex<float>>(fs).Process(src_dst)
+ * (src/antijamming/jse.hpp:89-102), in place: no detection leaves the
+ * samples unchanged; narrowband detections only null +-128 bins of the
+ * whole-signal DFT around each jammer (inverse scaled 2 / n); any wideband
+ * detection zeroes every STFT bin with |.| >= 20 and resynthesises by
+ * OverlapAndAdd, truncated or zero-padded to n.  Detections as for
+ * ugsdr_jamming_detect. */
+int ugsdr_jamming_suppress(ugsdr_ctx* ctx, float* iq, size_t n, double fs, int samples_on_device,
+	ugsdr_jamming_detection* out, int cap, int* n_detections);
 
 /* ------------------------------------------------------------ serving */
 /* Continuous-batching acquisition server.  A worker thread admits queued jobs

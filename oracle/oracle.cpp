@@ -338,6 +338,163 @@ namespace oracle {
 			b += sig[first_len + i] * full_code[second_phase + i];
 		return AddWithPhase(a, b, std::fmod(phase, static_cast<double>(samples_per_ms)) / samples_per_ms);
 	}
+
+	// ------------------------------------------------ interference mitigation
+	// SequentialStft::SplitIntoColumns (math/stft.hpp:34-61): column i =
+	// x[i hop, i hop + w) times the periodic Hann window (double, stored as T)
+	// through std::multiplies<complex<T>>, forward DFT.
+	template <typename T>
+	std::vector<std::vector<std::complex<T>>> Stft(const std::complex<T>* x, std::size_t n, std::size_t w, std::size_t overlap) {
+		const std::size_t hop = w - overlap;
+		const std::size_t cols = (n - overlap) / hop;
+		std::vector<T> win(w);
+		for (std::size_t i = 0; i < w; ++i)
+			win[i] = static_cast<T>(0.5 * (1 - std::cos(2.0 * kPi * static_cast<double>(i) / static_cast<double>(w))));
+		std::vector<std::vector<std::complex<T>>> dst(cols, std::vector<std::complex<T>>(w));
+		for (std::size_t c = 0; c < cols; ++c) {
+			std::vector<std::complex<T>> v(w);
+			for (std::size_t i = 0; i < w; ++i)
+				v[i] = x[c * hop + i] * std::complex<T>(win[i]);
+			DftC2c(v.data(), dst[c].data(), w, false);
+		}
+		return dst;
+	}
+
+	// OverlapAndAdd (math/stft.hpp:63-75): inverse DFTs (2/w scaled) summed at i hop
+	template <typename T>
+	std::vector<std::complex<T>> OverlapAdd(const std::vector<std::vector<std::complex<T>>>& cols, std::size_t w, std::size_t overlap) {
+		const std::size_t hop = w - overlap;
+		std::vector<std::complex<T>> dst(w + (cols.size() - 1) * hop);
+		std::vector<std::complex<T>> inv(w);
+		for (std::size_t i = 0; i < cols.size(); ++i) {
+			DftC2c(cols[i].data(), inv.data(), w, true);
+			for (std::size_t j = 0; j < w; ++j)
+				dst[i * hop + j] += inv[j];
+		}
+		return dst;
+	}
+
+	struct JamCandidate {
+		std::size_t bin;
+		double frequency;
+		double jn;
+	};
+	struct JamDetection {
+		int type;  // 1 narrowband, 2 wideband
+		std::size_t bin;
+		double frequency;
+		double jn;
+	};
+
+	// JammingDetector::IntermediateDetection (antijamming/jamming_detection.hpp:
+	// 113-128) with its NullRegion (101-110): 8 rounds of first max then +-3
+	// bins nulled, J/N against the sigma of what is left, J/N < 6 erased.
+	template <typename T>
+	std::vector<std::vector<JamCandidate>> JamIntermediate(const std::vector<std::vector<std::complex<T>>>& stft, double fs) {
+		std::vector<std::vector<JamCandidate>> out(stft.size());
+		for (std::size_t c = 0; c < stft.size(); ++c) {
+			const std::size_t w = stft[c].size();
+			std::vector<T> mag(w);
+			for (std::size_t k = 0; k < w; ++k)
+				mag[k] = std::abs(stft[c][k]);
+			auto& cand = out[c];
+			for (int r = 0; r < 8; ++r) {
+				const std::size_t index = MaxIndex(mag.data(), w);
+				cand.push_back({index, static_cast<double>(index) * fs / static_cast<double>(w), static_cast<double>(mag[index])});
+				const std::size_t start = (index - 3 + w) % w;
+				std::size_t finish = (index + 3 + w) % w;
+				if (finish < start)
+					finish += w;
+				for (std::size_t i = start; i <= finish; ++i)
+					mag[i % w] = 0;
+			}
+			T mean{}, sd{};
+			MeanStd(mag.data(), w, &mean, &sd);
+			for (auto& el : cand)
+				el.jn /= sd;
+			cand.erase(std::remove_if(cand.begin(), cand.end(), [](const JamCandidate& v) { return v.jn < 6.0; }), cand.end());
+		}
+		return out;
+	}
+
+	// AnalyzeStftData (jamming_detection.hpp:130-189)
+	std::vector<JamDetection> JamAnalyze(const std::vector<std::vector<JamCandidate>>& inter) {
+		std::vector<JamDetection> dst;
+		std::size_t mean_jammers = 0;
+		for (auto& el : inter)
+			mean_jammers += el.size();
+		mean_jammers /= inter.size();
+		for (std::size_t i = 0; i < mean_jammers; ++i) {
+			std::map<double, std::pair<double, JamCandidate>> occ;
+			double quantity = 0;
+			for (auto& el : inter) {
+				if (el.size() <= i)
+					continue;
+				auto& slot = occ[el[i].frequency];
+				slot.first += 1;
+				slot.second.frequency = el[i].frequency;
+				slot.second.bin = el[i].bin;
+				slot.second.jn += el[i].jn;
+				++quantity;
+			}
+			for (auto& kv : occ) {
+				kv.second.first /= quantity;
+				kv.second.second.jn /= quantity;
+			}
+			std::size_t cnt_wideband = 0;
+			const JamCandidate* wide = &occ.begin()->second.second;
+			for (auto& kv : occ) {
+				const double probability = kv.second.first;
+				if (probability >= 0.9) {
+					dst.push_back({1, kv.second.second.bin, kv.second.second.frequency, kv.second.second.jn});
+					break;
+				}
+				if (probability >= 0.9 / static_cast<double>(occ.size())) {
+					++cnt_wideband;
+					wide = &kv.second.second;
+				}
+			}
+			if (cnt_wideband >= static_cast<std::size_t>(occ.size() * 0.9))
+				dst.push_back({2, wide->bin, wide->frequency, wide->jn});
+		}
+		return dst;
+	}
+
+	// JammingSuppressionEngine::Process (antijamming/jse.hpp:89-102) in place
+	template <typename T>
+	std::vector<JamDetection> JamProcess(std::complex<T>* x, std::size_t n, double fs, bool suppress) {
+		auto stft = Stft(x, n, 128, 96);
+		const auto det = JamAnalyze(JamIntermediate(stft, fs));
+		if (!suppress || det.empty())
+			return det;
+		const bool wideband = std::any_of(det.begin(), det.end(), [](const JamDetection& d) { return d.type == 2; });
+		if (!wideband) {
+			// FilterInFreqencyDomain (jse.hpp:61-68) with NullRegion (50-59)
+			std::vector<std::complex<T>> spec(n);
+			DftC2c(x, spec.data(), n, false);
+			for (auto& d : det) {
+				const auto idx = static_cast<std::size_t>(d.frequency / fs * static_cast<double>(n));
+				std::ptrdiff_t start = static_cast<std::ptrdiff_t>(idx) - 128;
+				std::ptrdiff_t finish = static_cast<std::ptrdiff_t>(idx) + 128;
+				start += static_cast<std::ptrdiff_t>(n);
+				if (finish < start)
+					finish += static_cast<std::ptrdiff_t>(n);
+				for (std::ptrdiff_t i = start; i <= finish; ++i)
+					spec[static_cast<std::size_t>(i) % n] = 0;
+			}
+			DftC2c(spec.data(), x, n, true);
+			return det;
+		}
+		// FilterWideband (jse.hpp:70-87)
+		for (auto& col : stft)
+			for (auto& el : col)
+				if (std::abs(el) >= 20.0)
+					el = 0;
+		auto y = OverlapAdd(stft, 128, 96);
+		y.resize(n);
+		std::copy(y.begin(), y.end(), x);
+		return det;
+	}
 }
 
 using namespace oracle;
@@ -445,4 +602,34 @@ void orc_acquire_many_f32(const float* iq, std::size_t n_total, std::size_t n, s
 		t.join();
 }
 
+
+// SequentialStft split: returns the column count, columns to out when non-null
+std::size_t orc_stft_f32(const float* iq, std::size_t n, int w, int overlap, float* out) {
+	const auto cols = Stft(reinterpret_cast<const std::complex<float>*>(iq), n, static_cast<std::size_t>(w), static_cast<std::size_t>(overlap));
+	if (out)
+		for (std::size_t c = 0; c < cols.size(); ++c)
+			std::memcpy(out + 2 * c * w, cols[c].data(), sizeof(float) * 2 * w);
+	return cols.size();
+}
+// OverlapAndAdd of n_cols columns of w complex samples
+void orc_istft_f32(const float* cols_iq, std::size_t n_cols, int w, int overlap, float* out) {
+	std::vector<std::vector<std::complex<float>>> cols(n_cols, std::vector<std::complex<float>>(w));
+	for (std::size_t c = 0; c < n_cols; ++c)
+		std::memcpy(cols[c].data(), cols_iq + 2 * c * w, sizeof(float) * 2 * w);
+	const auto y = OverlapAdd(cols, static_cast<std::size_t>(w), static_cast<std::size_t>(overlap));
+	std::memcpy(out, y.data(), sizeof(float) * 2 * y.size());
+}
+// JammingDetector::Process (suppress = 0) or JammingSuppressionEngine::Process
+// (suppress = 1, iq modified in place); returns the detection count
+int orc_jamming_process_f32(float* iq, std::size_t n, double fs, int suppress, int* types, long* bins, double* freqs,
+	double* jn, int cap) {
+	const auto det = JamProcess(reinterpret_cast<std::complex<float>*>(iq), n, fs, suppress != 0);
+	for (int i = 0; i < cap && i < static_cast<int>(det.size()); ++i) {
+		types[i] = det[i].type;
+		bins[i] = static_cast<long>(det[i].bin);
+		freqs[i] = det[i].frequency;
+		jn[i] = det[i].jn;
+	}
+	return static_cast<int>(det.size());
+}
 }

@@ -48,6 +48,9 @@ def load() -> C.CDLL:
         "orc_acquire_f32": [vp, sz, sz, sz, vp, d, d, d, d, d, i, i, i, i, vp, vp, vp],
         "orc_acquire_f64": [vp, sz, sz, sz, vp, d, d, d, d, d, i, i, i, i, vp, vp, vp],
         "orc_acquire_many_f32": [vp, sz, sz, sz, vp, sz, d, d, d, d, d, i, i, i, i, i, vp],
+        "orc_stft_f32": [vp, sz, i, i, vp],
+        "orc_istft_f32": [vp, sz, i, i, vp],
+        "orc_jamming_process_f32": [vp, sz, d, i, vp, vp, vp, vp, i],
     }
     for name, args in sigs.items():
         fn = getattr(lib, name)
@@ -57,6 +60,8 @@ def load() -> C.CDLL:
     lib.orc_reshape_sum_c32.restype = i
     lib.orc_max_index_f32.restype = sz
     lib.orc_resample_c32.restype = sz
+    lib.orc_stft_f32.restype = sz
+    lib.orc_jamming_process_f32.restype = i
     _lib = lib
     return lib
 
@@ -236,3 +241,37 @@ def track_refine(x: np.ndarray, channels: list[dict], codes: list[np.ndarray]):
         phases.append(ch["code_phase"] + off if ok else ch["code_phase"])
         levels.append(rec["level"])
     return acc, offs, phases, levels
+
+
+def stft(x: np.ndarray, window: int = 128, overlap: int = 96) -> np.ndarray:
+    """SequentialStft split (math/stft.hpp:42-61): (columns, window) complex64."""
+    x = np.ascontiguousarray(x, np.complex64)
+    lib = load()
+    cols = lib.orc_stft_f32(_p(x), x.size, window, overlap, None)
+    out = np.empty((cols, window), np.complex64)
+    lib.orc_stft_f32(_p(x), x.size, window, overlap, _p(out))
+    return out
+
+
+def istft(columns: np.ndarray, overlap: int = 96) -> np.ndarray:
+    """OverlapAndAdd (math/stft.hpp:63-75)."""
+    columns = np.ascontiguousarray(columns, np.complex64)
+    n_cols, w = columns.shape
+    out = np.empty(w + (n_cols - 1) * (w - overlap), np.complex64)
+    load().orc_istft_f32(_p(columns), n_cols, w, overlap, _p(out))
+    return out
+
+
+def jamming(x: np.ndarray, fs: float, suppress: bool = True):
+    """JammingDetector::Process (suppress False) or JammingSuppressionEngine::
+    Process (antijamming/jse.hpp:89-102) on a copy of x: (detections as
+    (type, bin, frequency, J/N) tuples, output samples)."""
+    y = np.array(x, np.complex64, copy=True)
+    types = np.zeros(64, np.int32)
+    bins = np.zeros(64, np.int64)
+    freqs = np.zeros(64)
+    jn = np.zeros(64)
+    cnt = load().orc_jamming_process_f32(_p(y), y.size, fs, 1 if suppress else 0, _p(types), _p(bins), _p(freqs),
+                                         _p(jn), 64)
+    det = [(int(types[i]), int(bins[i]), float(freqs[i]), float(jn[i])) for i in range(min(cnt, 64))]
+    return det, y

@@ -30,6 +30,8 @@
 #include "resample/resampler.hpp"
 #include "resample/upsampler.hpp"
 #include "helpers/NtlabPackedSpan.hpp"
+#include "antijamming/jse.hpp"
+#include "math/stft.hpp"
 #include "signal_parameters.hpp"
 
 #include <complex>
@@ -296,5 +298,46 @@ void ref_nt1065_decode(const unsigned char* bytes, std::size_t n, int channel, f
 	case 2: { auto s = ugsdr::NtlabPackedSpan<2, float>(src, n); std::copy(s.begin(), s.end(), dst); break; }
 	default: { auto s = ugsdr::NtlabPackedSpan<0, float>(src, n); std::copy(s.begin(), s.end(), dst); break; }
 	}
+}
+
+// ShortTimeFourierTransform<SequentialStft>::Transform(src) with the default
+// 128-sample window and 96-sample overlap (math/stft.hpp:19-21, 42-61):
+// returns the column count; columns are written when cap allows.
+long ref_stft_f32(const float* iq, std::size_t n, float* out, std::size_t cap_columns) {
+	const auto v = ToComplex(iq, n);
+	const auto cols = ugsdr::ShortTimeFourierTransform<ugsdr::SequentialStft>::Transform(v);
+	if (out && cols.size() <= cap_columns)
+		for (std::size_t i = 0; i < cols.size(); ++i)
+			std::memcpy(out + 2 * i * cols[i].size(), cols[i].data(), sizeof(float) * 2 * cols[i].size());
+	return static_cast<long>(cols.size());
+}
+
+// the container-of-containers overload: OverlapAndAdd (math/stft.hpp:63-75)
+void ref_istft_f32(const float* cols_iq, std::size_t n_columns, float* out) {
+	std::vector<std::vector<std::complex<float>>> cols(n_columns);
+	for (std::size_t i = 0; i < n_columns; ++i)
+		cols[i] = ToComplex(cols_iq + 2 * i * 128, 128);
+	const auto r = ugsdr::ShortTimeFourierTransform<ugsdr::SequentialStft>::Transform(cols);
+	FromComplex(r, out);
+}
+
+// JammingSuppressionEngine<complex<float>>(fs).Process(src_dst) in place
+// (antijamming/jse.hpp:89-102); the detections (jamming_detection.hpp:29-48)
+// go out as type / bin / frequency / J/N; returns their count.
+int ref_jamming_process_f32(float* iq, std::size_t n, double fs, int* types, long* bins, double* freqs, double* jn,
+	int cap) {
+	auto v = ToComplex(iq, n);
+	ugsdr::JammingSuppressionEngine<std::complex<float>> engine(fs);
+	engine.Process(v);
+	FromComplex(v, iq);
+	const auto& det = engine.GetDetectionResults();
+	const int count = static_cast<int>(det.size());
+	for (int i = 0; i < count && i < cap; ++i) {
+		types[i] = static_cast<int>(det[i].interference_type);
+		bins[i] = static_cast<long>(det[i].frequency_bin);
+		freqs[i] = det[i].frequency;
+		jn[i] = det[i].jammer_to_noise;
+	}
+	return count;
 }
 }

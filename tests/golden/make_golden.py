@@ -58,6 +58,11 @@ def ref_lib(ref_dir: str) -> C.CDLL:
     lib.ref_bbp_read.argtypes = [C.c_char_p, d, d, sz, vp]
     lib.ref_bbp_read.restype = C.c_long
     lib.ref_nt1065_decode.argtypes = [vp, sz, i, vp]
+    lib.ref_stft_f32.argtypes = [vp, sz, vp, sz]
+    lib.ref_stft_f32.restype = C.c_long
+    lib.ref_istft_f32.argtypes = [vp, sz, vp]
+    lib.ref_jamming_process_f32.argtypes = [vp, sz, d, vp, vp, vp, vp, i]
+    lib.ref_jamming_process_f32.restype = i
     return lib
 
 
@@ -240,6 +245,71 @@ def packed(lib, ref_dir: str) -> dict[str, np.ndarray]:
     return out
 
 
+JAMMING_CASES = {  # name -> (fs, n, seed); signals built by jamming_input()
+    "clean": (2.048e6, 2048, 11),
+    "tone": (2.048e6, 2048, 12),
+    "two_tones": (2.048e6, 2048, 13),
+    "loud": (2.048e6, 2048, 14),
+    "narrow": (2.048e6, 2048, 15),
+    "narrow_4mhz": (4e6, 4000, 16),
+}
+
+
+def jamming_input(name: str, fs: float, n: int, seed: int) -> np.ndarray:
+    """Noise (sigma 0.5 per part) plus the case's interferers: CW tones, a
+    loud one over loud noise, and for the narrowband cases a weak steady tone
+    with a stronger tone gated on in one 128-sample slot of twenty."""
+    rng = np.random.default_rng(seed)
+    t = np.arange(n) / fs
+    x = rng.normal(0, 0.5, n) + 1j * rng.normal(0, 0.5, n)
+    if name == "tone":
+        x += 10 * np.exp(2j * np.pi * 0.5e6 * t)
+    elif name == "two_tones":
+        x += 10 * np.exp(2j * np.pi * 0.5e6 * t) + 5 * np.exp(2j * np.pi * -0.7e6 * t)
+    elif name == "loud":
+        x = 40 * x + 200 * np.exp(2j * np.pi * 0.3e6 * t)
+    elif name.startswith("narrow"):
+        gate = (np.arange(n) // 128) % 20 == 0
+        x += 10 * np.exp(2j * np.pi * 0.25e6 * t) + gate * 30 * np.exp(2j * np.pi * 0.9e6 * t)
+    return x.astype(np.complex64)
+
+
+def jamming(lib) -> dict[str, np.ndarray]:
+    """JammingSuppressionEngine<complex<float>>::Process (in place) on seeded
+    signals through the reference's own code, plus its STFT (128 / 96) and
+    OverlapAndAdd on the tone case.  In the cases the wideband filter runs
+    on, every STFT magnitude stays at least 0.1 % away from its threshold 20,
+    so an FP32 device transform takes the same zeroing decisions."""
+    out = {}
+    for name, (fs, n, seed) in JAMMING_CASES.items():
+        x = jamming_input(name, fs, n, seed)
+        iq = np.ascontiguousarray(x).view(np.float32).copy()
+        types = np.zeros(64, np.int32)
+        bins = np.zeros(64, np.int64)
+        freqs = np.zeros(64)
+        jn = np.zeros(64)
+        cnt = lib.ref_jamming_process_f32(p(iq), n, fs, p(types), p(bins), p(freqs), p(jn), 64)
+        cols = lib.ref_stft_f32(p(np.ascontiguousarray(x).view(np.float32)), n, None, 0)
+        spec = np.zeros(cols * 128 * 2, np.float32)
+        lib.ref_stft_f32(p(np.ascontiguousarray(x).view(np.float32)), n, p(spec), cols)
+        mag = np.abs(spec.view(np.complex64))
+        if 2 in types[:cnt]:  # the wideband filter zeroes |.| >= 20
+            assert np.min(np.abs(mag - 20.0)) > 0.02, (name, np.min(np.abs(mag - 20.0)))
+        out[f"{name}_in"] = x
+        out[f"{name}_out"] = iq.view(np.complex64)
+        out[f"{name}_fs"] = np.array(fs)
+        out[f"{name}_types"] = types[:cnt]
+        out[f"{name}_bins"] = bins[:cnt]
+        out[f"{name}_freqs"] = freqs[:cnt]
+        out[f"{name}_jn"] = jn[:cnt]
+        if name == "tone":
+            out["stft_cols"] = spec.view(np.complex64).reshape(cols, 128)
+            syn = np.zeros(2 * (128 + (cols - 1) * 32), np.float32)
+            lib.ref_istft_f32(p(spec), cols, p(syn))
+            out["istft"] = syn.view(np.complex64)
+    return out
+
+
 def main() -> None:
     ref_dir = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     lib = ref_lib(ref_dir)
@@ -250,6 +320,7 @@ def main() -> None:
     a = acquisition(lib, c)
     np.savez_compressed(HERE / "acq_gps_l1_4mhz.npz", **a)
     np.savez_compressed(HERE / "packed.npz", **packed(lib, ref_dir))
+    np.savez_compressed(HERE / "jamming.npz", **jamming(lib))
     for f in sorted(HERE.glob("*.npz")):
         print(f.name, f.stat().st_size)
 

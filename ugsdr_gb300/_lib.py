@@ -10,7 +10,7 @@ from pathlib import Path
 
 LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libugsdr_cuda.so"
 
-ABI_VERSION = 4  # UGSDR_CUDA_ABI_VERSION the structs below mirror
+ABI_VERSION = 5  # UGSDR_CUDA_ABI_VERSION the structs below mirror
 
 OK = 0
 E_INVALID = -1
@@ -110,6 +110,13 @@ class TrackOutput(C.Structure):
 
 SERVE_FIFO, SERVE_RESPONSE_RATIO = 0, 1
 
+INTERFERENCE_NONE, INTERFERENCE_NARROWBAND, INTERFERENCE_WIDEBAND = 0, 1, 2
+
+
+class JammingDetection(C.Structure):
+    _fields_ = [("type", C.c_int), ("frequency_bin", C.c_int), ("frequency", C.c_double),
+                ("jammer_to_noise", C.c_double)]
+
 
 class ServerConfig(C.Structure):
     _fields_ = [("max_inflight", C.c_int), ("memory_budget", C.c_size_t), ("queue_capacity", C.c_int),
@@ -158,6 +165,10 @@ SIGNATURES = {
     "ugsdr_track_destroy": (_i, [_vp]),
     "ugsdr_track_refine": (_i, [_vp, C.POINTER(TrackChannel), _i, _vp, C.POINTER(_i), _i, _i, _vp, _i, _i, _sz,
                                 C.POINTER(_i), C.POINTER(_i)]),
+    "ugsdr_stft": (_i, [_vp, _vp, _sz, _i, _i, _vp, C.POINTER(_sz)]),
+    "ugsdr_istft": (_i, [_vp, _vp, _sz, _i, _i, _vp]),
+    "ugsdr_jamming_detect": (_i, [_vp, _vp, _sz, _d, _i, C.POINTER(JammingDetection), _i, C.POINTER(_i)]),
+    "ugsdr_jamming_suppress": (_i, [_vp, _vp, _sz, _d, _i, C.POINTER(JammingDetection), _i, C.POINTER(_i)]),
     "ugsdr_server_create": (_i, [_vp, C.POINTER(ServerConfig), C.POINTER(_vp)]),
     "ugsdr_server_submit": (_i, [_vp, C.POINTER(AcqJob), C.POINTER(_u64)]),
     "ugsdr_server_poll": (_i, [_vp, _u64, C.POINTER(AcqResult), C.POINTER(_i)]),

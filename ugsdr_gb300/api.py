@@ -159,6 +159,55 @@ class Context:
         self._check(self.lib.ugsdr_mix(self.h, _ptr(iq), iq.size, fs, frequency, phase))
         return iq
 
+    # ------------------------------------------------ interference stage
+    def stft(self, x: np.ndarray, window_length: int = 128, overlap_length: int = 96) -> np.ndarray:
+        """ShortTimeFourierTransform<SequentialStft>::Transform(src, window, overlap):
+        (columns, window_length) complex64."""
+        x = np.ascontiguousarray(x, np.complex64)
+        cols = C.c_size_t()
+        self._check(self.lib.ugsdr_stft(self.h, _ptr(x), x.size, window_length, overlap_length, None, C.byref(cols)))
+        out = np.empty((cols.value, window_length), np.complex64)
+        self._check(self.lib.ugsdr_stft(self.h, _ptr(x), x.size, window_length, overlap_length, _ptr(out), C.byref(cols)))
+        return out
+
+    def istft(self, columns: np.ndarray, overlap_length: int = 96) -> np.ndarray:
+        """The container-of-containers Transform overload (OverlapAndAdd)."""
+        columns = np.ascontiguousarray(columns, np.complex64)
+        n_cols, w = columns.shape
+        out = np.empty(w + (n_cols - 1) * (w - overlap_length), np.complex64)
+        self._check(self.lib.ugsdr_istft(self.h, _ptr(columns), n_cols, w, overlap_length, _ptr(out)))
+        return out
+
+    @staticmethod
+    def _detections(buf, count: int) -> list[dict]:
+        return [{"type": buf[i].type, "frequency_bin": buf[i].frequency_bin, "frequency": buf[i].frequency,
+                 "jammer_to_noise": buf[i].jammer_to_noise} for i in range(min(count, len(buf)))]
+
+    def jamming_detect(self, x, fs: float, n: int | None = None) -> list[dict]:
+        """JammingDetector(fs).Process(src): detection results.  `x`: complex64
+        numpy array, or a device pointer (int) to `n` complex samples."""
+        buf = (L.JammingDetection * 64)()
+        cnt = C.c_int()
+        if isinstance(x, int):
+            self._check(self.lib.ugsdr_jamming_detect(self.h, C.c_void_p(x), n, fs, 1, buf, 64, C.byref(cnt)))
+        else:
+            x = np.ascontiguousarray(x, np.complex64)
+            self._check(self.lib.ugsdr_jamming_detect(self.h, _ptr(x), x.size, fs, 0, buf, 64, C.byref(cnt)))
+        return self._detections(buf, cnt.value)
+
+    def jamming_suppress(self, x, fs: float, n: int | None = None) -> list[dict]:
+        """JammingSuppressionEngine<complex<float>>(fs).Process(src_dst), in place
+        on a complex64 array (or on `n` samples at a device pointer); returns
+        the detections."""
+        buf = (L.JammingDetection * 64)()
+        cnt = C.c_int()
+        if isinstance(x, int):
+            self._check(self.lib.ugsdr_jamming_suppress(self.h, C.c_void_p(x), n, fs, 1, buf, 64, C.byref(cnt)))
+        else:
+            assert x.dtype == np.complex64 and x.flags.c_contiguous
+            self._check(self.lib.ugsdr_jamming_suppress(self.h, _ptr(x), x.size, fs, 0, buf, 64, C.byref(cnt)))
+        return self._detections(buf, cnt.value)
+
     def dft(self, x: np.ndarray, inverse: bool = False) -> np.ndarray:
         x = np.ascontiguousarray(x, np.complex64)
         out = np.empty_like(x)

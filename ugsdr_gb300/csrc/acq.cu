@@ -169,9 +169,9 @@ namespace ugsdr_gpu {
 
 		// Sub-transforms per CTA: 8 columns/rows (64-byte runs per k1 row) unless
 		// the tiles would exceed a third of shared memory.
-		// inv_cols holds three column tiles (input, work, prefetch) and an
-		// accumulator and runs two CTAs per SM; row kernels hold two row tiles
-		// and run three.
+		// Sized for inv_cols with three column tiles (input, work, prefetch) and
+		// an accumulator at two CTAs per SM (a compact plan drops the prefetch
+		// tile and runs three), and for row kernels with two row tiles at three.
 		void tile_shape(ugsdr_ctx* ctx, const LargePlan& lp, int& cw, int& rw) {
 			const size_t ld = static_cast<size_t>(lp.n1 | 1);
 			cw = 8;
@@ -198,10 +198,16 @@ namespace ugsdr_gpu {
 			return p;
 		}
 
-		// fwd_cols: two tiles; inv_cols: input, work and prefetch tiles + accumulator
-		size_t smem_cols(const BatchedParams& p, bool inverse) {
-			return (inverse ? 3 * sizeof(float2) + sizeof(float) : 2 * sizeof(float2)) * static_cast<size_t>(p.cw) * p.ld1
-				+ sizeof(float2) * p.n1 + 16;  // + the N1-point twiddle table
+		// fwd_cols: two tiles + the N1-point twiddle table
+		size_t smem_cols(const BatchedParams& p) {
+			return 2 * sizeof(float2) * static_cast<size_t>(p.cw) * p.ld1 + sizeof(float2) * p.n1 + 16;
+		}
+		// inv_cols: input, work and (not for a compact plan) prefetch tiles +
+		// accumulator + table
+		template <class F>
+		size_t smem_inv_cols(const BatchedParams& p) {
+			return ((F::kColsCompact ? 2 : 3) * sizeof(float2) + sizeof(float)) * static_cast<size_t>(p.cw) * p.ld1
+				+ sizeof(float2) * p.n1 + 16;
 		}
 		// row kernels: two tiles + the N2-point twiddle table
 		size_t smem_rows(const BatchedParams& p, bool) {
@@ -225,7 +231,7 @@ namespace ugsdr_gpu {
 
 		template <typename K>
 		void launch_fwd_cols(ugsdr_ctx* ctx, K kernel, const BatchedParams& p, int items, int threads) {
-			const size_t smem = smem_cols(p, false);
+			const size_t smem = smem_cols(p);
 			set_smem(kernel, smem);
 			kernel<<<items * chunks_of(p.n2, p.cw), threads, smem, ctx->stream>>>(p);
 		}
@@ -325,15 +331,16 @@ namespace ugsdr_gpu {
 			if (s.fold_mode == 2)
 				p.zcg = reinterpret_cast<float2*>(scratch + lay.zcg);
 		}
-		const size_t smem_c = smem_cols(p, true);
 		with_large_ffts(p.n1, p.n2, [&](auto f1, auto f2) {
 			using F1 = decltype(f1);
 			using F2 = decltype(f2);
+			const size_t smem_c = smem_inv_cols<F1>(p);
 			const size_t smem_r = smem_inv_rows<F2>(p);
 			set_smem(inv_rows_kernel<F2>, smem_r);
 			set_smem(inv_cols_kernel<F1>, smem_c);
 			const int t_rows = threads_of<F2>(p.p2, p.rw), t_cols = threads_of<F1>(p.p1, p.cw);
 			require(t_rows <= F2::kRowsMaxThreads, "row kernel needs more threads than its launch bound");
+			require(t_cols <= F1::kColsMaxThreads, "column kernel needs more threads than its launch bound");
 			KernelTimer timer(ctx, "acq_inverse_large");
 			for (int row0 = 0; row0 < s.rows; row0 += r_max) {
 				p.row0 = row0;

@@ -72,6 +72,9 @@ namespace ugsdr_gpu {
 		static constexpr bool kRowsCompact = false;
 		static constexpr int kRowsMaxThreads = 256;
 		static constexpr int kRowsMinBlocks = 3;
+		static constexpr bool kColsCompact = false;
+		static constexpr int kColsMaxThreads = 256;
+		static constexpr int kColsMinBlocks = 2;
 		__device__ static FftPlanDev prepare(const FftPlanDev& plan, void* dst) { return plan_in_smem(plan, dst, plan.n); }
 		template <bool INV>
 		__device__ static float2* run(float2* a, float2* b, const FftPlanDev& plan, int batch, int ld) {
@@ -369,7 +372,7 @@ namespace ugsdr_gpu {
 
 	// grid: rows * ceil(N2 / cw); shared: 3 * cw * ld1 float2 (input, work, prefetch) + cw * ld1 float
 	template <class F1>
-	__global__ void __launch_bounds__(256, 2) inv_cols_kernel(BatchedParams p) {
+	__global__ void __launch_bounds__(F1::kColsMaxThreads, F1::kColsMinBlocks) inv_cols_kernel(BatchedParams p) {
 		extern __shared__ float2 smem[];
 		__shared__ MaxIdx s_max[8];
 		__shared__ double s_sum[8], s_sq[8];
@@ -384,10 +387,11 @@ namespace ugsdr_gpu {
 		const int ld = p.ld1;
 		const int mask = p.cw - 1;
 		const int tile = p.cw * ld;
+		constexpr bool kCompact = F1::kColsCompact;  // no prefetch tile: the next block lands in `in` after pass 0
 		float2* in = smem;
 		float2* work = smem + tile;
 		float2* pre = smem + 2 * tile;
-		float* acc = reinterpret_cast<float*>(smem + 3 * tile);
+		float* acc = reinterpret_cast<float*>(smem + (kCompact ? 2 : 3) * tile);
 		const FftPlanDev p1 = F1::prepare(p.p1, acc + tile);
 		const float inv_n = 1.0f / static_cast<float>(n);
 		const float post = q.one_sided ? 2.0f : 1.0f;
@@ -407,13 +411,23 @@ namespace ugsdr_gpu {
 		for (int blk = 0; blk < q.k_blocks; ++blk) {
 			cp_async_wait_all();
 			__syncthreads();
-			if (blk + 1 < q.k_blocks)
+			if (!kCompact && blk + 1 < q.k_blocks)
 				prefetch(pre, blk + 1);
 			if constexpr (F1::kHooked) {
 				float2* zg = q.fold_mode == 2 ? p.zcg + (static_cast<size_t>(lrow) * q.k_blocks + blk) * m : nullptr;
 				const InvColsEmit emit{acc, ld, q.stat, q.fold_mode, n2, c0, m, inv_n * post,
 					q.fold_mode == 1 ? p.accg + static_cast<size_t>(lrow) * m : nullptr, zg};
 				const NoLoad none{};
+				if constexpr (kCompact) {
+					// the next iteration's first barrier orders this block's last-pass
+					// reads of `work` and writes of `acc` before they are reused
+					auto mid = [&] {
+						if (blk + 1 < q.k_blocks)
+							prefetch(in, blk + 1);
+					};
+					F1::template run_hooked<true, false>(in, work, p1, cw, ld, none, emit, mid);
+					continue;
+				}
 				F1::template run_hooked<true, false>(in, work, p1, cw, ld, none, emit);
 				__syncthreads();
 				float2* t = in;
@@ -452,6 +466,8 @@ namespace ugsdr_gpu {
 			in = pre;
 			pre = t;
 		}
+		if constexpr (kCompact)
+			__syncthreads();  // the last block's accumulation is complete
 		if (q.fold_mode != 0)
 			return;
 		// chunk partial: first max (lowest natural index on ties), sum, sum of squares
@@ -520,7 +536,7 @@ namespace ugsdr_gpu {
 	}
 
 	// folded rows: acc (fold 1) or |complex fold| summed over blocks (fold 2) -> cell; grid: rows
-	__global__ void __launch_bounds__(256) fold_finish_kernel(BatchedParams p) {
+	static __global__ void __launch_bounds__(256) fold_finish_kernel(BatchedParams p) {
 		const AcqParams& q = p.base;
 		const int lrow = blockIdx.x;
 		const int m = q.m;

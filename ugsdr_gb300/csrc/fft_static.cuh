@@ -117,18 +117,25 @@ namespace ugsdr_gpu {
 		}
 	}
 
+	// a between-passes hook that does nothing
+	struct NoMid {
+		__device__ void operator()() const {}
+	};
+
 	template <int N, int NS, bool INV, bool FIRST, int... Rs>
 	struct HookedPasses;
 
 	template <int N, int NS, bool INV, bool FIRST, int R, int... Rest>
 	struct HookedPasses<N, NS, INV, FIRST, R, Rest...> {
-		template <class Load, class Emit>
-		__device__ static void run(float2* a, float2* b, const float2* tw, int batch, int ld, Load& load, Emit& emit) {
+		template <class Load, class Emit, class Mid>
+		__device__ static void run(float2* a, float2* b, const float2* tw, int batch, int ld, Load& load, Emit& emit, Mid& mid) {
 			constexpr bool LAST = sizeof...(Rest) == 0;
 			hooked_pass<N, R, NS, INV, FIRST, LAST>(a, b, tw, batch, ld, load, emit);
 			if constexpr (!LAST) {
 				__syncthreads();
-				HookedPasses<N, NS * R, INV, false, Rest...>::run(b, a, tw + pass_table_size<NS, R>(), batch, ld, load, emit);
+				if constexpr (NS == 1)
+					mid();  // pass 0's input tile is free from here on
+				HookedPasses<N, NS * R, INV, false, Rest...>::run(b, a, tw + pass_table_size<NS, R>(), batch, ld, load, emit, mid);
 			}
 		}
 	};
@@ -184,6 +191,13 @@ namespace ugsdr_gpu {
 		static constexpr bool kRowsCompact = kPasses == 2 && 8 * (N_ / radix_min<Rs...>()) <= 224;
 		static constexpr int kRowsMaxThreads = kRowsCompact ? 224 : 256;
 		static constexpr int kRowsMinBlocks = kRowsCompact ? 4 : 3;
+		// inverse column kernel: a hooked two-pass plan of the same width
+		// prefetches the next block into the input tile once pass 0 has read it
+		// (two tiles + accumulator, three CTAs per SM); other plans keep a third
+		// prefetch tile and run two
+		static constexpr bool kColsCompact = kRowsCompact;
+		static constexpr int kColsMaxThreads = kColsCompact ? 224 : 256;
+		static constexpr int kColsMinBlocks = kColsCompact ? 3 : 2;
 		// most butterflies of one pass over `batch` transforms
 		static constexpr int most_butterflies(int batch) { return batch * (N_ / radix_min<Rs...>()); }
 		static_assert(tables_size<1, Rs...>() <= N_, "pass tables fit the N-entry table space");
@@ -204,9 +218,15 @@ namespace ugsdr_gpu {
 		// Pass 0 reads `a` (or gathers through `load` when FIRST), intermediate
 		// passes ping-pong between the tiles, the last pass emits.  With FIRST and
 		// two radices only one tile (`b`) is used.
+		// `mid()` runs after the barrier that ends pass 0.
+		template <bool INV, bool FIRST, class Load, class Emit, class Mid>
+		__device__ static void run_hooked(float2* a, float2* b, const FftPlanDev& plan, int batch, int ld, Load& load, Emit& emit, Mid& mid) {
+			HookedPasses<N_, 1, INV, FIRST, Rs...>::run(a, b, plan.tw, batch, ld, load, emit, mid);
+		}
 		template <bool INV, bool FIRST, class Load, class Emit>
 		__device__ static void run_hooked(float2* a, float2* b, const FftPlanDev& plan, int batch, int ld, Load& load, Emit& emit) {
-			HookedPasses<N_, 1, INV, FIRST, Rs...>::run(a, b, plan.tw, batch, ld, load, emit);
+			NoMid mid{};
+			run_hooked<INV, FIRST>(a, b, plan, batch, ld, load, emit, mid);
 		}
 	};
 
@@ -218,6 +238,9 @@ namespace ugsdr_gpu {
 		static constexpr bool kRowsCompact = false;
 		static constexpr int kRowsMaxThreads = 256;
 		static constexpr int kRowsMinBlocks = 3;
+		static constexpr bool kColsCompact = false;
+		static constexpr int kColsMaxThreads = 256;
+		static constexpr int kColsMinBlocks = 2;
 	};
 
 	// a load hook for plans that read their first pass from shared memory

@@ -148,6 +148,10 @@ struct ugsdr_ctx {
 	ugsdr_gpu::DevBuf lut;        // float[80] TableMixer sine table
 	ugsdr_gpu::Workspace ws;      // acquisition scratch of the synchronous entry points
 	ugsdr_gpu::DevBuf op_a, op_b, op_c;  // per-op entry staging
+	// interference stage: staged samples, STFT spectra, inverse columns /
+	// whole-signal spectrum, per-column candidates, DFT scratch, window
+	ugsdr_gpu::DevBuf jam_x, jam_s, jam_t, jam_cand, jam_tmp, jam_window;
+	int jam_window_len = 0;
 	int sm_count = 0;
 	size_t smem_optin = 0;
 
@@ -204,6 +208,10 @@ namespace ugsdr_gpu {
 			return UGSDR_E_INVALID;
 		}
 	}
+
+	// complex DFT device to device with the reference's scaling: forward
+	// unnormalised, inverse (v / n) * 2 (ops.cu); `in` and `out` distinct
+	void dft_scaled(ugsdr_ctx* ctx, const float2* in, float2* out, size_t n, bool inverse, DevBuf& tmp);
 
 	// plan accessors (acq.cu)
 	const FftPlanDesc& get_plan(ugsdr_ctx* ctx, int n);

@@ -406,6 +406,14 @@ namespace ugsdr_gpu {
 			note_launch(ctx, 2);
 		}
 	}
+
+	void dft_scaled(ugsdr_ctx* ctx, const float2* in, float2* out, size_t n, bool inverse, DevBuf& tmp) {
+		dft_device(ctx, in, out, n, inverse, tmp);
+		if (inverse) {
+			inverse_scale_kernel<<<blocks_for(n), kT, 0, ctx->stream>>>(out, n, 1);
+			note_launch(ctx);
+		}
+	}
 }
 
 using namespace ugsdr_gpu;
