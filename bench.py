@@ -763,6 +763,147 @@ def run_track(args, world, rank):
     return line
 
 
+# ------------------------------------------------------- interference stage
+JAM_FS = 50e6
+JAM_SECONDS = 0.4
+JAM_BIN = 20  # CW jammer on STFT bin 20 (7.8125 MHz at 50 MHz)
+# algorithmic bytes per sample: the detector reads the samples once and writes
+# 8 rounds x (1 B bin + 8 B J/N) per 32-sample hop; the wideband filter reads
+# and writes them once; the in-place copy back reads and writes them once
+JAM_DETECT_BYTES = 8 + 8 * 9 / 32
+JAM_WIDEBAND_BYTES = 16
+JAM_COPY_BYTES = 16
+
+
+def jamming_capture(dev, seconds=JAM_SECONDS):
+    """Complex float samples at 50 MHz: noise (sigma 0.5 per part) + a CW
+    jammer of amplitude 10 on an STFT bin centre, synthesised on the device
+    from a fixed seed."""
+    import torch
+    n = int(round(seconds * JAM_FS))
+    gen = torch.Generator(device=f"cuda:{dev}")
+    gen.manual_seed(5)
+    x = torch.randn((n, 2), generator=gen, device=f"cuda:{dev}") * 0.5
+    t = torch.arange(n, device=f"cuda:{dev}", dtype=torch.float64)
+    ph = 2 * np.pi * (JAM_BIN / 128) * t
+    x[:, 0] += (10 * torch.cos(ph)).float()
+    x[:, 1] += (10 * torch.sin(ph)).float()
+    return x.contiguous()
+
+
+def jamming_cpu_baseline(x_host, samples=2_000_000):
+    """JammingSuppressionEngine::Process restated in the oracle (FP64-internal
+    FFT, float arithmetic), one thread, on the first `samples` samples."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import pyoracle
+    xs = x_host[:samples]
+    t0 = time.perf_counter()
+    det, _ = pyoracle.jamming(xs, JAM_FS)
+    dt = time.perf_counter() - t0
+    return {"value": len(xs) / dt, "unit": "samples/s", "cores": 1, "kind": "port",
+            "sample": f"{len(xs)} samples (first {len(xs) / JAM_FS * 1e3:.0f} ms) in {dt:.2f}s, "
+                      f"{len(det)} detections (oracle engine, one thread)"}
+
+
+def run_jamming(args, world, rank):
+    """Interference stage: JammingSuppressionEngine<complex<float>>(50 MHz)
+    .Process over 400 ms of samples per step (detect + wideband suppression,
+    in place on the device)."""
+    import torch
+    from ugsdr_gb300 import api
+    if args.impl == "reference" and rank != 0:
+        return None
+    dev = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(dev)
+    pristine = jamming_capture(dev)
+    n = pristine.shape[0]
+    workload = (f"interference stage: JammingSuppressionEngine::Process (STFT 128/96 detection + wideband "
+                f"suppression), complex float {JAM_FS / 1e6:.0f} MHz, {JAM_SECONDS * 1e3:.0f} ms, CW jammer + noise")
+    if args.impl == "reference":
+        xh = pristine.cpu().numpy().view(np.complex64).ravel()
+        vals = [jamming_cpu_baseline(xh) for _ in range(args.warmup + args.steps)][args.warmup:]
+        v = float(np.mean([b["value"] for b in vals]))
+        return {"metric": "interference stage samples/s", "value": v, "unit": "samples/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": n / v * 1e3, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
+                "config": {"workload": workload},
+                "cpu_baseline": {k: vals[-1][k] for k in ("value", "unit", "cores", "kind", "sample")},
+                "e2e": {"value": v, "unit": "samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    ctx = api.Context(dev)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    work = torch.empty_like(pristine)
+    h_pristine = pristine.cpu().numpy().view(np.complex64).ravel().copy()
+    h_work = torch.empty((n, 2), dtype=torch.float32, pin_memory=True).numpy().view(np.complex64).ravel()
+
+    def timed(k, on_device):
+        times, dets = [], None
+        l0 = ctx.launch_count()
+        for _ in range(k):
+            if on_device:
+                with torch.cuda.stream(stream):
+                    work.copy_(pristine)
+            else:
+                np.copyto(h_work, h_pristine)
+            stream.synchronize()
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record(stream)
+            t0 = time.perf_counter()
+            if on_device:
+                dets = ctx.jamming_suppress(work.data_ptr(), JAM_FS, n=n)
+            else:
+                dets = ctx.jamming_suppress(h_work, JAM_FS)
+            e.record(stream)
+            e.synchronize()
+            times.append(max(s.elapsed_time(e) / 1e3, time.perf_counter() - t0))
+        return times, (ctx.launch_count() - l0) / k, dets
+
+    timed(args.warmup, True)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    ctx.enable_timing(True)
+    ctx.reset_timing()
+    with ClockSampler() as clk:
+        times, launches, dets = timed(args.steps, True)
+    kt = {name: ctx.kernel_time(name) for name in ("jam_stft_detect", "jam_wideband")}
+    ctx.enable_timing(False)
+    t_step = float(np.mean(times))
+    if world > 1:
+        t = torch.tensor([t_step], device=f"cuda:{dev}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_step = float(t.item())
+    e2e_times, _, _ = timed(max(2, args.steps // 2), False)
+    t_e2e = float(np.mean(e2e_times))
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    per_launch = {name: ms / max(cnt, 1) for name, (cnt, ms) in kt.items()}
+    top = max(per_launch, key=per_launch.get)
+    top_bytes = n * (JAM_DETECT_BYTES if top == "jam_stft_detect" else JAM_WIDEBAND_BYTES)
+    achieved = top_bytes / (per_launch[top] / 1e3) / 1e9
+    alg = n * (JAM_DETECT_BYTES + JAM_WIDEBAND_BYTES + JAM_COPY_BYTES)
+    line = {
+        "metric": "interference stage samples/s", "value": world * n / t_step, "unit": "samples/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (device-synthesised, seeded)",
+        "config": {"workload": workload, "samples": n, "detections": [(d["type"], d["frequency_bin"]) for d in dets],
+                   "parallelism": f"replicas x{world}", "l2": f"input {n * 8 / 1e6:.0f} MB > L2, restored before each step"},
+        "e2e": {"value": world * n / t_e2e, "unit": "samples/s", "h2d_bytes_per_step": n * 8, "d2h_bytes_per_step": n * 8,
+                "ms_per_step": t_e2e * 1e3},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "traffic": None,
+                     "algorithmic_bytes_per_launch": top_bytes,
+                     "kernel_ms": {k: v for k, v in per_launch.items()},
+                     "step_hbm_gbs": alg / t_step / 1e9,
+                     "peak_source": "hbm_gbs of MEASURED_PEAKS.json"},
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = jamming_cpu_baseline(h_pristine)
+    return line
+
+
 # ------------------------------------------------------------ CPU reference
 def cpu_baseline(args, jobs, raw, fs, budget_s: float = 20.0):
     """Bounded sample of the same workload on the host cores through the CPU
@@ -834,7 +975,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--config", choices=sorted(WORKLOADS) + ["track"], default="multi")
+    ap.add_argument("--config", choices=sorted(WORKLOADS) + ["track", "jamming"], default="multi")
     ap.add_argument("--track-seconds", type=float, default=10.0, help="capture length of --config track")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--served", action="store_true", help="run the served request stream instead")
@@ -854,6 +995,8 @@ def main():
         return
     if args.config == "track":
         line = run_track(args, world, rank)
+    elif args.config == "jamming":
+        line = run_jamming(args, world, rank)
     else:
         line = run_ours(args, world, rank) if args.impl == "ours" else run_reference(args, world, rank)
     if rank == 0 and line is not None:

@@ -8,12 +8,16 @@
 //                       strongest bins with their peak / sigma
 //                       (JammingDetector::IntermediateDetection,
 //                       src/antijamming/jamming_detection.hpp:113-128)
-//   host                AnalyzeStftData (130-189): the occupation vote over
-//                       at most 8 candidates per column — branchy, a few KB
-//   istft_cols_kernel   FilterWideband (src/antijamming/jse.hpp:70-87): bins
-//                       with |.| >= 20 zeroed, inverse column DFTs scaled 2/W
-//   overlap_add_kernel  OverlapAndAdd (src/math/stft.hpp:63-75) as a gather:
-//                       each output sums its covering columns in column order
+//                       and each CTA's occupation histograms
+//   decide_kernel,      AnalyzeStftData (130-189): the occupation vote per
+//   jn_sum_kernel       round, then the reported J/N sums; only the detection
+//                       list goes back to the host
+//   wideband_kernel     FilterWideband (src/antijamming/jse.hpp:70-87) fused
+//                       per output tile: the covering columns re-transformed
+//                       from the samples, bins with |.| >= 20 zeroed, inverse
+//                       DFTs scaled 2/W, overlap-added in column order
+//   istft_cols_kernel,  the per-op OverlapAndAdd (src/math/stft.hpp:63-75):
+//   overlap_add_kernel  inverse columns, then a gather in column order
 //   null_bins_kernel    FilterInFreqencyDomain (jse.hpp:61-68): +-128 bins
 //                       around each narrowband jammer of the whole-signal DFT
 #include "internal.hpp"
@@ -22,7 +26,6 @@
 
 #include <algorithm>
 #include <cmath>
-#include <map>
 #include <vector>
 
 namespace ugsdr_gpu {
@@ -30,17 +33,78 @@ namespace ugsdr_gpu {
 		constexpr int kJamThreads = 256;
 		constexpr int kMaxCandidates = 8;      // max_inreference_cnt (jamming_detection.hpp:81)
 		constexpr int kNullHalfWidth = 3;      // null_window_size (82)
-		constexpr double kJnThreshold = 6.0;   // j_s_threshold (78)
+		constexpr float kJnThreshold = 6.0f;   // j_s_threshold (78)
 		constexpr double kProbability = 0.9;   // probability_threshold (79)
 		constexpr float kWidebandLevel = 20.0f;  // j_s_absolute_threshold (jse.hpp:43)
 		constexpr int kNarrowNull = 128;       // null_window_size (jse.hpp:47)
 		constexpr int kDetectWindow = 128;     // Transform's defaults (stft.hpp:19)
 		constexpr int kDetectOverlap = 96;
 
-		struct JamCandidate {
-			double jn;  // peak / sigma
+		constexpr int kDetectBins = 128;        // the detector's window
+		constexpr int kMaxDetections = 2 * kMaxCandidates;  // two per round at most
+		constexpr int kSumCtas = 256;           // CTAs of the J/N sums
+		constexpr uint8_t kNoBin = 0xFF;
+
+		struct Detection {
+			int type;
 			int bin;
+			double frequency;
+			double jn;
+		};
+
+		struct DetectionList {
+			int n;
 			int pad;
+			Detection d[kMaxDetections];
+		};
+
+		// Device scratch of the detector (one allocation, 256-byte regions):
+		// per round r the occupation histogram over bins, the candidate count,
+		// the decisions, the J/N partial sums and the detection list; then the
+		// per-column candidates as rounds x columns arrays (bin, J/N).
+		struct DetectScratch {
+			int* hist;                  // [kMaxCandidates][kDetectBins]
+			unsigned long long* total;  // candidates over all columns
+			unsigned int* done;         // CTAs of jn_sum_kernel finished
+			int* picks;                 // [kMaxCandidates][2]: narrowband, wideband bin or -1
+			double* quantity;           // [kMaxCandidates]
+			int* rounds;                // mean candidates per column
+			DetectionList* list;
+			double* partials;           // [kSumCtas][kMaxDetections]
+			uint8_t* bins;              // [kMaxCandidates][cols], kNoBin past the column's count
+			float* jn;                  // [kMaxCandidates][cols]
+		};
+
+		struct DetectLayout {
+			size_t hist, total, done, picks, quantity, rounds, list, partials, bins, jn, bytes, zero_bytes;
+			explicit DetectLayout(size_t cols) {
+				size_t at = 0;
+				auto take = [&](size_t b) {
+					const size_t r = at;
+					at = (at + b + 255) / 256 * 256;
+					return r;
+				};
+				hist = take(sizeof(int) * kMaxCandidates * kDetectBins);
+				total = take(sizeof(unsigned long long));
+				done = take(sizeof(unsigned int));
+				zero_bytes = at;  // hist, total and done start at zero
+				picks = take(sizeof(int) * kMaxCandidates * 2);
+				quantity = take(sizeof(double) * kMaxCandidates);
+				rounds = take(sizeof(int));
+				list = take(sizeof(DetectionList));
+				partials = take(sizeof(double) * kSumCtas * kMaxDetections);
+				bins = take(kMaxCandidates * cols);
+				jn = take(sizeof(float) * kMaxCandidates * cols);
+				bytes = at;
+			}
+			DetectScratch carve(void* base) const {
+				char* b = static_cast<char*>(base);
+				return DetectScratch{reinterpret_cast<int*>(b + hist), reinterpret_cast<unsigned long long*>(b + total),
+					reinterpret_cast<unsigned int*>(b + done), reinterpret_cast<int*>(b + picks),
+					reinterpret_cast<double*>(b + quantity), reinterpret_cast<int*>(b + rounds),
+					reinterpret_cast<DetectionList*>(b + list), reinterpret_cast<double*>(b + partials),
+					reinterpret_cast<uint8_t*>(b + bins), reinterpret_cast<float*>(b + jn)};
+			}
 		};
 
 		struct StftParams {
@@ -50,73 +114,85 @@ namespace ugsdr_gpu {
 			int per_cta;           // columns per CTA
 			const float* window;   // w floats
 			FftPlanDev plan;
-			float2* s;             // cols x w spectra
-			int detect;
-			JamCandidate* cand;    // cols x kMaxCandidates
-			int* counts;           // cols
+			float2* s;             // cols x w spectra (null: not stored)
+			int detect;            // w == kDetectBins
+			DetectScratch det;
 		};
 
 		__device__ __forceinline__ float magnitude(float2 v) { return sqrtf(v.x * v.x + v.y * v.y); }
 
-		// The warp's column: kMaxCandidates rounds of first-max (lowest index on
-		// ties, as std::max_element) each followed by nulling +-3 bins
-		// (NullRegion, jamming_detection.hpp:101-110), then one-pass float mean
-		// and unbiased sigma over the nulled magnitudes (SequentialMeanStdDev,
-		// src/math/mean_stddev.hpp:29-42) and J/N = peak / sigma in double;
-		// candidates with J/N < 6 are erased, the rest kept in order.
-		__device__ void detect_column(float* m, int w, JamCandidate* out, int* count) {
+		// The warp's column, magnitudes in registers (lane l holds bins l + 32 j):
+		// kMaxCandidates rounds of first-max — the largest magnitude (redux max
+		// over the bit patterns, which order as non-negative floats do), then
+		// the lowest bin holding it (redux min), as std::max_element — each
+		// followed by nulling +-3 bins (NullRegion, jamming_detection.hpp:
+		// 101-110); then the float mean and unbiased sigma of the nulled
+		// magnitudes with SequentialMeanStdDev's formula (src/math/
+		// mean_stddev.hpp:29-42; the sums in warp-tree order) and J/N =
+		// peak / sigma.  Candidates with J/N < 6 are erased, the rest
+		// kept in order: kept candidate r of column `col` goes to [r][col] and
+		// into the CTA's round-r occupation histogram.
+		__device__ void detect_column(float (&mv)[kDetectBins / 32], const DetectScratch& d, size_t col, size_t cols,
+			int* s_hist, unsigned int* s_total) {
+			constexpr int J = kDetectBins / 32;
 			const int lane = threadIdx.x & 31;
 			int bins[kMaxCandidates];
 			float peaks[kMaxCandidates];
 #pragma unroll
 			for (int r = 0; r < kMaxCandidates; ++r) {
-				float bv = -1.0f;
-				int bi = 0x7fffffff;
-				for (int k = lane; k < w; k += 32) {
-					const float v = m[k];
-					if (v > bv) {
-						bv = v;
-						bi = k;
-					}
-				}
-				for (int o = 16; o > 0; o >>= 1) {
-					const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
-					const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-					if (ov > bv || (ov == bv && oi < bi)) {
-						bv = ov;
-						bi = oi;
-					}
-				}
+				unsigned int top = 0;
+#pragma unroll
+				for (int j = 0; j < J; ++j)
+					top = max(top, __float_as_uint(mv[j]));
+				top = __reduce_max_sync(0xffffffffu, top);
+				unsigned int first = 0xffffffffu;
+#pragma unroll
+				for (int j = J - 1; j >= 0; --j)
+					if (__float_as_uint(mv[j]) == top)
+						first = lane + 32 * j;
+				const int bi = static_cast<int>(__reduce_min_sync(0xffffffffu, first));
 				bins[r] = bi;
-				peaks[r] = bv;
-				__syncwarp();
-				if (lane <= 2 * kNullHalfWidth)
-					m[(bi - kNullHalfWidth + lane + w) % w] = 0.0f;
-				__syncwarp();
+				peaks[r] = __uint_as_float(top);
+#pragma unroll
+				for (int j = 0; j < J; ++j) {
+					const int dist = (lane + 32 * j - bi + kDetectBins) % kDetectBins;
+					if (dist <= kNullHalfWidth || dist >= kDetectBins - kNullHalfWidth)
+						mv[j] = 0.0f;
+				}
+			}
+			float q = 0.0f, s = 0.0f;
+#pragma unroll
+			for (int j = 0; j < J; ++j) {
+				q = __fadd_rn(q, __fmul_rn(mv[j], mv[j]));
+				s = __fadd_rn(s, mv[j]);
+			}
+			for (int o = 16; o > 0; o >>= 1) {
+				q = __fadd_rn(q, __shfl_xor_sync(0xffffffffu, q, o));
+				s = __fadd_rn(s, __shfl_xor_sync(0xffffffffu, s, o));
 			}
 			if (lane != 0)
 				return;
-			float q = 0.0f, s = 0.0f;
-			for (int k = 0; k < w; ++k) {
-				const float el = m[k];
-				q = __fadd_rn(q, __fmul_rn(el, el));
-				s = __fadd_rn(s, el);
-			}
-			const float fw = static_cast<float>(w);
-			const float var = __fdiv_rn(__fsub_rn(q, __fdiv_rn(__fmul_rn(s, s), fw)), static_cast<float>(w - 1));
-			const double sigma = static_cast<double>(__fsqrt_rn(var));
+			const float fw = static_cast<float>(kDetectBins);
+			const float var = __fdiv_rn(__fsub_rn(q, __fdiv_rn(__fmul_rn(s, s), fw)), static_cast<float>(kDetectBins - 1));
+			const float sigma = __fsqrt_rn(var);
 			int c = 0;
 #pragma unroll
 			for (int r = 0; r < kMaxCandidates; ++r) {
-				const double jn = static_cast<double>(peaks[r]) / sigma;
-				if (!(jn < kJnThreshold)) {  // remove_if(jn < threshold): a NaN stays
-					out[c].jn = jn;
-					out[c].bin = bins[r];
-					out[c].pad = 0;
+				// double(peak) / double(sigma) < 6 exactly when peak - 6 sigma < 0
+				// (two floats' double quotient cannot round onto 6 unless it is 6),
+				// and fmaf rounds that difference once, keeping its sign: the
+				// reference's double test without FP64 (a NaN stays, as in
+				// remove_if(jn < threshold)).  The kept J/N is the float quotient.
+				if (!(fmaf(-kJnThreshold, sigma, peaks[r]) < 0.0f)) {
+					d.bins[static_cast<size_t>(c) * cols + col] = static_cast<uint8_t>(bins[r]);
+					d.jn[static_cast<size_t>(c) * cols + col] = __fdiv_rn(peaks[r], sigma);
+					atomicAdd(&s_hist[c * kDetectBins + bins[r]], 1);
 					++c;
 				}
 			}
-			*count = c;
+			for (int r = c; r < kMaxCandidates; ++r)
+				d.bins[static_cast<size_t>(r) * cols + col] = kNoBin;
+			atomicAdd(s_total, static_cast<unsigned int>(c));
 		}
 
 		template <class F>
@@ -141,24 +217,35 @@ namespace ugsdr_gpu {
 			}
 			__syncthreads();
 			const float2* y = F::template run<false>(a, b, plan, nc, ld);
-			for (int e = threadIdx.x; e < nc * w; e += blockDim.x) {
-				const int f = e / w, i = e - f * w;
-				p.s[static_cast<size_t>(c0 + f) * w + i] = y[f * ld + i];
-			}
+			if (p.s)
+				for (int e = threadIdx.x; e < nc * w; e += blockDim.x) {
+					const int f = e / w, i = e - f * w;
+					p.s[static_cast<size_t>(c0 + f) * w + i] = y[f * ld + i];
+				}
 			if (!p.detect)
 				return;
-			// magnitudes into the free tile, one warp per column
-			float* mags = reinterpret_cast<float*>(y == a ? b : a);
-			const int warp = threadIdx.x >> 5, n_warps = blockDim.x >> 5;
+			__shared__ int s_hist[kMaxCandidates * kDetectBins];
+			__shared__ unsigned int s_total;
+			for (int e = threadIdx.x; e < kMaxCandidates * kDetectBins; e += blockDim.x)
+				s_hist[e] = 0;
+			if (threadIdx.x == 0)
+				s_total = 0;
+			__syncthreads();
+			// one warp per column (w == kDetectBins here)
+			const int warp = threadIdx.x >> 5, n_warps = blockDim.x >> 5, lane = threadIdx.x & 31;
 			for (int f = warp; f < nc; f += n_warps) {
-				float* m = mags + f * 2 * ld;
-				for (int k = threadIdx.x & 31; k < w; k += 32)
-					m[k] = magnitude(y[f * ld + k]);
-				__syncwarp();
-				const int col = c0 + f;
-				detect_column(m, w, p.cand + static_cast<size_t>(col) * kMaxCandidates, p.counts + col);
-				__syncwarp();
+				float mv[kDetectBins / 32];
+#pragma unroll
+				for (int j = 0; j < kDetectBins / 32; ++j)
+					mv[j] = magnitude(y[f * ld + lane + 32 * j]);
+				detect_column(mv, p.det, static_cast<size_t>(c0 + f), static_cast<size_t>(p.cols), s_hist, &s_total);
 			}
+			__syncthreads();
+			for (int e = threadIdx.x; e < kMaxCandidates * kDetectBins; e += blockDim.x)
+				if (s_hist[e])
+					atomicAdd(p.det.hist + e, s_hist[e]);
+			if (threadIdx.x == 0 && s_total)
+				atomicAdd(p.det.total, static_cast<unsigned long long>(s_total));
 		}
 
 		struct IstftParams {
@@ -166,7 +253,6 @@ namespace ugsdr_gpu {
 			int w;
 			int cols;
 			int per_cta;
-			int zero_wideband;     // FilterWideband's |.| >= 20 -> 0
 			FftPlanDev plan;
 			float2* t;             // cols x w inverse columns
 		};
@@ -183,10 +269,7 @@ namespace ugsdr_gpu {
 			const FftPlanDev plan = F::prepare(p.plan, b + p.per_cta * ld);
 			for (int e = threadIdx.x; e < nc * w; e += blockDim.x) {
 				const int f = e / w, i = e - f * w;
-				float2 v = p.s[static_cast<size_t>(c0 + f) * w + i];
-				if (p.zero_wideband && magnitude(v) >= kWidebandLevel)
-					v = c2(0.0f, 0.0f);
-				a[f * ld + i] = v;
+				a[f * ld + i] = p.s[static_cast<size_t>(c0 + f) * w + i];
 			}
 			__syncthreads();
 			const float2* y = F::template run<true>(a, b, plan, nc, ld);
@@ -219,6 +302,72 @@ namespace ugsdr_gpu {
 					}
 				}
 				out[k] = c2(ax, ay);
+			}
+		}
+
+		struct WidebandParams {
+			const float2* x;       // n input samples
+			uint64_t n;
+			int w, hop;
+			int cols;
+			int per_cta;           // columns per CTA, the halo included
+			int slots;             // output hops per CTA: per_cta - (w / hop - 1)
+			const float* window;
+			FftPlanDev plan;
+			float2* out;           // n output samples (not x)
+		};
+
+		// FilterWideband fused for one tile of slots * hop output samples: the
+		// covering columns (the tile's own and w / hop - 1 before it) are
+		// re-transformed from x exactly as the detector's STFT did, zeroed where
+		// |.| >= 20, inverse-transformed, scaled 2/w and overlap-added in column
+		// order; the spectra never leave shared memory.
+		template <class F>
+		__global__ void __launch_bounds__(kJamThreads) wideband_kernel(WidebandParams p) {
+			extern __shared__ float2 sm[];
+			const int w = fft_n<F>(p.plan.n);
+			const int ld = w | 1;
+			const int hop = p.hop;
+			const uint64_t t0 = static_cast<uint64_t>(blockIdx.x) * p.slots * hop;
+			const uint64_t t1 = min(t0 + static_cast<uint64_t>(p.slots) * hop, p.n);
+			const int i_lo = t0 >= static_cast<uint64_t>(w) ? static_cast<int>((t0 - w) / hop) + 1 : 0;
+			const int i_hi = min(p.cols - 1, static_cast<int>((t1 - 1) / hop));
+			const int nc = max(0, i_hi - i_lo + 1);
+			float2* a = sm;
+			float2* b = sm + p.per_cta * ld;
+			float* win = reinterpret_cast<float*>(sm + 2 * p.per_cta * ld);
+			const FftPlanDev plan = F::prepare(p.plan, win + w);
+			for (int i = threadIdx.x; i < w; i += blockDim.x)
+				win[i] = p.window[i];
+			__syncthreads();
+			for (int e = threadIdx.x; e < nc * w; e += blockDim.x) {
+				const int f = e / w, i = e - f * w;
+				const float2 v = p.x[static_cast<size_t>(i_lo + f) * hop + i];
+				a[f * ld + i] = c2(__fmul_rn(v.x, win[i]), __fmul_rn(v.y, win[i]));
+			}
+			__syncthreads();
+			float2* y = F::template run<false>(a, b, plan, nc, ld);
+			for (int e = threadIdx.x; e < nc * w; e += blockDim.x) {
+				const int f = e / w, i = e - f * w;
+				if (magnitude(y[f * ld + i]) >= kWidebandLevel)
+					y[f * ld + i] = c2(0.0f, 0.0f);
+			}
+			__syncthreads();
+			const float2* z = F::template run<true>(y, y == a ? b : a, plan, nc, ld);
+			const float fw = static_cast<float>(w);
+			const uint64_t len = static_cast<uint64_t>(w) + static_cast<uint64_t>(p.cols - 1) * hop;
+			for (uint64_t k = t0 + threadIdx.x; k < t1; k += blockDim.x) {
+				float ax = 0.0f, ay = 0.0f;
+				if (k < len) {
+					const int lo = k >= static_cast<uint64_t>(w) ? static_cast<int>((k - w) / hop) + 1 : 0;
+					const int hi = min(p.cols - 1, static_cast<int>(k / hop));
+					for (int i = lo; i <= hi; ++i) {
+						const float2 v = z[(i - i_lo) * ld + static_cast<int>(k - static_cast<uint64_t>(i) * hop)];
+						ax = __fadd_rn(ax, __fmul_rn(__fdiv_rn(v.x, fw), 2.0f));
+						ay = __fadd_rn(ay, __fmul_rn(__fdiv_rn(v.y, fw), 2.0f));
+					}
+				}
+				p.out[k] = c2(ax, ay);
 			}
 		}
 
@@ -297,12 +446,14 @@ namespace ugsdr_gpu {
 			return cols;
 		}
 
-		// STFT of device samples x into ctx->jam_s, with detection candidates
-		// into ctx->jam_cand when `detect`
-		void stft_device(ugsdr_ctx* ctx, const float2* x, size_t cols, int w, int overlap, bool detect) {
+		// STFT of device samples x: spectra into ctx->jam_s when `spectra`,
+		// detection candidates and histograms into `det` when given
+		void stft_device(ugsdr_ctx* ctx, const float2* x, size_t cols, int w, int overlap, bool spectra,
+			const DetectScratch* det) {
 			size_t smem = 0;
 			const int per = columns_per_cta(ctx, w, smem);
-			ctx->jam_s.reserve(sizeof(float2) * cols * w);
+			if (spectra)
+				ctx->jam_s.reserve(sizeof(float2) * cols * w);
 			StftParams p{};
 			p.x = x;
 			p.w = w;
@@ -311,13 +462,13 @@ namespace ugsdr_gpu {
 			p.per_cta = per;
 			p.window = hann_window(ctx, w);
 			p.plan = column_plan(ctx, w);
-			p.s = ctx->jam_s.as<float2>();
-			p.detect = detect ? 1 : 0;
-			if (detect) {
-				ctx->jam_cand.reserve((sizeof(JamCandidate) * kMaxCandidates + sizeof(int)) * cols);
-				p.cand = ctx->jam_cand.as<JamCandidate>();
-				p.counts = reinterpret_cast<int*>(p.cand + cols * kMaxCandidates);
+			p.s = spectra ? ctx->jam_s.as<float2>() : nullptr;
+			p.detect = det ? 1 : 0;
+			if (det) {
+				require(w == kDetectBins, "detection runs on 128-point columns");
+				p.det = *det;
 			}
+			KernelTimer timer(ctx, det ? "jam_stft_detect" : "jam_stft");
 			with_column_fft(w, [&](auto f) {
 				using F = decltype(f);
 				UG_CUDA(cudaFuncSetAttribute(stft_kernel<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
@@ -326,9 +477,9 @@ namespace ugsdr_gpu {
 			});
 		}
 
-		// inverse columns of ctx->jam_s (zeroing |.| >= 20 when asked) into
-		// ctx->jam_t, overlap-added into n samples at out
-		void istft_device(ugsdr_ctx* ctx, size_t cols, int w, int overlap, bool zero_wideband, float2* out, size_t n) {
+		// inverse columns of ctx->jam_s into ctx->jam_t, overlap-added into n
+		// samples at out
+		void istft_device(ugsdr_ctx* ctx, size_t cols, int w, int overlap, float2* out, size_t n) {
 			size_t smem = 0;
 			const int per = columns_per_cta(ctx, w, smem);
 			ctx->jam_t.reserve(sizeof(float2) * cols * w);
@@ -337,7 +488,6 @@ namespace ugsdr_gpu {
 			p.w = w;
 			p.cols = static_cast<int>(cols);
 			p.per_cta = per;
-			p.zero_wideband = zero_wideband ? 1 : 0;
 			p.plan = column_plan(ctx, w);
 			p.t = ctx->jam_t.as<float2>();
 			with_column_fft(w, [&](auto f) {
@@ -350,82 +500,165 @@ namespace ugsdr_gpu {
 			note_launch(ctx, 2);
 		}
 
-		struct Detection {
-			int type;
-			int bin;
-			double frequency;
-			double jn;
-		};
-
-		// AnalyzeStftData (jamming_detection.hpp:130-189) over the columns'
-		// candidates, restated with its float/double and integer conversions;
-		// frequency = bin * fs / 128 as the candidates are built (120).
-		std::vector<Detection> analyze(const std::vector<int>& counts, const std::vector<JamCandidate>& cand, double fs, int w) {
-			std::vector<Detection> dst;
-			const size_t cols = counts.size();
-			size_t mean_jammers = 0;
-			for (int c : counts)
-				mean_jammers += static_cast<size_t>(c);
-			mean_jammers /= cols;
-			struct Occupation {
-				double count = 0;
-				int bin = 0;
-				double frequency = 0;
-				double jn = 0;
-			};
-			for (size_t i = 0; i < mean_jammers; ++i) {
-				std::map<double, Occupation> occ;
-				double quantity = 0;
-				for (size_t c = 0; c < cols; ++c) {
-					if (static_cast<size_t>(counts[c]) <= i)
-						continue;
-					const JamCandidate& k = cand[c * kMaxCandidates + i];
-					const double f = static_cast<double>(k.bin) * fs / static_cast<double>(w);
-					Occupation& o = occ[f];
-					o.count += 1;
-					o.frequency = f;
-					o.bin = k.bin;
-					o.jn += k.jn;
-					++quantity;
-				}
-				for (auto& kv : occ) {
-					kv.second.count /= quantity;
-					kv.second.jn /= quantity;
-				}
-				size_t cnt_wideband = 0;
-				const Occupation* wide = &occ.begin()->second;
-				for (auto& kv : occ) {
-					const double probability = kv.second.count;
-					if (probability >= kProbability) {
-						dst.push_back({UGSDR_INTERFERENCE_NARROWBAND, kv.second.bin, kv.second.frequency, kv.second.jn});
-						break;
-					}
-					if (probability >= kProbability / static_cast<double>(occ.size())) {
-						++cnt_wideband;
-						wide = &kv.second;
-					}
-				}
-				// a single occupied frequency makes the bound 0: the reference
-				// then reports it as wideband as well
-				if (cnt_wideband >= static_cast<size_t>(occ.size() * kProbability))
-					dst.push_back({UGSDR_INTERFERENCE_WIDEBAND, wide->bin, wide->frequency, wide->jn});
-			}
-			return dst;
+		// FilterWideband + OverlapAndAdd + resize to n, fused: x -> out
+		void wideband_device(ugsdr_ctx* ctx, const float2* x, size_t n, float2* out) {
+			const int w = kDetectWindow, hop = kDetectWindow - kDetectOverlap;
+			const size_t cols = stft_columns(n, w, kDetectOverlap);
+			size_t smem = 0;
+			const int per = columns_per_cta(ctx, w, smem);
+			WidebandParams p{};
+			p.x = x;
+			p.n = n;
+			p.w = w;
+			p.hop = hop;
+			p.cols = static_cast<int>(cols);
+			p.per_cta = per;
+			p.slots = per - (w / hop - 1);
+			require(p.slots >= 1, "wideband tile too small");
+			p.window = hann_window(ctx, w);
+			p.plan = column_plan(ctx, w);
+			p.out = out;
+			const uint64_t tile = static_cast<uint64_t>(p.slots) * hop;
+			using F = StaticFft<128, 16, 8>;
+			KernelTimer timer(ctx, "jam_wideband");
+			UG_CUDA(cudaFuncSetAttribute(wideband_kernel<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+			wideband_kernel<F><<<static_cast<unsigned>((n + tile - 1) / tile), kJamThreads, smem, ctx->stream>>>(p);
+			note_launch(ctx);
 		}
 
-		// detector over device samples x (n): STFT + candidates on the device,
-		// analysis on the host
+		// deterministic block sum of per-thread doubles (fixed tree order)
+		__device__ double block_sum(double v, double* scratch) {
+			for (int o = 16; o > 0; o >>= 1)
+				v += __shfl_down_sync(0xffffffffu, v, o);
+			const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+			__syncthreads();
+			if (lane == 0)
+				scratch[warp] = v;
+			__syncthreads();
+			if (warp == 0) {
+				v = lane < (blockDim.x >> 5) ? scratch[lane] : 0.0;
+				for (int o = 16; o > 0; o >>= 1)
+					v += __shfl_down_sync(0xffffffffu, v, o);
+				if (lane == 0)
+					scratch[0] = v;
+			}
+			__syncthreads();
+			return scratch[0];
+		}
+
+		// AnalyzeStftData (jamming_detection.hpp:130-189), decisions.  Round i
+		// looks at every column's i-th candidate: its occupation map is keyed
+		// by frequency = bin * fs / w, which orders as the bins do, so the
+		// reference's walk over the map is a walk over occupied bins in
+		// increasing order of the round's histogram.
+		__global__ void decide_kernel(DetectScratch d, unsigned long long cols) {
+			if (threadIdx.x != 0)
+				return;
+			const int rounds = static_cast<int>(*d.total / cols);
+			for (int i = 0; i < rounds; ++i) {
+				const int* occ = d.hist + i * kDetectBins;
+				double quantity = 0;
+				int occupied = 0;
+				for (int b = 0; b < kDetectBins; ++b)
+					if (occ[b]) {
+						quantity += occ[b];
+						++occupied;
+					}
+				int narrow = -1, wide = -1, first = -1;
+				unsigned long long cnt_wideband = 0;
+				for (int b = 0; b < kDetectBins; ++b) {
+					if (!occ[b])
+						continue;
+					if (first < 0)
+						first = b;
+					const double probability = occ[b] / quantity;
+					if (probability >= kProbability) {
+						narrow = b;
+						break;
+					}
+					if (probability >= kProbability / static_cast<double>(occupied)) {
+						++cnt_wideband;
+						wide = b;
+					}
+				}
+				if (wide < 0)
+					wide = first;  // the reference's pointer starts at the map's first entry
+				d.picks[2 * i] = narrow;
+				// one occupied bin makes the bound 0: reported as wideband too
+				d.picks[2 * i + 1] = cnt_wideband >= static_cast<unsigned long long>(occupied * kProbability) ? wide : -1;
+				d.quantity[i] = quantity;
+			}
+			*d.rounds = rounds;
+		}
+
+		// The reported J/N of each pick: the mean of the round's candidate J/N
+		// at that bin.  Per-CTA partial sums over a fixed column split, combined
+		// in CTA order by the last CTA, which also writes the detection list —
+		// deterministic, within rounding of the reference's column-order sum.
+		__global__ void __launch_bounds__(kJamThreads) jn_sum_kernel(DetectScratch d, unsigned long long cols, double fs) {
+			__shared__ double scratch[32];
+			__shared__ bool s_last;
+			const int rounds = *d.rounds;
+			for (int i = 0; i < rounds; ++i)
+				for (int k = 0; k < 2; ++k) {
+					const int b = d.picks[2 * i + k];
+					if (b < 0)
+						continue;
+					double part = 0;
+					const uint8_t* bins = d.bins + static_cast<size_t>(i) * cols;
+					const float* jn = d.jn + static_cast<size_t>(i) * cols;
+					for (unsigned long long c = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x; c < cols;
+						 c += static_cast<unsigned long long>(gridDim.x) * blockDim.x)
+						if (bins[c] == b)
+							part += jn[c];
+					const double sum = block_sum(part, scratch);
+					if (threadIdx.x == 0)
+						d.partials[blockIdx.x * kMaxDetections + 2 * i + k] = sum;
+				}
+			__syncthreads();
+			if (threadIdx.x == 0) {
+				__threadfence();
+				s_last = atomicAdd(d.done, 1u) == gridDim.x - 1;
+			}
+			__syncthreads();
+			if (!s_last || threadIdx.x != 0)
+				return;
+			__threadfence();
+			int n = 0;
+			for (int i = 0; i < rounds; ++i)
+				for (int k = 0; k < 2; ++k) {
+					const int b = d.picks[2 * i + k];
+					if (b < 0 || n >= kMaxDetections)
+						continue;
+					double sum = 0;
+					for (unsigned int g = 0; g < gridDim.x; ++g)
+						sum += __ldcg(d.partials + g * kMaxDetections + 2 * i + k);
+					Detection& out = d.list->d[n++];
+					out.type = k == 0 ? UGSDR_INTERFERENCE_NARROWBAND : UGSDR_INTERFERENCE_WIDEBAND;
+					out.bin = b;
+					out.frequency = static_cast<double>(b) * fs / static_cast<double>(kDetectBins);
+					out.jn = sum / d.quantity[i];
+				}
+			d.list->n = n;
+		}
+
+		// detector over device samples x (n): STFT + candidates, decisions and
+		// J/N sums on the device; only the detection list comes back
 		std::vector<Detection> detect_device(ugsdr_ctx* ctx, const float2* x, size_t n, double fs) {
 			require(fs > 0, "sampling rate must be positive");
 			const size_t cols = stft_columns(n, kDetectWindow, kDetectOverlap);
-			stft_device(ctx, x, cols, kDetectWindow, kDetectOverlap, true);
-			std::vector<JamCandidate> cand(cols * kMaxCandidates);
-			std::vector<int> counts(cols);
-			const JamCandidate* dc = ctx->jam_cand.as<JamCandidate>();
-			UG_CUDA(cudaMemcpyAsync(cand.data(), dc, sizeof(JamCandidate) * cand.size(), cudaMemcpyDeviceToHost, ctx->stream));
-			UG_CUDA(cudaMemcpyAsync(counts.data(), dc + cols * kMaxCandidates, sizeof(int) * cols, cudaMemcpyDeviceToHost, ctx->stream));
+			const DetectLayout lay(cols);
+			ctx->jam_cand.reserve(lay.bytes);
+			const DetectScratch d = lay.carve(ctx->jam_cand.ptr);
+			UG_CUDA(cudaMemsetAsync(ctx->jam_cand.ptr, 0, lay.zero_bytes, ctx->stream));
+			stft_device(ctx, x, cols, kDetectWindow, kDetectOverlap, false, &d);
+			decide_kernel<<<1, 32, 0, ctx->stream>>>(d, cols);
+			jn_sum_kernel<<<kSumCtas, kJamThreads, 0, ctx->stream>>>(d, cols, fs);
+			note_launch(ctx, 2);
+			DetectionList host{};
+			UG_CUDA(cudaMemcpyAsync(&host, d.list, sizeof(DetectionList), cudaMemcpyDeviceToHost, ctx->stream));
 			UG_CUDA(cudaStreamSynchronize(ctx->stream));
-			return analyze(counts, cand, fs, kDetectWindow);
+			return std::vector<Detection>(host.d, host.d + std::min(host.n, kMaxDetections));
 		}
 
 		void report(const std::vector<Detection>& det, ugsdr_jamming_detection* out, int cap, int* n_detections) {
@@ -471,7 +704,7 @@ int ugsdr_stft(ugsdr_ctx* ctx, const float* in_iq, size_t n, int window_length, 
 		if (!out_iq)
 			return;
 		const float2* x = stage(ctx, in_iq, n, 0);
-		stft_device(ctx, x, cols, window_length, overlap_length, false);
+		stft_device(ctx, x, cols, window_length, overlap_length, true, nullptr);
 		UG_CUDA(cudaMemcpyAsync(out_iq, ctx->jam_s.ptr, sizeof(float2) * cols * window_length, cudaMemcpyDeviceToHost, ctx->stream));
 		UG_CUDA(cudaStreamSynchronize(ctx->stream));
 	});
@@ -488,7 +721,7 @@ int ugsdr_istft(ugsdr_ctx* ctx, const float* in_iq, size_t n_columns, int window
 		ctx->jam_s.reserve(sizeof(float2) * n_columns * w);
 		UG_CUDA(cudaMemcpyAsync(ctx->jam_s.ptr, in_iq, sizeof(float2) * n_columns * w, cudaMemcpyHostToDevice, ctx->stream));
 		ctx->jam_x.reserve(sizeof(float2) * len);
-		istft_device(ctx, n_columns, window_length, overlap_length, false, ctx->jam_x.as<float2>(), len);
+		istft_device(ctx, n_columns, window_length, overlap_length, ctx->jam_x.as<float2>(), len);
 		UG_CUDA(cudaMemcpyAsync(out_iq, ctx->jam_x.ptr, sizeof(float2) * len, cudaMemcpyDeviceToHost, ctx->stream));
 		UG_CUDA(cudaStreamSynchronize(ctx->stream));
 	});
@@ -512,8 +745,13 @@ int ugsdr_jamming_suppress(ugsdr_ctx* ctx, float* iq, size_t n, double fs, int s
 			return;
 		const bool wideband = std::any_of(det.begin(), det.end(), [](const Detection& d) { return d.type == UGSDR_INTERFERENCE_WIDEBAND; });
 		if (wideband) {
-			const size_t cols = stft_columns(n, kDetectWindow, kDetectOverlap);
-			istft_device(ctx, cols, kDetectWindow, kDetectOverlap, true, x, n);
+			// out of place (a tile reads its neighbours' inputs), then back
+			ctx->jam_t.reserve(sizeof(float2) * n);
+			wideband_device(ctx, x, n, ctx->jam_t.as<float2>());
+			if (samples_on_device)
+				UG_CUDA(cudaMemcpyAsync(x, ctx->jam_t.ptr, sizeof(float2) * n, cudaMemcpyDeviceToDevice, ctx->stream));
+			else
+				x = ctx->jam_t.as<float2>();
 		}
 		else {
 			// idx = size_t(frequency / fs * n); zero [idx - 128 + n, idx + 128]
