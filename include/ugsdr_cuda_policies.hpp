@@ -24,6 +24,8 @@
 #include UGSDR_STR(UGSDR_REF_SRC/acquisition/fse.hpp)
 #include UGSDR_STR(UGSDR_REF_SRC/correlator/correlator.hpp)
 #include UGSDR_STR(UGSDR_REF_SRC/math/dft.hpp)
+#include UGSDR_STR(UGSDR_REF_SRC/math/stft.hpp)
+#include UGSDR_STR(UGSDR_REF_SRC/antijamming/jamming_detection.hpp)
 
 #include <complex>
 #include <span>
@@ -249,6 +251,71 @@ namespace ugsdr {
 			cuda_detail::Check(ugsdr_correlate(cuda_detail::Context(), cuda_detail::F(s), c.data(), c.size(), out));
 			return std::complex<UnderlyingType>(out[0], out[1]);
 		}
+	};
+
+	// SequentialStft (math/stft.hpp:33-88): both Transform overloads
+	class CudaStft final : public ShortTimeFourierTransform<CudaStft> {
+	protected:
+		friend class ShortTimeFourierTransform<CudaStft>;
+		template <typename T>
+		static auto Process(const std::vector<T>& src, std::size_t window_length, std::size_t overlap_length) {
+			using Dst = std::conditional_t<is_complex_v<T>, T, std::complex<T>>;
+			std::vector<std::complex<float>> x(src.begin(), src.end());
+			std::size_t cols = 0;
+			auto* ctx = cuda_detail::Context();
+			const int w = static_cast<int>(window_length), ov = static_cast<int>(overlap_length);
+			cuda_detail::Check(ugsdr_stft(ctx, cuda_detail::F(x), x.size(), w, ov, nullptr, &cols));
+			std::vector<std::complex<float>> flat(cols * window_length);
+			cuda_detail::Check(ugsdr_stft(ctx, cuda_detail::F(x), x.size(), w, ov, cuda_detail::F(flat), &cols));
+			std::vector<std::vector<Dst>> dst(cols);
+			for (std::size_t c = 0; c < cols; ++c)
+				dst[c].assign(flat.begin() + c * window_length, flat.begin() + (c + 1) * window_length);
+			return dst;
+		}
+		template <typename T>
+		static auto Process(const std::vector<std::vector<T>>& src, std::size_t window_length, std::size_t overlap_length) {
+			std::vector<std::complex<float>> flat;
+			flat.reserve(src.size() * window_length);
+			for (const auto& col : src)
+				flat.insert(flat.end(), col.begin(), col.end());
+			std::vector<std::complex<float>> out(window_length + (src.size() - 1) * (window_length - overlap_length));
+			cuda_detail::Check(ugsdr_istft(cuda_detail::Context(), cuda_detail::F(flat), src.size(), static_cast<int>(window_length),
+				static_cast<int>(overlap_length), cuda_detail::F(out)));
+			return std::vector<T>(out.begin(), out.end());
+		}
+	};
+
+	// JammingSuppressionEngine<T> (antijamming/jse.hpp:24-107) on the GPU: the
+	// same constructor, Process(src_dst) in place and GetDetectionResults.
+	// The front end holds the engine as a member, not a policy
+	// (dfe/dfe.hpp:113): a GPU build swaps that member's type.
+	template <typename T>
+	class CudaJammingSuppressionEngine {
+	public:
+		using DetectionResult = typename JammingDetector<std::complex<underlying_t<T>>>::DetectionResult;
+
+		explicit CudaJammingSuppressionEngine(double sampling_rate) : fs(sampling_rate) {}
+
+		void Process(std::vector<T>& src_dst) {
+			auto x = cuda_detail::ToF(src_dst);
+			ugsdr_jamming_detection det[16];
+			int n = 0;
+			cuda_detail::Check(ugsdr_jamming_suppress(cuda_detail::Context(), cuda_detail::F(x), x.size(), fs, 0, det, 16, &n));
+			if constexpr (std::is_same_v<T, std::complex<float>>)
+				src_dst.swap(x);
+			else
+				cuda_detail::Assign(src_dst, x);
+			results.clear();
+			for (int i = 0; i < n && i < 16; ++i)
+				results.emplace_back(static_cast<typename DetectionResult::InterferenceType>(det[i].type),
+					static_cast<std::size_t>(det[i].frequency_bin), det[i].frequency, det[i].jammer_to_noise);
+		}
+
+		const auto& GetDetectionResults() const { return results; }
+
+	private:
+		double fs = 0.0;
+		std::vector<DetectionResult> results;
 	};
 
 	// FseConfig bundle (fse.hpp:36-67, 98-109) on the GPU policies

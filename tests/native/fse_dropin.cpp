@@ -4,6 +4,8 @@
 // tests/test_integration.py; executed only where a GPU is present.
 #include "ugsdr_cuda_policies.hpp"
 
+#include <algorithm>
+#include <cmath>
 #include <cstdio>
 
 using Fse = ugsdr::FastSearchEngineBase<ugsdr::ParametricCudaFseConfig<8192000>, ugsdr::DefaultChannelConfig, float>;
@@ -25,6 +27,36 @@ int main() {
 	const std::vector<std::complex<float>> gsig(glo.begin(), glo.end());
 	const auto mf = ugsdr::CudaMatchedFilter::Filter(gsig, glo);
 	bad |= std::abs(mf[0].real() - 511.0f) > 5e-3f;
-	std::printf("%s correlate=(%g,%g) mf0=%g\n", bad ? "FAIL" : "ok", dst.real(), dst.imag(), mf[0].real());
+	// interference stage: the GPU engine against the reference's own on a CW
+	// jammer over small noise (jse.hpp:89-102)
+	std::vector<std::complex<float>> jam(4000);
+	unsigned s = 12345u;
+	auto noise = [&s] {
+		s = s * 1664525u + 1013904223u;
+		return (static_cast<float>(s >> 8) / 16777216.0f - 0.5f) * 0.8f;
+	};
+	for (std::size_t i = 0; i < jam.size(); ++i) {
+		const double ph = 2 * 3.14159265358979323846 * 16.0 / 128.0 * static_cast<double>(i);
+		jam[i] = {noise() + 10.0f * static_cast<float>(std::cos(ph)), noise() + 10.0f * static_cast<float>(std::sin(ph))};
+	}
+	auto cpu = jam, gpu = jam;
+	ugsdr::JammingSuppressionEngine<std::complex<float>> ref_engine(4e6);
+	ref_engine.Process(cpu);
+	ugsdr::CudaJammingSuppressionEngine<std::complex<float>> cuda_engine(4e6);
+	cuda_engine.Process(gpu);
+	const auto& rd = ref_engine.GetDetectionResults();
+	const auto& gd = cuda_engine.GetDetectionResults();
+	bad |= rd.size() != gd.size() || rd.empty();
+	for (std::size_t i = 0; i < rd.size() && i < gd.size(); ++i)
+		bad |= rd[i].interference_type != gd[i].interference_type || rd[i].frequency_bin != gd[i].frequency_bin;
+	float worst = 0.0f;
+	for (std::size_t i = 0; i < cpu.size(); ++i)
+		worst = std::max(worst, std::abs(cpu[i] - gpu[i]));
+	bad |= worst > 1e-3f;
+	const auto cols = ugsdr::ShortTimeFourierTransform<ugsdr::CudaStft>::Transform(jam);
+	const auto back = ugsdr::ShortTimeFourierTransform<ugsdr::CudaStft>::Transform(cols);
+	bad |= cols.size() != (jam.size() - 96) / 32 || back.size() != 128 + (cols.size() - 1) * 32;
+	std::printf("%s correlate=(%g,%g) mf0=%g jamming=%zu worst=%g\n", bad ? "FAIL" : "ok", dst.real(), dst.imag(),
+		mf[0].real(), gd.size(), worst);
 	return bad || instantiate_process == nullptr;
 }

@@ -22,7 +22,8 @@ def build():
     cmd = ["g++", "-std=gnu++20", "-O1", "-include", "algorithm", "-DIppDft=SequentialDft",
            f"-DUGSDR_REF_SRC={REF / 'src'}", "-I", str(ROOT / "include"), "-I", str(ROOT / "oracle" / "shims"),
            "-I", str(ROOT / "oracle" / "shims" / "anchor" / "dir"), str(ROOT / "tests" / "native" / "fse_dropin.cpp"),
-           str(REF / "src" / "prn_codes" / "GalileoMemoryCodes.cpp"), "-L", str(lib), "-lugsdr_cuda",
+           str(REF / "src" / "prn_codes" / "GalileoMemoryCodes.cpp"), str(ROOT / "oracle" / "fftw_shim.cpp"),
+           "-I", str(ROOT / "oracle"), "-L", str(lib), "-lugsdr_cuda",
            f"-Wl,-rpath,{lib}", "-o", str(BIN)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-3000:]
