@@ -144,3 +144,53 @@ def test_edges(ctx, oracle):
         ctx.jamming_suppress(np.zeros(100, np.complex64), 2.048e6)
     with pytest.raises(L.UgsdrError):
         ctx.stft(np.zeros(1000, np.complex64), 128, 128)
+
+
+def test_mitigation_before_acquisition(ctx, oracle, golden_codes):
+    """The front end's mitigation stage ahead of the search: Channel::
+    GetSeveralEpochs suppresses (dfe/dfe.hpp:199-202) the samples that
+    FastSearchEngineBase::Process then searches (acquisition/fse.hpp:456-460).
+    A CW jammer 55 dB above the noise hides three GPS L1 C/A satellites; the
+    device suppresses it in place and the batched search runs on the same
+    device buffer.  Peaks (code phase, Doppler bin) equal the oracle chain's
+    (oracle engine, then oracle acquisition), levels within 1e-4 of its FP64
+    search."""
+    torch = pytest.importorskip("torch")
+    from conftest import unpack_codes
+    from ugsdr_gb300 import signals
+    ca = unpack_codes(golden_codes, "gps_l1ca")
+    fs, n, k = 4e6, 4000, 10
+    sats = [(3, 100.5, 1500.0), (11, 700.25, -2500.0), (17, 333.0, 500.0)]
+    ems = [signals.Emitter(ca[p], 1.023e6, cp, dop, 50.0, data_rate=0.0) for p, cp, dop in sats]
+    x = signals.synthesize(ems, fs, n * k, 0.5, "cf32", seed=21)
+    # on STFT bin 40 (1.25 MHz at 4 MHz): no magnitude near the wideband threshold
+    x = (x + 400 * np.exp(2j * np.pi * 1.25e6 * np.arange(n * k) / fs)).astype(np.complex64)
+    assert np.min(np.abs(np.abs(oracle.stft(x)) - 20.0)) > 0.02
+    det_ref, y_ref = oracle.jamming(x, fs)
+    assert det_ref and {d[0] for d in det_ref} == {1, 2}
+
+    def search(samples, on_device):
+        hs = [ctx.code_put(ca[p], n) for p, _, _ in sats]
+        try:
+            job = ctx.make_job(samples, L.SAMPLES_CF32, fs, n, k, hs, 5000, 500, n_samples=n * k, on_device=on_device)
+            return ctx.acquire(job)
+        finally:
+            for h in hs:
+                ctx.code_release(h)
+
+    # jammed: the satellites are not found at their true code phase
+    blind = search(x, False)
+    assert any(r.snr < 2.0 for r in blind)
+    d = torch.from_numpy(x.view(np.float32).copy()).cuda()
+    torch.cuda.synchronize()
+    det = ctx.jamming_suppress(d.data_ptr(), fs, n=n * k)
+    same_detections(det, det_ref)
+    res = search(d.data_ptr(), True)
+    for (p, cp, dop), r in zip(sats, res):
+        code = oracle.upsample(ca[p], n)
+        o32 = oracle.acquire(y_ref, n, k, code, fs, 5000, 500)
+        o64 = oracle.acquire(y_ref, n, k, code, fs, 5000, 500, double=True)
+        assert r.index == int(o32["index"]) and r.doppler_bin == int(o32["doppler_bin"]), (p, r, o32)
+        assert abs(r.index - cp * fs / 1.023e6) <= 1 and r.doppler == pytest.approx(dop)
+        assert abs(r.level - o64["level"]) <= 1e-4 * o64["level"]
+        assert r.snr > 3.3
