@@ -213,9 +213,11 @@ namespace ugsdr_gpu {
 		size_t smem_rows(const BatchedParams& p, bool) {
 			return 2 * sizeof(float2) * static_cast<size_t>(p.rw) * p.n2 + sizeof(float2) * p.n2 + 16;
 		}
+		// inverse rows: work tile(s), the staged X (and code) rows of hooked
+		// plans, the twiddle table
 		template <class F>
 		size_t smem_inv_rows(const BatchedParams& p) {
-			return (rows_one_tile<F>() ? 1 : 2) * sizeof(float2) * static_cast<size_t>(p.rw) * p.n2 + sizeof(float2) * p.n2 + 16;
+			return rows_tiles<F>() * sizeof(float2) * static_cast<size_t>(p.rw) * p.n2 + sizeof(float2) * p.n2 + 16;
 		}
 
 		int chunks_of(int total, int per) { return (total + per - 1) / per; }
@@ -351,7 +353,8 @@ namespace ugsdr_gpu {
 					if (s.fold_mode == 2)
 						UG_CUDA(cudaMemsetAsync(p.zcg, 0, sizeof(float2) * static_cast<size_t>(p.rows) * s.k * s.m, ctx->stream));
 				}
-				inv_rows_kernel<F2><<<p.rows * s.k * chunks_of(p.n1, p.rw), t_rows, smem_r, ctx->stream>>>(p);
+				const int row_items = F2::kHooked ? p.rows : p.rows * s.k;  // hooked: each CTA loops over the K blocks
+				inv_rows_kernel<F2><<<row_items * chunks_of(p.n1, p.rw), t_rows, smem_r, ctx->stream>>>(p);
 				inv_cols_kernel<F1><<<p.rows * chunks, t_cols, smem_c, ctx->stream>>>(p);
 				note_launch(ctx, 2);
 				if (s.fold_mode) {

@@ -112,6 +112,10 @@ namespace ugsdr_gpu {
 		const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
 		asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem));
 	}
+	__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+		const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+		asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem));
+	}
 	__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
 	__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
@@ -240,6 +244,21 @@ namespace ugsdr_gpu {
 			return cmul(__ldg(x + off), __ldg(code + off));
 		}
 	};
+	// the same gather from shared-memory copies of the CTA's rows: X of the
+	// current block, and the code rows (or, when those are not staged, the
+	// code rows straight from global memory)
+	struct InvRowsLoadStaged {
+		const float2* xs;
+		const float2* cs;
+		const float2* code_g;
+		int n1, n2, r0, half, one_sided;
+		__device__ __forceinline__ float2 operator()(int f, int k2) const {
+			if (one_sided && (r0 + f) + n1 * k2 > half)
+				return c2(0.f, 0.f);
+			const int off = f * n2 + k2;
+			return cmul(xs[off], cs ? cs[off] : __ldg(code_g + off));
+		}
+	};
 	struct InvRowsEmit {
 		float2* out;
 		int n2, r0;
@@ -292,18 +311,81 @@ namespace ugsdr_gpu {
 		}
 	};
 
-	// grid: rows * K * ceil(N1 / rw)
-	// a compact plan (hooked, two passes) gathers pass 0 from global memory:
-	// one shared tile, and more CTAs per SM to hide the gathers' latency
+	// a compact plan (hooked, two passes) gathers pass 0 from its staged
+	// rows: one work tile
 	template <class F>
 	constexpr bool rows_one_tile() { return F::kRowsCompact; }
+	// hooked plans run one CTA per (row, chunk of rw sub-rows) over all K
+	// blocks: X of block k + 1 is copied in while block k's last pass runs,
+	// and the code rows (the same for every block) are staged once when
+	// three row tiles still leave four CTAs per SM (N2 <= 256)
+	template <class F>
+	constexpr bool rows_stage_code() { return F::kHooked && F::N <= 256; }
+	template <class F>
+	constexpr int rows_tiles() {
+		return (rows_one_tile<F>() ? 1 : 2) + (F::kHooked ? 1 : 0) + (rows_stage_code<F>() ? 1 : 0);
+	}
 
+	// hooked plans: grid rows * ceil(N1 / rw), each CTA over the K blocks;
+	// others: grid rows * K * ceil(N1 / rw)
 	template <class F2>
 	__global__ void __launch_bounds__(F2::kRowsMaxThreads, F2::kRowsMinBlocks) inv_rows_kernel(BatchedParams p) {
 		extern __shared__ float2 smem[];
 		const AcqParams& q = p.base;
 		const int n1 = p.n1, n2 = fft_n<F2>(p.n2), n = q.n;
 		const int chunks = (n1 + p.rw - 1) / p.rw;
+		const int half = n / 2;
+		const int tile = p.rw * n2;
+		float2* a = smem;
+		float2* b = rows_one_tile<F2>() ? smem : smem + tile;
+		if constexpr (F2::kHooked) {
+			const int lrow = blockIdx.x / chunks;
+			const int r0 = (blockIdx.x - lrow * chunks) * p.rw;
+			const int rw = min(p.rw, n1 - r0);
+			const int row = p.row0 + lrow;
+			const int c = row % q.n_codes;
+			const int d = row / q.n_codes;
+			float2* xs = b + tile;
+			float2* cs = rows_stage_code<F2>() ? xs + tile : nullptr;
+			const FftPlanDev p2 = F2::prepare(p.p2, smem + rows_tiles<F2>() * tile);
+			const float2* code = q.codes[c] + static_cast<size_t>(r0) * n2;
+			const float2* xg = q.spectra + static_cast<size_t>(d) * q.k_blocks * n + static_cast<size_t>(r0) * n2;
+			const int elems = rw * n2;
+			// 16-byte copies when every row start is 16-byte aligned
+			const bool wide = (n2 % 2 == 0) && (n % 2 == 0);
+			auto copy_rows = [&](float2* dst, const float2* src) {
+				if (wide) {
+					for (int e = 2 * threadIdx.x; e < elems; e += 2 * blockDim.x)
+						cp_async16(dst + e, src + e);
+				}
+				else {
+					for (int e = threadIdx.x; e < elems; e += blockDim.x)
+						cp_async8(dst + e, src + e);
+				}
+			};
+			if (cs)
+				copy_rows(cs, code);
+			copy_rows(xs, xg);
+			cp_async_commit();
+			const InvRowsLoadStaged load{xs, cs, code, n1, n2, r0, half, q.one_sided};
+			for (int blk = 0; blk < q.k_blocks; ++blk) {
+				cp_async_wait_all();
+				__syncthreads();  // this block's X (and the twiddle table) in shared memory
+				const size_t item = static_cast<size_t>(lrow) * q.k_blocks + blk;
+				const InvRowsEmit emit{p.bbuf + item * n + static_cast<size_t>(r0) * n2, n2, r0, static_cast<uint32_t>(n),
+					2.0f / static_cast<float>(n)};
+				auto next = [&] {  // pass 0 has read xs: the next block's X goes there
+					if (blk + 1 < q.k_blocks) {
+						copy_rows(xs, xg + static_cast<size_t>(blk + 1) * n);
+						cp_async_commit();
+					}
+				};
+				F2::template run_hooked<true, true>(a, b, p2, rw, n2, load, emit, next);
+				// the next iteration's first barrier orders this block's last-pass
+				// reads of `b` before its first pass writes it again
+			}
+			return;
+		}
 		const int item = blockIdx.x / chunks;       // (local row, block)
 		const int r0 = (blockIdx.x - item * chunks) * p.rw;
 		const int rw = min(p.rw, n1 - r0);
@@ -314,19 +396,8 @@ namespace ugsdr_gpu {
 		const int d = row / q.n_codes;
 		const float2* x = q.spectra + (static_cast<size_t>(d) * q.k_blocks + blk) * n + static_cast<size_t>(r0) * n2;
 		const float2* code = q.codes[c] + static_cast<size_t>(r0) * n2;
-		float2* a = smem;
-		float2* b = rows_one_tile<F2>() ? smem : smem + p.rw * n2;
-		const FftPlanDev p2 = F2::prepare(p.p2, smem + (rows_one_tile<F2>() ? 1 : 2) * p.rw * n2);
-		const int half = n / 2;
+		const FftPlanDev p2 = F2::prepare(p.p2, smem + (rows_one_tile<F2>() ? 1 : 2) * tile);
 		const float inv_n2f = 1.0f / static_cast<float>(n2);
-		if constexpr (F2::kHooked) {
-			float2* out = p.bbuf + static_cast<size_t>(item) * n + static_cast<size_t>(r0) * n2;
-			const InvRowsLoad load{x, code, n1, n2, r0, half, q.one_sided};
-			const InvRowsEmit emit{out, n2, r0, static_cast<uint32_t>(n), 2.0f / static_cast<float>(n)};
-			__syncthreads();  // twiddle table in shared memory
-			F2::template run_hooked<true, true>(a, b, p2, rw, n2, load, emit);
-			return;
-		}
 		// Z = X * C, four element pairs in flight per thread
 		const int total = rw * n2;
 		for (int e0 = threadIdx.x; e0 < total; e0 += 4 * blockDim.x) {
