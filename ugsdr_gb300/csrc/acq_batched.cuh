@@ -317,10 +317,11 @@ namespace ugsdr_gpu {
 	constexpr bool rows_one_tile() { return F::kRowsCompact; }
 	// hooked plans run one CTA per (row, chunk of rw sub-rows) over all K
 	// blocks: X of block k + 1 is copied in while block k's last pass runs,
-	// and the code rows (the same for every block) are staged once when
-	// three row tiles still leave four CTAs per SM (N2 <= 256)
+	// and the code rows (the same for every block) are staged once (N2 <= 512:
+	// for 500-point rows three 32 KB tiles leave two CTAs per SM, still
+	// faster than re-reading the code rows from L2 for every block)
 	template <class F>
-	constexpr bool rows_stage_code() { return F::kHooked && F::N <= 256; }
+	constexpr bool rows_stage_code() { return F::kHooked && F::N <= 512; }
 	template <class F>
 	constexpr int rows_tiles() {
 		return (rows_one_tile<F>() ? 1 : 2) + (F::kHooked ? 1 : 0) + (rows_stage_code<F>() ? 1 : 0);
