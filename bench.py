@@ -179,9 +179,9 @@ def inverse_flops(j):
 
 
 # DRAM bytes per inverse-transform point of the four-step kernels (inv_rows +
-# inv_cols), measured with ncu on the 200,000- and 50,000-point profiling cases
-# (15.6 and 15.7; the intermediate B buffer is 14.5 of it); see profiles/.
-TRAFFIC_BYTES_PER_INVERSE_POINT = 15.6
+# inv_cols), measured with ncu on the 200,000-point profiling case (17.5: the
+# intermediate B buffer is 16 of it); see profiles/.
+TRAFFIC_BYTES_PER_INVERSE_POINT = 17.5
 
 
 def inverse_points(j):
@@ -358,7 +358,7 @@ def run_ours(args, world, rank):
         "gpu_launches": launches,
         "roofline": {"bound": "fp32", "kernel": inv_name, "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": achieved / fp32_peak if achieved else None, "traffic": traffic,
-                     "traffic_source": "ncu dram__bytes_read+write per inverse point (15.6 B, 200k/50k profiling "
+                     "traffic_source": "ncu dram__bytes_read+write per inverse point (17.5 B, 200k profiling "
                                        "cases) x points per launch" if traffic else None,
                      "algorithmic_bytes_per_launch": bytes_inv / max(n_inv, 1),
                      "peak_source": f"{n_sm} SMs x 128 FP32 lanes x 2 x sm_max_mhz {sm_max} (MEASURED_PEAKS.json)",
