@@ -259,7 +259,8 @@ namespace ugsdr_gpu {
 				}
 				const size_t smem = smem_rows(p, false);
 				set_smem(fwd_rows_kernel<F2>, smem);
-				fwd_rows_kernel<F2><<<items * chunks_of(p.n1, p.rw), threads_of<F2>(p.p2, p.rw), smem, ctx->stream>>>(p);
+				const int groups = F2::kRowsCompact ? (items + kFwdRowItems - 1) / kFwdRowItems : items;
+				fwd_rows_kernel<F2><<<groups * chunks_of(p.n1, p.rw), threads_of<F2>(p.p2, p.rw), smem, ctx->stream>>>(p, items);
 			});
 			note_launch(ctx, 2);
 		}

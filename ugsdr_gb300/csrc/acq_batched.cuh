@@ -187,20 +187,100 @@ namespace ugsdr_gpu {
 		const float2* y = F1::template run<false>(a, b, p1, cw, ld);
 		float2* out = p.out + static_cast<size_t>(item) * p.base.n;
 		const float inv_n2 = 2.0f / static_cast<float>(p.base.n);
-		for (int e = threadIdx.x; e < p.cw * n1; e += blockDim.x) {
-			const int f = e & mask, k1 = e >> p.cw_shift;
-			if (f < cw)
-				out[static_cast<size_t>(k1) * n2 + c0 + f] =
-					cmul(y[f * ld + k1], tw_n(static_cast<uint32_t>(c0 + f) * static_cast<uint32_t>(k1), p.base.n, inv_n2, false));
+		// inter-step twiddle W_N^{(c0 + f) k1}: a thread keeps its column f
+		// (the block is a multiple of cw) and steps k1 by blockDim / cw, so its
+		// twiddle advances by a fixed W_N^{(c0 + f) blockDim / cw} (two
+		// sincospif per thread, at most N1 cw / blockDim products in the chain)
+		const uint32_t nn = static_cast<uint32_t>(p.base.n);
+		const int e0 = threadIdx.x, f0 = e0 & mask;
+		const uint32_t col = static_cast<uint32_t>(c0 + f0);
+		float2 w = tw_n((col * static_cast<uint32_t>(e0 >> p.cw_shift)) % nn, p.base.n, inv_n2, false);
+		const float2 step = tw_n((col * static_cast<uint32_t>(blockDim.x >> p.cw_shift)) % nn, p.base.n, inv_n2, false);
+		for (int e = e0; e < p.cw * n1; e += blockDim.x) {
+			const int k1 = e >> p.cw_shift;
+			if (f0 < cw)
+				out[static_cast<size_t>(k1) * n2 + c0 + f0] = cmul(y[f0 * ld + k1], w);
+			w = cmul(w, step);
 		}
 	}
 
-	// grid: items * ceil(N1 / rw); code mode also conjugates and masks (conj(FFT(code)))
+	// Row stage of the forward transform, hooked plans: pass 0 reads the
+	// CTA's staged rows, the last pass stores the spectrum (one-sided: bins
+	// above N/2 are never read, so they are not written; code mode conjugates
+	// and zeroes them: conj(FFT(code)))
+	struct FwdRowsLoad {
+		const float2* xs;
+		int n2;
+		__device__ __forceinline__ float2 operator()(int f, int k2) const { return xs[f * n2 + k2]; }
+	};
+	struct FwdRowsEmit {
+		float2* out;
+		int n1, n2, r0, half, one_sided, code_mode;
+		template <int R, int NS>
+		__device__ __forceinline__ void put(int f, int base, const float2 (&v)[R]) const {
+			float2* o = out + static_cast<size_t>(f) * n2 + base;
+#pragma unroll
+			for (int r = 0; r < R; ++r) {
+				const int k2 = base + r * NS;
+				const bool zero = one_sided && (r0 + f) + static_cast<int64_t>(n1) * k2 > half;
+				if (code_mode)
+					o[r * NS] = zero ? c2(0.f, 0.f) : c2(v[r].x, -v[r].y);
+				else if (!zero)
+					o[r * NS] = v[r];
+			}
+		}
+	};
+	// items per CTA of the hooked forward rows
+	constexpr int kFwdRowItems = 4;
+
+	// grid: items * ceil(N1 / rw), or for compact plans ceil(items / 4) *
+	// ceil(N1 / rw) with each CTA over up to four items (the next item's rows
+	// copied in while the current item's last pass runs); code mode also
+	// conjugates and masks (conj(FFT(code)))
 	template <class F2>
-	__global__ void __launch_bounds__(256, 3) fwd_rows_kernel(BatchedParams p) {
+	__global__ void __launch_bounds__(256, 3) fwd_rows_kernel(BatchedParams p, int items) {
 		extern __shared__ float2 smem[];
 		const int n1 = p.n1, n2 = fft_n<F2>(p.n2);
 		const int chunks = (n1 + p.rw - 1) / p.rw;
+		if constexpr (F2::kRowsCompact) {  // hooked, two passes: one work tile (pass 1 emits)
+			const int group = blockIdx.x / chunks;
+			const int r0 = (blockIdx.x - group * chunks) * p.rw;
+			const int rw = min(p.rw, n1 - r0);
+			const int tile = p.rw * n2;
+			float2* b = smem;
+			float2* xs = smem + tile;
+			const FftPlanDev p2 = F2::prepare(p.p2, smem + 2 * tile);
+			const int it0 = group * kFwdRowItems;
+			const int it1 = min(items, it0 + kFwdRowItems);
+			const int elems = rw * n2;
+			const bool wide = (n2 % 2 == 0) && (p.base.n % 2 == 0);
+			auto copy_rows = [&](int item) {
+				const float2* src = p.out + static_cast<size_t>(item) * p.base.n + static_cast<size_t>(r0) * n2;
+				if (wide) {
+					for (int e = 2 * threadIdx.x; e < elems; e += 2 * blockDim.x)
+						cp_async16(xs + e, src + e);
+				}
+				else {
+					for (int e = threadIdx.x; e < elems; e += blockDim.x)
+						cp_async8(xs + e, src + e);
+				}
+				cp_async_commit();
+			};
+			copy_rows(it0);
+			const FwdRowsLoad load{xs, n2};
+			for (int item = it0; item < it1; ++item) {
+				cp_async_wait_all();
+				__syncthreads();
+				const FwdRowsEmit emit{p.out + static_cast<size_t>(item) * p.base.n + static_cast<size_t>(r0) * n2, n1, n2, r0,
+					p.base.n / 2, p.base.one_sided, p.code_mode};
+				auto next = [&] {
+					if (item + 1 < it1)
+						copy_rows(item + 1);
+				};
+				F2::template run_hooked<false, true>(b, b, p2, rw, n2, load, emit, next);
+			}
+			return;
+		}
 		const int item = blockIdx.x / chunks;
 		const int r0 = (blockIdx.x - item * chunks) * p.rw;
 		const int rw = min(p.rw, n1 - r0);
