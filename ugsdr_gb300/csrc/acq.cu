@@ -106,19 +106,24 @@ namespace ugsdr_gpu {
 		const size_t budget = ctx->smem_optin - 2048;
 		int best1 = 0;
 		std::vector<int> r;
-		for (int a = 2; static_cast<long>(a) * a <= n; ++a) {
-			if (n % a)
-				continue;
-			const int b = n / a;
-			if (!plan_radices(a, r) || !plan_radices(b, r))
-				continue;
-			// both kernels' tiles and twiddle tables must fit with at least
-			// 4 columns (inverse: 3 tiles + accumulator) and 1 row (2 tiles)
-			const size_t cols = (3 * sizeof(float2) + sizeof(float)) * 4 * static_cast<size_t>(a | 1) + sizeof(float2) * a + 16;
-			const size_t rows = 3 * sizeof(float2) * static_cast<size_t>(b) + 16;
-			if (cols > budget || rows > budget)
-				continue;
-			best1 = a;  // increasing a -> closest to sqrt(n) last
+		// both kernels' tiles and twiddle tables must fit with at least
+		// 4 columns (inverse: 3 tiles + accumulator) and 1 row (2 tiles); the
+		// largest sizes (beyond ~1.8e7 points) fall back to single columns
+		for (const int min_cols : {4, 1}) {
+			for (int a = 2; static_cast<long>(a) * a <= n; ++a) {
+				if (n % a)
+					continue;
+				const int b = n / a;
+				if (!plan_radices(a, r) || !plan_radices(b, r))
+					continue;
+				const size_t cols = (3 * sizeof(float2) + sizeof(float)) * min_cols * static_cast<size_t>(a | 1) + sizeof(float2) * a + 16;
+				const size_t rows = 3 * sizeof(float2) * static_cast<size_t>(b) + 16;
+				if (cols > budget || rows > budget)
+					continue;
+				best1 = a;  // increasing a -> closest to sqrt(n) last
+			}
+			if (best1 > 0)
+				break;
 		}
 		require(best1 > 0, "no four-step split for FFT size " + std::to_string(n), UGSDR_E_UNSUPPORTED);
 		LargePlan lp;
@@ -127,8 +132,6 @@ namespace ugsdr_gpu {
 		lp.n2 = n / best1;
 		lp.p1 = get_plan(ctx, lp.n1);
 		lp.p2 = get_plan(ctx, lp.n2);
-		upload_twiddles(ctx, n);
-		lp.tw = ctx->twiddles[n]->as<float2>();
 		return ctx->large_plans[n] = lp;
 	}
 
@@ -318,6 +321,27 @@ namespace ugsdr_gpu {
 		p.out = e.spectrum.as<float2>();
 		launch_forward(ctx, UGSDR_SAMPLES_CF32, p, 1);
 		UG_CUDA(cudaStreamSynchronize(ctx->stream));
+	}
+
+	// One forward DFT of a whole device array on the batched four-step kernels
+	// (one item; the mixer's zero adder multiplies by table[16] + i table[0] =
+	// 1 + 0i exactly): output k1-major, X_T[k1][k2] = X[k1 + N1 k2].
+	void dft_four_step(ugsdr_ctx* ctx, const float2* in, float2* out_k1, int n, int& n1, int& n2) {
+		if (!ctx->zero_adder.ptr) {
+			ctx->zero_adder.reserve(sizeof(uint32_t));
+			UG_CUDA(cudaMemsetAsync(ctx->zero_adder.ptr, 0, sizeof(uint32_t), ctx->stream));
+		}
+		AcqParams base{};
+		base.n = n;
+		base.k_blocks = 1;
+		base.samples = in;
+		base.lut = get_lut(ctx);
+		base.adders = ctx->zero_adder.as<uint32_t>();
+		BatchedParams p = batched_params(ctx, base, n);
+		p.out = out_k1;
+		launch_forward(ctx, UGSDR_SAMPLES_CF32, p, 1);
+		n1 = p.n1;
+		n2 = p.n2;
 	}
 
 	// One Doppler chunk of nd bins (base.d_base first): forward over nd x K

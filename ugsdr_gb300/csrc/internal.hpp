@@ -84,11 +84,7 @@ namespace ugsdr_gpu {
 	struct LargePlan {
 		int n = 0;
 		int n1 = 0, n2 = 0;
-		FftPlanDesc p1, p2;    // N1-point and N2-point plans
-		const float2* tw = nullptr;  // N-point table for the inter-step twiddle
-		// two-level table: W_N^e = hi[e >> 8] * lo[e & 255]; lo has 256 entries, hi n_hi
-		const float2* tw_lohi = nullptr;
-		int n_hi = 0;
+		FftPlanDesc p1, p2;    // N1-point and N2-point plans (the inter-step twiddles are computed in the kernels)
 	};
 
 	struct CodeEntry {
@@ -136,7 +132,6 @@ struct ugsdr_ctx {
 
 	// twiddle tables and plans per size
 	std::map<int, std::unique_ptr<ugsdr_gpu::DevBuf>> twiddles;
-	std::map<int, std::unique_ptr<ugsdr_gpu::DevBuf>> twiddles_lohi;
 	std::map<int, ugsdr_gpu::FftPlanDesc> plans;
 	std::map<int, ugsdr_gpu::LargePlan> large_plans;
 
@@ -146,6 +141,7 @@ struct ugsdr_ctx {
 
 	// scratch
 	ugsdr_gpu::DevBuf lut;        // float[80] TableMixer sine table
+	ugsdr_gpu::DevBuf zero_adder; // uint32 0: an NCO that leaves samples unchanged
 	ugsdr_gpu::Workspace ws;      // acquisition scratch of the synchronous entry points
 	ugsdr_gpu::DevBuf op_a, op_b, op_c;  // per-op entry staging
 	// interference stage: staged samples, STFT spectra, inverse columns /
@@ -208,6 +204,10 @@ namespace ugsdr_gpu {
 			return UGSDR_E_INVALID;
 		}
 	}
+
+	// forward DFT of a device array (n with a four-step split) on the batched
+	// kernels, output k1-major; n1, n2 receive the split (acq.cu)
+	void dft_four_step(ugsdr_ctx* ctx, const float2* in, float2* out_k1, int n, int& n1, int& n2);
 
 	// complex DFT device to device with the reference's scaling: forward
 	// unnormalised, inverse (v / n) * 2 (ops.cu); `in` and `out` distinct

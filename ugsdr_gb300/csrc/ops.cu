@@ -4,7 +4,6 @@
 // every call stages through the context's device scratch on its stream.
 #include "internal.hpp"
 #include "acq_kernels.cuh"
-#include "four_step.cuh"
 #include "dfe.cuh"
 #include "packed.cuh"
 #include "fft_plan.hpp"
@@ -61,16 +60,6 @@ namespace ugsdr_gpu {
 				out[i] = scale == 1.0f ? y[i] : cscale(y[i], scale);
 		}
 
-		// four-step forward of one array (k1-major output) for sizes above one CTA
-		__global__ void __launch_bounds__(512) dft_large_kernel(LargeParams p, const float2* in, int conj_in) {
-			extern __shared__ float2 sm[];
-			const int tile = max(p.cw * p.n1, p.rw * p.n2);
-			four_step_forward(p, sm, sm + tile, p.code_out, [&](int64_t i) {
-				const float2 v = in[i];
-				return conj_in ? c2(v.x, -v.y) : v;
-			});
-		}
-
 		// k1-major (X_T[k1][k2] = X[k1 + N1 k2]) -> natural order, optional conj and scale
 		__global__ void untranspose_kernel(const float2* t, float2* out, int n1, int n2, int conj_out, float scale) {
 			const size_t n = static_cast<size_t>(n1) * n2;
@@ -81,6 +70,11 @@ namespace ugsdr_gpu {
 					v.y = -v.y;
 				out[k1 + static_cast<size_t>(n1) * k2] = scale == 1.0f ? v : cscale(v, scale);
 			}
+		}
+
+		__global__ void conj_kernel(const float2* in, float2* out, size_t n) {
+			for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n; i += static_cast<size_t>(gridDim.x) * blockDim.x)
+				out[i] = c2(in[i].x, -in[i].y);
 		}
 
 		__global__ void cmul_kernel(float2* x, const float2* s, size_t n) {
@@ -357,7 +351,7 @@ namespace ugsdr_gpu {
 
 		// complex DFT device->device: out = DFT(in) (unnormalised, sign by `inverse`)
 		void dft_device(ugsdr_ctx* ctx, const float2* in, float2* out, size_t n, bool inverse, DevBuf& tmp) {
-			require(n >= 2 && n <= (1u << 24), "DFT size out of range");
+			require(n >= 2 && n <= (1u << 28), "DFT size out of range");
 			const int ni = static_cast<int>(n);
 			if (!plannable(ni)) {
 				// inverse via conj(DFT(conj(x)))
@@ -381,29 +375,21 @@ namespace ugsdr_gpu {
 				note_launch(ctx);
 				return;
 			}
-			const LargePlan& lp = get_large_plan(ctx, ni);
-			LargeParams p{};
-			p.base.n = ni;
-			p.p1 = dev_plan(lp.p1);
-			p.p2 = dev_plan(lp.p2);
-			p.n1 = lp.n1;
-			p.n2 = lp.n2;
-			const size_t budget = ctx->smem_optin - 2048;
-			p.cw = 16;
-			while (p.cw > 4 && 2 * sizeof(float2) * p.cw * static_cast<size_t>(lp.n1) > budget)
-				p.cw /= 2;
-			p.rw = 16;
-			while (p.rw > 1 && 2 * sizeof(float2) * p.rw * static_cast<size_t>(lp.n2) > budget)
-				p.rw /= 2;
-			p.tw = lp.tw;
-			tmp.reserve(sizeof(float2) * n);
-			p.code_out = tmp.as<float2>();
-			const size_t smem = 2 * sizeof(float2) * std::max(p.cw * lp.n1, p.rw * lp.n2);
-			smem_attr(dft_large_kernel, smem);
-			// inverse via conj(DFT(conj(x)))
-			dft_large_kernel<<<1, 512, smem, ctx->stream>>>(p, in, inverse ? 1 : 0);
-			untranspose_kernel<<<blocks_for(n), kT, 0, ctx->stream>>>(tmp.as<float2>(), out, lp.n1, lp.n2, inverse ? 1 : 0, 1.0f);
-			note_launch(ctx, 2);
+			// the batched four-step kernels over the whole GPU; the inverse as
+			// conj(DFT(conj(x)))
+			tmp.reserve(2 * sizeof(float2) * n);  // k1-major spectrum, conjugated input
+			float2* spec = tmp.as<float2>();
+			const float2* src = in;
+			if (inverse) {
+				float2* c = spec + n;
+				conj_kernel<<<blocks_for(n), kT, 0, ctx->stream>>>(in, c, n);
+				note_launch(ctx);
+				src = c;
+			}
+			int n1 = 0, n2 = 0;
+			dft_four_step(ctx, src, spec, ni, n1, n2);
+			untranspose_kernel<<<blocks_for(n), kT, 0, ctx->stream>>>(spec, out, n1, n2, inverse ? 1 : 0, 1.0f);
+			note_launch(ctx);
 		}
 	}
 
