@@ -45,6 +45,21 @@ def test_dft_large_vs_oracle(ctx, oracle, n):
         assert np.abs(out - ref).max() <= 2e-5 * np.abs(ref).max()
 
 
+def test_dft_beyond_four_step_columns(ctx):
+    """2e7 points (400 ms at 50 MHz, the whole-signal DFT of the narrowband
+    interference filter): past the size where four-column tiles fit, the
+    split falls back to single columns.  numpy's FP64 FFT is the reference;
+    the inverse carries the reference's 2/N scale."""
+    n = 20_000_000
+    rng = np.random.default_rng(20)
+    v = (rng.normal(size=n) + 1j * rng.normal(size=n)).astype(np.complex64)
+    ref = np.fft.fft(v.astype(np.complex128))
+    out = ctx.dft(v)
+    assert np.abs(out - ref).max() <= 2e-5 * np.abs(ref).max()
+    back = ctx.dft(out, True)
+    assert np.abs(back - 2 * v).max() <= 2e-5 * 2 * np.abs(v).max()
+
+
 @pytest.mark.parametrize("name", ["glo", "ca4000"])
 def test_matched_filter(ctx, kats, name):
     code = kats[f"mf_code_{name}"]
