@@ -566,7 +566,58 @@ namespace ugsdr_gpu {
 		(void)best_bin;
 	}
 
+	namespace {
+		// single-CTA block sizes with a compile-time plan (4000: 1 ms at 4 MHz)
+		template <class Fn>
+		bool with_small_fft(int n, Fn&& fn) {
+			if (n == 4000) {
+				fn(StaticFft<4000, 25, 10, 16>{});
+				return true;
+			}
+			return false;
+		}
+
+		template <class F>
+		void launch_small_static(ugsdr_ctx* ctx, const ugsdr_acq_job& job, const AcqParams& p, int nd, int k, int n_codes) {
+			const size_t smem_f = 3 * sizeof(float2) * F::N + 16;
+			const int grid_f = nd * k;
+			{
+				KernelTimer timer(ctx, "acq_forward");
+				switch (job.sample_type) {
+				case UGSDR_SAMPLES_CF32:
+					set_smem(acq_forward_static_kernel<UGSDR_SAMPLES_CF32, F>, smem_f);
+					acq_forward_static_kernel<UGSDR_SAMPLES_CF32, F><<<grid_f, kThreads, smem_f, ctx->stream>>>(p);
+					break;
+				case UGSDR_SAMPLES_CI8:
+					set_smem(acq_forward_static_kernel<UGSDR_SAMPLES_CI8, F>, smem_f);
+					acq_forward_static_kernel<UGSDR_SAMPLES_CI8, F><<<grid_f, kThreads, smem_f, ctx->stream>>>(p);
+					break;
+				case UGSDR_SAMPLES_CI16:
+					set_smem(acq_forward_static_kernel<UGSDR_SAMPLES_CI16, F>, smem_f);
+					acq_forward_static_kernel<UGSDR_SAMPLES_CI16, F><<<grid_f, kThreads, smem_f, ctx->stream>>>(p);
+					break;
+				default:
+					set_smem(acq_forward_static_kernel<UGSDR_SAMPLES_RI8, F>, smem_f);
+					acq_forward_static_kernel<UGSDR_SAMPLES_RI8, F><<<grid_f, kThreads, smem_f, ctx->stream>>>(p);
+					break;
+				}
+			}
+			note_launch(ctx);
+			// a, b, the N-float accumulator, the pass tables (N entries)
+			const size_t smem_i = 2 * sizeof(float2) * F::N + sizeof(float) * F::N + sizeof(float2) * F::N + 16;
+			set_smem(acq_inverse_static_kernel<F>, smem_i);
+			KernelTimer timer(ctx, "acq_inverse");
+			acq_inverse_static_kernel<F><<<nd * n_codes, kThreads, smem_i, ctx->stream>>>(p);
+			note_launch(ctx);
+		}
+	}
+
 	void launch_chunk(ugsdr_ctx* ctx, const ugsdr_acq_job& job, const JobLaunch& L, AcqParams& p, int nd, char* scratch) {
+		if (!L.large && L.fold_mode == 0 && L.m == L.n && L.n == 4000) {
+			p.plan = to_dev(get_plan(ctx, L.n));
+			with_small_fft(L.n, [&](auto f) { launch_small_static<decltype(f)>(ctx, job, p, nd, L.k, L.n_codes); });
+			return;
+		}
 		if (!L.large) {
 			p.plan = to_dev(get_plan(ctx, L.n));
 			const size_t smem_f = 2 * sizeof(float2) * L.n;

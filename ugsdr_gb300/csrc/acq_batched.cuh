@@ -142,6 +142,100 @@ namespace ugsdr_gpu {
 		float2* zcg;            // fold mode 2: [row - row0][block][M]
 	};
 
+	// ----------------------------------------- single CTA, compile-time plan
+	// acq_forward_kernel / acq_inverse_kernel for a block size whose plan is a
+	// type (F::N): the mix-and-load is pass 0's gather and the spectrum store
+	// (forward) or the |.| accumulation (inverse, unfolded) its last pass.
+	template <int ST>
+	struct SmallFwdLoad {
+		const void* samples;
+		const float* lut;
+		uint64_t base;
+		uint32_t adder, fe_adder, phase0;
+		int fe_on;
+		__device__ __forceinline__ float2 operator()(int, int i) const {
+			const uint64_t g = base + static_cast<uint64_t>(i);
+			float2 v = load_sample<ST>(samples, g);
+			if (fe_on)
+				v = table_mix(v, g, fe_adder, 0u, lut);
+			return table_mix(v, g, adder, phase0, lut);
+		}
+	};
+	struct SmallFwdEmit {
+		float2* dst;
+		int limit;  // one-sided: bins 0..N/2
+		template <int R, int NS>
+		__device__ __forceinline__ void put(int, int base, const float2 (&v)[R]) const {
+#pragma unroll
+			for (int r = 0; r < R; ++r)
+				if (base + r * NS < limit)
+					dst[base + r * NS] = v[r];
+		}
+	};
+	// grid: Doppler bins x K blocks, one transform each
+	template <int ST, class F>
+	__global__ void __launch_bounds__(256) acq_forward_static_kernel(AcqParams p) {
+		extern __shared__ float2 smem[];
+		__shared__ float lut[80];
+		float2* a = smem;
+		float2* b = smem + F::N;
+		const FftPlanDev plan = F::prepare(p.plan, smem + 2 * F::N);
+		if (threadIdx.x < 80)
+			lut[threadIdx.x] = p.lut[threadIdx.x];
+		__syncthreads();
+		const int d = blockIdx.x / p.k_blocks;
+		const int blk = blockIdx.x - d * p.k_blocks;
+		const SmallFwdLoad<ST> load{p.samples, lut, static_cast<uint64_t>(blk) * F::N, p.adders[p.d_base + d], p.fe_adder,
+			p.phase0, p.fe_on};
+		const SmallFwdEmit emit{p.spectra + (static_cast<size_t>(d) * p.k_blocks + blk) * F::N, p.one_sided ? F::N / 2 + 1 : F::N};
+		F::template run_hooked<false, true>(a, b, plan, 1, F::N, load, emit);
+	}
+
+	struct SmallInvLoad {
+		const float2* x;
+		const float2* code;
+		int half, one_sided;
+		__device__ __forceinline__ float2 operator()(int, int i) const {
+			return (one_sided && i > half) ? c2(0.f, 0.f) : cmul(__ldg(x + i), __ldg(code + i));
+		}
+	};
+	struct SmallInvEmit {
+		float* acc;
+		float inv_n, post;
+		int stat;
+		template <int R, int NS>
+		__device__ __forceinline__ void put(int, int base, const float2 (&v)[R]) const {
+#pragma unroll
+			for (int r = 0; r < R; ++r)
+				acc[base + r * NS] += stat_of(cscale(cscale(v[r], inv_n), post), stat);
+		}
+	};
+	// grid: codes x Doppler bins; unfolded rows (m == N) only.  Each thread
+	// owns the same last-pass outputs in every block, so its accumulator
+	// entries need no barrier between blocks.
+	template <class F>
+	__global__ void __launch_bounds__(256) acq_inverse_static_kernel(AcqParams p) {
+		extern __shared__ float2 smem[];
+		float2* a = smem;
+		float2* b = smem + F::N;
+		float* acc = reinterpret_cast<float*>(smem + 2 * F::N);
+		const FftPlanDev plan = F::prepare(p.plan, acc + F::N);
+		const int row = blockIdx.x;
+		const int c = row % p.n_codes;
+		const int d = row / p.n_codes;
+		for (int i = threadIdx.x; i < F::N; i += blockDim.x)
+			acc[i] = 0.f;
+		__syncthreads();
+		const SmallInvEmit emit{acc, 1.0f / static_cast<float>(F::N), p.one_sided ? 2.0f : 1.0f, p.stat};
+		for (int blk = 0; blk < p.k_blocks; ++blk) {
+			const SmallInvLoad load{p.spectra + (static_cast<size_t>(d) * p.k_blocks + blk) * F::N, p.codes[c], F::N / 2,
+				p.one_sided};
+			F::template run_hooked<true, true>(a, b, plan, 1, F::N, load, emit);
+			__syncthreads();  // pass 0 of the next block rewrites the tiles
+		}
+		reduce_cell(acc, F::N, p.cells + static_cast<size_t>(c) * p.n_doppler + p.d_base + d);
+	}
+
 	// ------------------------------------------------------------- forward
 	template <int ST>
 	__device__ __forceinline__ float2 fwd_load(const BatchedParams& p, int item, int64_t i, const float* lut) {
