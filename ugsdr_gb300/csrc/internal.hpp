@@ -148,6 +148,10 @@ struct ugsdr_ctx {
 	// whole-signal spectrum, per-column candidates, DFT scratch, window
 	ugsdr_gpu::DevBuf jam_x, jam_s, jam_t, jam_cand, jam_tmp, jam_window;
 	int jam_window_len = 0;
+	// tracking banks' staging (host captures, decoded packed captures, host
+	// outputs): shared by the context's banks, whose calls the context
+	// serialises on its stream, and kept between banks
+	ugsdr_gpu::DevBuf track_samples, track_unpacked, track_out;
 	int sm_count = 0;
 	size_t smem_optin = 0;
 

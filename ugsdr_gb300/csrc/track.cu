@@ -487,7 +487,7 @@ struct ugsdr_track_bank {
 	size_t spm = 0;
 	double offsets[5] = {};
 	double k1_pll = 0, k2_pll = 0, k3_pll = 0, k1_dll = 0, k2_dll = 0;
-	DevBuf chips, states, samples, out, unpacked;
+	DevBuf chips, states;
 };
 
 namespace {
@@ -503,20 +503,20 @@ namespace {
 		const size_t bytes = capture_bytes(sample_type, bank->fs, n);
 		const void* dev = samples;
 		if (!samples_on_device) {
-			bank->samples.reserve(bytes);
-			UG_CUDA(cudaMemcpyAsync(bank->samples.ptr, samples, bytes, cudaMemcpyHostToDevice, ctx->stream));
-			dev = bank->samples.ptr;
+			ctx->track_samples.reserve(bytes);
+			UG_CUDA(cudaMemcpyAsync(ctx->track_samples.ptr, samples, bytes, cudaMemcpyHostToDevice, ctx->stream));
+			dev = ctx->track_samples.ptr;
 		}
 		if (is_packed(sample_type)) {
 			// packed captures (BBP DDC, NT1065) are decoded to complex float first
 			PackedLayout l;
 			l.spm = static_cast<uint32_t>(bank->spm);
 			l.epoch_bytes = static_cast<uint32_t>(bbp_epoch_bytes(bank->fs));
-			bank->unpacked.reserve(sizeof(float2) * n);
+			ctx->track_unpacked.reserve(sizeof(float2) * n);
 			const int blocks = static_cast<int>(std::min<size_t>((n + 255) / 256, static_cast<size_t>(ctx->sm_count) * 8));
-			unpack_kernel<<<blocks, 256, 0, ctx->stream>>>(dev, sample_type, l, n, bank->unpacked.as<float2>());
+			unpack_kernel<<<blocks, 256, 0, ctx->stream>>>(dev, sample_type, l, n, ctx->track_unpacked.as<float2>());
 			note_launch(ctx);
-			dev = bank->unpacked.ptr;
+			dev = ctx->track_unpacked.ptr;
 			sample_type = UGSDR_SAMPLES_CF32;
 		}
 		const size_t per = capture_bytes(sample_type, bank->fs, n) / n;  // bytes per sample the kernel reads
@@ -659,8 +659,8 @@ int ugsdr_track_run(ugsdr_track_bank* bank, const void* samples, int sample_type
 		TrackOut* dev_out = nullptr;
 		if (outputs) {
 			require(n_epochs > 0, "null samples or no epochs");
-			bank->out.reserve(sizeof(TrackOut) * static_cast<size_t>(n_epochs) * bank->n_channels);
-			dev_out = bank->out.as<TrackOut>();
+			ctx->track_out.reserve(sizeof(TrackOut) * static_cast<size_t>(n_epochs) * bank->n_channels);
+			dev_out = ctx->track_out.as<TrackOut>();
 		}
 		track_enqueue(bank, samples, sample_type, samples_on_device, samples_per_epoch, n_epochs, dev_out);
 		if (outputs)
