@@ -42,6 +42,16 @@ int ugsdr_ctx_destroy(ugsdr_ctx* ctx) {
 		return UGSDR_E_INVALID;
 	cudaSetDevice(ctx->device);
 	cudaStreamSynchronize(ctx->stream);
+	if (ctx->copy_stream) {
+		cudaStreamSynchronize(ctx->copy_stream);
+		cudaStreamDestroy(ctx->copy_stream);
+	}
+	for (int i = 0; i < 2; ++i) {
+		if (ctx->slot_copied[i])
+			cudaEventDestroy(ctx->slot_copied[i]);
+		if (ctx->slot_used[i])
+			cudaEventDestroy(ctx->slot_used[i]);
+	}
 	if (ctx->own_stream)
 		cudaStreamDestroy(ctx->own_stream);
 	delete ctx;

@@ -152,6 +152,10 @@ struct ugsdr_ctx {
 	// outputs): shared by the context's banks, whose calls the context
 	// serialises on its stream, and kept between banks
 	ugsdr_gpu::DevBuf track_samples, track_unpacked, track_out;
+	// copies of host-buffer calls that overlap the context stream's kernels
+	// (created on first use): a stream and per-slot events
+	cudaStream_t copy_stream = nullptr;
+	cudaEvent_t slot_copied[2] = {nullptr, nullptr}, slot_used[2] = {nullptr, nullptr};
 	int sm_count = 0;
 	size_t smem_optin = 0;
 

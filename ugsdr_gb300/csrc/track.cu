@@ -28,6 +28,7 @@ namespace ugsdr_gpu {
 		constexpr int kWinChunk = 8192;   // samples per replica window (a multiple of kTrackThreads)
 		constexpr int kWinPad = 128;      // window margin: taps within +-kWinPad samples of the prompt
 		constexpr int kMaxChunks = 32;    // chunks per epoch
+		constexpr int kCopyChunkEpochs = 1000;  // host-buffer runs: epochs per overlapped copy
 		constexpr int kStageBytes = 32768;  // one staged sample chunk (two buffers, double-buffered)
 
 		template <int ST>
@@ -656,16 +657,67 @@ int ugsdr_track_run(ugsdr_track_bank* bank, const void* samples, int sample_type
 	ugsdr_ctx* ctx = bank->ctx;
 	std::lock_guard<std::mutex> lock(ctx->mutex);
 	return guarded(ctx, [&] {
+		require(samples && n_epochs > 0, "null samples or no epochs");
 		TrackOut* dev_out = nullptr;
+		const size_t out_per_epoch = sizeof(TrackOut) * bank->n_channels;
 		if (outputs) {
-			require(n_epochs > 0, "null samples or no epochs");
-			ctx->track_out.reserve(sizeof(TrackOut) * static_cast<size_t>(n_epochs) * bank->n_channels);
+			ctx->track_out.reserve(out_per_epoch * static_cast<size_t>(n_epochs));
 			dev_out = ctx->track_out.as<TrackOut>();
 		}
-		track_enqueue(bank, samples, sample_type, samples_on_device, samples_per_epoch, n_epochs, dev_out);
-		if (outputs)
-			UG_CUDA(cudaMemcpyAsync(outputs, dev_out, sizeof(TrackOut) * static_cast<size_t>(n_epochs) * bank->n_channels,
-				cudaMemcpyDeviceToHost, ctx->stream));
+		if (samples_on_device || n_epochs <= kCopyChunkEpochs) {
+			track_enqueue(bank, samples, sample_type, samples_on_device, samples_per_epoch, n_epochs, dev_out);
+			if (outputs)
+				UG_CUDA(cudaMemcpyAsync(outputs, dev_out, out_per_epoch * static_cast<size_t>(n_epochs), cudaMemcpyDeviceToHost,
+					ctx->stream));
+			UG_CUDA(cudaStreamSynchronize(ctx->stream));
+			return;
+		}
+		// host capture: chunks of kCopyChunkEpochs epochs through two staging
+		// slots, the copy of chunk c + 1 (copy stream) overlapping the bank's
+		// run over chunk c (context stream); each chunk's outputs are copied
+		// back as soon as its run ends
+		require(samples_per_epoch == bank->spm, "samples_per_epoch must be sampling_rate / 1000");
+		require(sample_type >= 0 && sample_type <= UGSDR_SAMPLES_NT1065_4, "unknown sample type");
+		if (!ctx->copy_stream) {
+			UG_CUDA(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+			for (int i = 0; i < 2; ++i) {
+				UG_CUDA(cudaEventCreateWithFlags(&ctx->slot_copied[i], cudaEventDisableTiming));
+				UG_CUDA(cudaEventCreateWithFlags(&ctx->slot_used[i], cudaEventDisableTiming));
+			}
+		}
+		const size_t chunk_bytes = capture_bytes(sample_type, bank->fs, bank->spm * static_cast<size_t>(kCopyChunkEpochs));
+		ctx->track_samples.reserve(2 * chunk_bytes);
+		const char* src = static_cast<const char*>(samples);
+		const int n_chunks = (n_epochs + kCopyChunkEpochs - 1) / kCopyChunkEpochs;
+		auto epochs_of = [&](int c) { return std::min(kCopyChunkEpochs, n_epochs - c * kCopyChunkEpochs); };
+		auto slot_ptr = [&](int c) { return ctx->track_samples.as<char>() + (c & 1) * chunk_bytes; };
+		auto copy_in = [&](int c) {
+			if (c >= 2)  // the run over chunk c - 2 has read the slot
+				UG_CUDA(cudaStreamWaitEvent(ctx->copy_stream, ctx->slot_used[c & 1], 0));
+			const size_t bytes = capture_bytes(sample_type, bank->fs, bank->spm * static_cast<size_t>(epochs_of(c)));
+			UG_CUDA(cudaMemcpyAsync(slot_ptr(c), src + static_cast<size_t>(c) * chunk_bytes, bytes, cudaMemcpyHostToDevice,
+				ctx->copy_stream));
+			UG_CUDA(cudaEventRecord(ctx->slot_copied[c & 1], ctx->copy_stream));
+		};
+		copy_in(0);
+		for (int c = 0; c < n_chunks; ++c) {
+			const int e0 = c * kCopyChunkEpochs;
+			const int ne = epochs_of(c);
+			UG_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->slot_copied[c & 1], 0));
+			TrackOut* out_c = dev_out ? dev_out + static_cast<size_t>(e0) * bank->n_channels : nullptr;
+			track_enqueue(bank, slot_ptr(c), sample_type, 1, samples_per_epoch, ne, out_c);
+			UG_CUDA(cudaEventRecord(ctx->slot_used[c & 1], ctx->stream));
+			// the next chunk's copy goes ahead of this chunk's outputs on the
+			// copy stream, so it overlaps this run
+			if (c + 1 < n_chunks)
+				copy_in(c + 1);
+			if (outputs) {
+				UG_CUDA(cudaStreamWaitEvent(ctx->copy_stream, ctx->slot_used[c & 1], 0));
+				UG_CUDA(cudaMemcpyAsync(reinterpret_cast<char*>(outputs) + out_per_epoch * static_cast<size_t>(e0), out_c,
+					out_per_epoch * static_cast<size_t>(ne), cudaMemcpyDeviceToHost, ctx->copy_stream));
+			}
+		}
+		UG_CUDA(cudaStreamSynchronize(ctx->copy_stream));
 		UG_CUDA(cudaStreamSynchronize(ctx->stream));
 	});
 }
