@@ -264,3 +264,28 @@ def test_large_368280_runtime_plan(ctx, oracle, golden_codes):
     for f in ("level", "mean", "std", "snr", "sigma"):
         assert abs(getattr(r, f) - o64[f]) <= RTOL * abs(o64[f]), (f, getattr(r, f), o64[f])
     assert abs(r.index % 20460 - 321.5 * 20) <= 2
+
+
+@pytest.mark.parametrize("fs,ms,k", [(4e6, 4, 2), (10.23e6, 12, 1), (6.144e6, 16, 1), (12.5e6, 8, 1)])
+def test_runtime_four_step_sizes_vs_oracle(ctx, oracle, golden_codes, fs, ms, k):
+    """Block sizes of the served mix's kind that have no compile-time plan
+    (16,000; 122,760; 98,304; 100,000: runtime four-step splits), a Galileo
+    E1B BOC(1,1) code repeated over whole 4 ms periods: peak bin exact, peak
+    index exact modulo the code period (the replica repeats), levels within
+    the FP64 bar."""
+    chips = unpack_codes(golden_codes, "galileo_e1b")[7]  # 8184 BOC half-chips per 4 ms
+    n = int(round(fs * ms / 1000))
+    reps = max(1, ms // 4)
+    samples_per_period = n // reps
+    em = signals.Emitter(chips, 2.046e6, 1234.25, 250.0, 60.0, data_rate=0.0)  # no half-sample delays
+    raw = signals.synthesize([em], fs, n * k, 20.0, "ci16", seed=int(fs) % 97 + ms)
+    x = to_complex(raw)
+    res, _ = run_engine(ctx, raw, fs, n, k, [chips], reps, 500, 250)
+    code = oracle.upsample(np.tile(chips, reps), n)
+    o32 = oracle.acquire(x, n, k, code, fs, 500, 250)
+    o64 = oracle.acquire(x, n, k, code, fs, 500, 250, double=True)
+    r = res[0]
+    assert r.doppler_bin == int(o32["doppler_bin"])
+    assert r.index % samples_per_period == int(o32["index"]) % samples_per_period
+    for f in ("level", "mean", "std", "snr", "sigma"):
+        assert abs(getattr(r, f) - o64[f]) <= RTOL * abs(o64[f]), (f, getattr(r, f), o64[f])
