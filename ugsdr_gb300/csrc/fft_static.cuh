@@ -193,11 +193,11 @@ namespace ugsdr_gpu {
 		static constexpr int kRowsMinBlocks = kRowsCompact ? 4 : 3;
 		// inverse column kernel: a hooked two-pass plan of the same width
 		// prefetches the next block into the input tile once pass 0 has read it
-		// (two tiles + accumulator, three CTAs per SM); other plans keep a third
-		// prefetch tile and run two
+		// (two tiles + accumulator, three CTAs per SM, four for N <= 256 whose
+		// tiles are small); other plans keep a third prefetch tile and run two
 		static constexpr bool kColsCompact = kRowsCompact;
 		static constexpr int kColsMaxThreads = kColsCompact ? 224 : 256;
-		static constexpr int kColsMinBlocks = kColsCompact ? 3 : 2;
+		static constexpr int kColsMinBlocks = kColsCompact ? (N_ <= 256 ? 4 : 3) : 2;
 		// most butterflies of one pass over `batch` transforms
 		static constexpr int most_butterflies(int batch) { return batch * (N_ / radix_min<Rs...>()); }
 		static_assert(tables_size<1, Rs...>() <= N_, "pass tables fit the N-entry table space");
