@@ -272,10 +272,31 @@ namespace ugsdr_gpu {
 		float2* b = smem + p.cw * ld;
 		const FftPlanDev p1 = F1::prepare(p.p1, smem + 2 * p.cw * ld);
 		// consecutive threads take consecutive columns of one n1 row: coalesced reads
-		for (int e = threadIdx.x; e < p.cw * n1; e += blockDim.x) {
-			const int f = e & mask, i1 = e >> p.cw_shift;
-			if (f < cw)
-				a[f * ld + i1] = fwd_load<ST>(p, item, static_cast<int64_t>(n2) * i1 + c0 + f, lut);
+		if (p.code_mode) {
+			for (int e = threadIdx.x; e < p.cw * n1; e += blockDim.x) {
+				const int f = e & mask, i1 = e >> p.cw_shift;
+				if (f < cw)
+					a[f * ld + i1] = fwd_load<ST>(p, item, static_cast<int64_t>(n2) * i1 + c0 + f, lut);
+			}
+		}
+		else {
+			// signal items: (Doppler, block) and the NCO adders once per CTA
+			const int d = item / p.base.k_blocks;
+			const int blk = item - d * p.base.k_blocks;
+			const uint32_t adder = p.base.adders[p.base.d_base + d];
+			const uint64_t g0 = static_cast<uint64_t>(blk) * p.base.n + c0;
+			const int fe_on = p.base.fe_on;
+			const uint32_t fe_adder = p.base.fe_adder, phase0 = p.base.phase0;
+			for (int e = threadIdx.x; e < p.cw * n1; e += blockDim.x) {
+				const int f = e & mask, i1 = e >> p.cw_shift;
+				if (f < cw) {
+					const uint64_t g = g0 + static_cast<uint64_t>(n2) * i1 + f;
+					float2 v = load_sample<ST>(p.base.samples, g);
+					if (fe_on)
+						v = table_mix(v, g, fe_adder, 0u, lut);
+					a[f * ld + i1] = table_mix(v, g, adder, phase0, lut);
+				}
+			}
 		}
 		__syncthreads();
 		const float2* y = F1::template run<false>(a, b, p1, cw, ld);
