@@ -2,20 +2,22 @@
 // the suppression engine the digital front end runs after resampling
 // (src/dfe/dfe.hpp:199-202).
 //
-//   stft_kernel         one CTA per group of columns: Hann window, forward
-//                       column DFTs (compile-time 128-point plan), spectra
-//                       out, and — for the detector — per column the eight
-//                       strongest bins with their peak / sigma
-//                       (JammingDetector::IntermediateDetection,
-//                       src/antijamming/jamming_detection.hpp:113-128)
-//                       and each CTA's occupation histograms
+//   detect_kernel       the detector's STFT, one warp per column with the
+//                       128-point transform in registers and shuffles
+//                       (Warp128), then the eight strongest bins with their
+//                       peak / sigma (JammingDetector::IntermediateDetection,
+//                       src/antijamming/jamming_detection.hpp:113-128) and
+//                       each CTA's occupation histograms
+//   stft_kernel         the per-op STFT (spectra out): columns per CTA in
+//                       shared memory (compile-time 128-point plan)
 //   decide_kernel,      AnalyzeStftData (130-189): the occupation vote per
 //   jn_sum_kernel       round, then the reported J/N sums; only the detection
 //                       list goes back to the host
-//   wideband_kernel     FilterWideband (src/antijamming/jse.hpp:70-87) fused
-//                       per output tile: the covering columns re-transformed
-//                       from the samples, bins with |.| >= 20 zeroed, inverse
-//                       DFTs scaled 2/W, overlap-added in column order
+//   wideband_kernel     FilterWideband (src/antijamming/jse.hpp:70-87) fused,
+//                       one warp per run of output slots: the covering columns
+//                       re-transformed from the samples (Warp128), bins with
+//                       |.| >= 20 zeroed, inverse transforms scaled 2/W,
+//                       overlap-added in column order in registers
 //   istft_cols_kernel,  the per-op OverlapAndAdd (src/math/stft.hpp:63-75):
 //   overlap_add_kernel  inverse columns, then a gather in column order
 //   null_bins_kernel    FilterInFreqencyDomain (jse.hpp:61-68): +-128 bins
@@ -114,14 +116,12 @@ namespace ugsdr_gpu {
 			int per_cta;           // columns per CTA
 			const float* window;   // w floats
 			FftPlanDev plan;
-			float2* s;             // cols x w spectra (null: not stored)
-			int detect;            // w == kDetectBins
-			DetectScratch det;
+			float2* s;             // cols x w spectra
 		};
 
 		__device__ __forceinline__ float magnitude(float2 v) { return sqrtf(v.x * v.x + v.y * v.y); }
 
-		// The warp's column, magnitudes in registers (lane l holds bins l + 32 j):
+		// The warp's column, magnitudes in registers (mv[j] of lane l is bin idx[j]):
 		// kMaxCandidates rounds of first-max — the largest magnitude (redux max
 		// over the bit patterns, which order as non-negative floats do), then
 		// the lowest bin holding it (redux min), as std::max_element — each
@@ -132,8 +132,8 @@ namespace ugsdr_gpu {
 		// peak / sigma.  Candidates with J/N < 6 are erased, the rest
 		// kept in order: kept candidate r of column `col` goes to [r][col] and
 		// into the CTA's round-r occupation histogram.
-		__device__ void detect_column(float (&mv)[kDetectBins / 32], const DetectScratch& d, size_t col, size_t cols,
-			int* s_hist, unsigned int* s_total) {
+		__device__ void detect_column(float (&mv)[kDetectBins / 32], const int (&idx)[kDetectBins / 32], const DetectScratch& d,
+			size_t col, size_t cols, int* s_hist, unsigned int* s_total) {
 			constexpr int J = kDetectBins / 32;
 			const int lane = threadIdx.x & 31;
 			int bins[kMaxCandidates];
@@ -147,15 +147,15 @@ namespace ugsdr_gpu {
 				top = __reduce_max_sync(0xffffffffu, top);
 				unsigned int first = 0xffffffffu;
 #pragma unroll
-				for (int j = J - 1; j >= 0; --j)
+				for (int j = 0; j < J; ++j)
 					if (__float_as_uint(mv[j]) == top)
-						first = lane + 32 * j;
+						first = min(first, static_cast<unsigned int>(idx[j]));
 				const int bi = static_cast<int>(__reduce_min_sync(0xffffffffu, first));
 				bins[r] = bi;
 				peaks[r] = __uint_as_float(top);
 #pragma unroll
 				for (int j = 0; j < J; ++j) {
-					const int dist = (lane + 32 * j - bi + kDetectBins) % kDetectBins;
+					const int dist = (idx[j] - bi + kDetectBins) % kDetectBins;
 					if (dist <= kNullHalfWidth || dist >= kDetectBins - kNullHalfWidth)
 						mv[j] = 0.0f;
 				}
@@ -217,28 +217,128 @@ namespace ugsdr_gpu {
 			}
 			__syncthreads();
 			const float2* y = F::template run<false>(a, b, plan, nc, ld);
-			if (p.s)
-				for (int e = threadIdx.x; e < nc * w; e += blockDim.x) {
-					const int f = e / w, i = e - f * w;
-					p.s[static_cast<size_t>(c0 + f) * w + i] = y[f * ld + i];
+			for (int e = threadIdx.x; e < nc * w; e += blockDim.x) {
+				const int f = e / w, i = e - f * w;
+				p.s[static_cast<size_t>(c0 + f) * w + i] = y[f * ld + i];
+			}
+		}
+
+		// 128-point DFT of one warp in registers: lane l holds v[j] =
+		// x[l + 32 j]; a radix-4 step over j, the twiddle W_128^{l k1}, then per
+		// k1 a 32-point DFT across the lanes in five radix-2
+		// decimation-in-frequency shuffle stages (h = 16 .. 1).  Lane l then
+		// holds X[k1 + 4 rev5(l)] in v[k1] (X[k1 + 4 k2] = sum_l W_128^{l k1}
+		// W_32^{l k2} sum_j x[l + 32 j] W_4^{j k1}).  The inverse runs the
+		// network backwards with conjugate twiddles, from that layout back to
+		// x[l + 32 j], unnormalised (x 128).  No shared memory, no barrier.
+		struct Warp128 {
+			float2 tw[3];  // W_128^{l k1}, k1 = 1..3
+			float2 ts[5];  // W_{2h}^{l mod h}, h = 16, 8, 4, 2, 1
+			__device__ __forceinline__ void init(const float2* tab, int lane) {
+#pragma unroll
+				for (int k1 = 1; k1 < 4; ++k1)
+					tw[k1 - 1] = tab[(lane * k1) & 127];
+#pragma unroll
+				for (int st = 0; st < 5; ++st) {
+					const int h = 16 >> st;
+					ts[st] = tab[(lane & (h - 1)) * (64 / h)];
 				}
-			if (!p.detect)
-				return;
+			}
+			__device__ __forceinline__ static int natural(int j, int lane) { return j + 4 * static_cast<int>(__brev(lane) >> 27); }
+			__device__ __forceinline__ void forward(float2 (&v)[4], int lane) const {
+				const float2 a0 = cadd(v[0], v[2]), a1 = csub(v[0], v[2]);
+				const float2 b0 = cadd(v[1], v[3]), dd = csub(v[1], v[3]);
+				const float2 b1 = c2(dd.y, -dd.x);  // (v1 - v3)(-i)
+				v[0] = cadd(a0, b0);
+				v[2] = csub(a0, b0);
+				v[1] = cadd(a1, b1);
+				v[3] = csub(a1, b1);
+#pragma unroll
+				for (int k1 = 1; k1 < 4; ++k1)
+					v[k1] = cmul(v[k1], tw[k1 - 1]);
+#pragma unroll
+				for (int st = 0; st < 5; ++st) {
+					const int h = 16 >> st;
+					const bool hi = (lane & h) != 0;
+#pragma unroll
+					for (int j = 0; j < 4; ++j) {
+						const float2 o = c2(__shfl_xor_sync(0xffffffffu, v[j].x, h), __shfl_xor_sync(0xffffffffu, v[j].y, h));
+						v[j] = hi ? cmul(csub(o, v[j]), ts[st]) : cadd(v[j], o);
+					}
+				}
+			}
+			__device__ __forceinline__ void inverse(float2 (&v)[4], int lane) const {
+#pragma unroll
+				for (int st = 4; st >= 0; --st) {
+					const int h = 16 >> st;
+					const bool hi = (lane & h) != 0;
+#pragma unroll
+					for (int j = 0; j < 4; ++j) {
+						const float2 q = hi ? cmulc(v[j], ts[st]) : v[j];
+						const float2 o = c2(__shfl_xor_sync(0xffffffffu, q.x, h), __shfl_xor_sync(0xffffffffu, q.y, h));
+						v[j] = hi ? csub(o, q) : cadd(q, o);
+					}
+				}
+#pragma unroll
+				for (int k1 = 1; k1 < 4; ++k1)
+					v[k1] = cmulc(v[k1], tw[k1 - 1]);
+				const float2 a0 = cadd(v[0], v[2]), a1 = csub(v[0], v[2]);
+				const float2 b0 = cadd(v[1], v[3]), dd = csub(v[1], v[3]);
+				const float2 b1 = c2(-dd.y, dd.x);  // (v1 - v3)(+i)
+				v[0] = cadd(a0, b0);
+				v[2] = csub(a0, b0);
+				v[1] = cadd(a1, b1);
+				v[3] = csub(a1, b1);
+			}
+		};
+
+		struct DetectParams {
+			const float2* x;       // samples; column c starts at 32 c
+			int cols;
+			const float* window;   // 128 Hann coefficients
+			const float2* tw;      // W_128^m, m < 128
+			DetectScratch det;
+		};
+
+		// JammingDetector's STFT and per-column candidates, one warp per column
+		// (grid-stride), the column's transform in registers (Warp128)
+		__global__ void __launch_bounds__(kJamThreads) detect_kernel(DetectParams p) {
+			__shared__ float2 tab[kDetectBins];
 			__shared__ int s_hist[kMaxCandidates * kDetectBins];
 			__shared__ unsigned int s_total;
+			for (int e = threadIdx.x; e < kDetectBins; e += blockDim.x)
+				tab[e] = p.tw[e];
 			for (int e = threadIdx.x; e < kMaxCandidates * kDetectBins; e += blockDim.x)
 				s_hist[e] = 0;
 			if (threadIdx.x == 0)
 				s_total = 0;
 			__syncthreads();
-			// one warp per column (w == kDetectBins here)
-			const int warp = threadIdx.x >> 5, n_warps = blockDim.x >> 5, lane = threadIdx.x & 31;
-			for (int f = warp; f < nc; f += n_warps) {
-				float mv[kDetectBins / 32];
+			const int lane = threadIdx.x & 31;
+			Warp128 fft;
+			fft.init(tab, lane);
+			float win[4];
+			int idx[4];
 #pragma unroll
-				for (int j = 0; j < kDetectBins / 32; ++j)
-					mv[j] = magnitude(y[f * ld + lane + 32 * j]);
-				detect_column(mv, p.det, static_cast<size_t>(c0 + f), static_cast<size_t>(p.cols), s_hist, &s_total);
+			for (int j = 0; j < 4; ++j) {
+				win[j] = p.window[lane + 32 * j];
+				idx[j] = Warp128::natural(j, lane);
+			}
+			const int warps = gridDim.x * (blockDim.x >> 5);
+			for (int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); c < p.cols; c += warps) {
+				const float2* xc = p.x + static_cast<size_t>(c) * 32;
+				float2 v[4];
+#pragma unroll
+				for (int j = 0; j < 4; ++j) {
+					const float2 smp = xc[lane + 32 * j];
+					// vec * complex(window, 0) (stft.hpp:55-56): both parts scaled
+					v[j] = c2(__fmul_rn(smp.x, win[j]), __fmul_rn(smp.y, win[j]));
+				}
+				fft.forward(v, lane);
+				float mv[4];
+#pragma unroll
+				for (int j = 0; j < 4; ++j)
+					mv[j] = magnitude(v[j]);
+				detect_column(mv, idx, p.det, static_cast<size_t>(c), static_cast<size_t>(p.cols), s_hist, &s_total);
 			}
 			__syncthreads();
 			for (int e = threadIdx.x; e < kMaxCandidates * kDetectBins; e += blockDim.x)
@@ -308,67 +408,82 @@ namespace ugsdr_gpu {
 		struct WidebandParams {
 			const float2* x;       // n input samples
 			uint64_t n;
-			int w, hop;
 			int cols;
-			int per_cta;           // columns per CTA, the halo included
-			int slots;             // output hops per CTA: per_cta - (w / hop - 1)
+			int slots_per_warp;    // 32-sample output slots per warp
 			const float* window;
-			FftPlanDev plan;
+			const float2* tw;      // W_128^m, m < 128
 			float2* out;           // n output samples (not x)
 		};
 
-		// FilterWideband fused for one tile of slots * hop output samples: the
-		// covering columns (the tile's own and w / hop - 1 before it) are
-		// re-transformed from x exactly as the detector's STFT did, zeroed where
-		// |.| >= 20, inverse-transformed, scaled 2/w and overlap-added in column
-		// order; the spectra never leave shared memory.
-		template <class F>
+		// FilterWideband (jse.hpp:70-87) + OverlapAndAdd + resize to n, one warp
+		// per run of 32-sample output slots: it walks the covering columns in
+		// order (its first slot's three predecessors first), re-transforming each
+		// from the samples as the detector did (Warp128), zeroing |.| >= 20,
+		// inverse-transforming and scaling (v / 128) * 2; column i's value j
+		// belongs to slot i + j, so four slot accumulators per lane take the
+		// columns in column order, and slot i is complete after column i.
 		__global__ void __launch_bounds__(kJamThreads) wideband_kernel(WidebandParams p) {
-			extern __shared__ float2 sm[];
-			const int w = fft_n<F>(p.plan.n);
-			const int ld = w | 1;
-			const int hop = p.hop;
-			const uint64_t t0 = static_cast<uint64_t>(blockIdx.x) * p.slots * hop;
-			const uint64_t t1 = min(t0 + static_cast<uint64_t>(p.slots) * hop, p.n);
-			const int i_lo = t0 >= static_cast<uint64_t>(w) ? static_cast<int>((t0 - w) / hop) + 1 : 0;
-			const int i_hi = min(p.cols - 1, static_cast<int>((t1 - 1) / hop));
-			const int nc = max(0, i_hi - i_lo + 1);
-			float2* a = sm;
-			float2* b = sm + p.per_cta * ld;
-			float* win = reinterpret_cast<float*>(sm + 2 * p.per_cta * ld);
-			const FftPlanDev plan = F::prepare(p.plan, win + w);
-			for (int i = threadIdx.x; i < w; i += blockDim.x)
-				win[i] = p.window[i];
+			__shared__ float2 tab[kDetectBins];
+			for (int e = threadIdx.x; e < kDetectBins; e += blockDim.x)
+				tab[e] = p.tw[e];
 			__syncthreads();
-			for (int e = threadIdx.x; e < nc * w; e += blockDim.x) {
-				const int f = e / w, i = e - f * w;
-				const float2 v = p.x[static_cast<size_t>(i_lo + f) * hop + i];
-				a[f * ld + i] = c2(__fmul_rn(v.x, win[i]), __fmul_rn(v.y, win[i]));
-			}
-			__syncthreads();
-			float2* y = F::template run<false>(a, b, plan, nc, ld);
-			for (int e = threadIdx.x; e < nc * w; e += blockDim.x) {
-				const int f = e / w, i = e - f * w;
-				if (magnitude(y[f * ld + i]) >= kWidebandLevel)
-					y[f * ld + i] = c2(0.0f, 0.0f);
-			}
-			__syncthreads();
-			const float2* z = F::template run<true>(y, y == a ? b : a, plan, nc, ld);
-			const float fw = static_cast<float>(w);
-			const uint64_t len = static_cast<uint64_t>(w) + static_cast<uint64_t>(p.cols - 1) * hop;
-			for (uint64_t k = t0 + threadIdx.x; k < t1; k += blockDim.x) {
-				float ax = 0.0f, ay = 0.0f;
-				if (k < len) {
-					const int lo = k >= static_cast<uint64_t>(w) ? static_cast<int>((k - w) / hop) + 1 : 0;
-					const int hi = min(p.cols - 1, static_cast<int>(k / hop));
-					for (int i = lo; i <= hi; ++i) {
-						const float2 v = z[(i - i_lo) * ld + static_cast<int>(k - static_cast<uint64_t>(i) * hop)];
-						ax = __fadd_rn(ax, __fmul_rn(__fdiv_rn(v.x, fw), 2.0f));
-						ay = __fadd_rn(ay, __fmul_rn(__fdiv_rn(v.y, fw), 2.0f));
+			const int lane = threadIdx.x & 31;
+			const long long total_slots = static_cast<long long>((p.n + 31) / 32);
+			const long long s0 = (static_cast<long long>(blockIdx.x) * (blockDim.x >> 5) + (threadIdx.x >> 5)) * p.slots_per_warp;
+			if (s0 >= total_slots)
+				return;
+			const long long s1 = min(s0 + p.slots_per_warp, total_slots);
+			Warp128 fft;
+			fft.init(tab, lane);
+			float win[4];
+#pragma unroll
+			for (int j = 0; j < 4; ++j)
+				win[j] = p.window[lane + 32 * j];
+			const float fw = static_cast<float>(kDetectBins);
+			float2 acc[4];
+#pragma unroll
+			for (int j = 0; j < 4; ++j)
+				acc[j] = c2(0.0f, 0.0f);
+			auto put = [&](long long s, float2 v) {
+				const uint64_t k = static_cast<uint64_t>(s) * 32 + lane;
+				if (k < p.n)
+					p.out[k] = v;
+			};
+			const long long i_lo = max(0LL, s0 - 3);
+			const long long i_hi = min(static_cast<long long>(p.cols) - 1, s1 - 1);
+			for (long long i = i_lo; i <= i_hi; ++i) {
+				const float2* xc = p.x + static_cast<size_t>(i) * 32;
+				float2 v[4];
+#pragma unroll
+				for (int j = 0; j < 4; ++j) {
+					const float2 smp = xc[lane + 32 * j];
+					v[j] = c2(__fmul_rn(smp.x, win[j]), __fmul_rn(smp.y, win[j]));
+				}
+				fft.forward(v, lane);
+#pragma unroll
+				for (int j = 0; j < 4; ++j)
+					if (magnitude(v[j]) >= kWidebandLevel)
+						v[j] = c2(0.0f, 0.0f);
+				fft.inverse(v, lane);
+#pragma unroll
+				for (int j = 0; j < 4; ++j) {
+					const long long s = i + j;
+					if (s >= s0 && s < s1) {
+						float2& a = acc[s & 3];
+						a = c2(__fadd_rn(a.x, __fmul_rn(__fdiv_rn(v[j].x, fw), 2.0f)),
+							__fadd_rn(a.y, __fmul_rn(__fdiv_rn(v[j].y, fw), 2.0f)));
 					}
 				}
-				p.out[k] = c2(ax, ay);
+				if (i >= s0) {
+					put(i, acc[i & 3]);
+					acc[i & 3] = c2(0.0f, 0.0f);
+				}
 			}
+			// past the last column: the synthesis tail (slots cols .. cols + 2),
+			// then the zeros of the resize to n
+			const long long len_slots = static_cast<long long>(p.cols) + 3;
+			for (long long s = max(s0, static_cast<long long>(p.cols)); s < s1; ++s)
+				put(s, s < len_slots ? acc[s & 3] : c2(0.0f, 0.0f));
 		}
 
 		struct NullRange {
@@ -446,14 +561,11 @@ namespace ugsdr_gpu {
 			return cols;
 		}
 
-		// STFT of device samples x: spectra into ctx->jam_s when `spectra`,
-		// detection candidates and histograms into `det` when given
-		void stft_device(ugsdr_ctx* ctx, const float2* x, size_t cols, int w, int overlap, bool spectra,
-			const DetectScratch* det) {
+		// STFT of device samples x into ctx->jam_s (the per-op Transform)
+		void stft_device(ugsdr_ctx* ctx, const float2* x, size_t cols, int w, int overlap) {
 			size_t smem = 0;
 			const int per = columns_per_cta(ctx, w, smem);
-			if (spectra)
-				ctx->jam_s.reserve(sizeof(float2) * cols * w);
+			ctx->jam_s.reserve(sizeof(float2) * cols * w);
 			StftParams p{};
 			p.x = x;
 			p.w = w;
@@ -462,13 +574,8 @@ namespace ugsdr_gpu {
 			p.per_cta = per;
 			p.window = hann_window(ctx, w);
 			p.plan = column_plan(ctx, w);
-			p.s = spectra ? ctx->jam_s.as<float2>() : nullptr;
-			p.detect = det ? 1 : 0;
-			if (det) {
-				require(w == kDetectBins, "detection runs on 128-point columns");
-				p.det = *det;
-			}
-			KernelTimer timer(ctx, det ? "jam_stft_detect" : "jam_stft");
+			p.s = ctx->jam_s.as<float2>();
+			KernelTimer timer(ctx, "jam_stft");
 			with_column_fft(w, [&](auto f) {
 				using F = decltype(f);
 				UG_CUDA(cudaFuncSetAttribute(stft_kernel<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
@@ -500,29 +607,28 @@ namespace ugsdr_gpu {
 			note_launch(ctx, 2);
 		}
 
+		int grid_for_warps(ugsdr_ctx* ctx, long long warps) {
+			const long long per_cta = kJamThreads / 32;
+			return static_cast<int>(std::max<long long>(1, std::min<long long>((warps + per_cta - 1) / per_cta,
+				static_cast<long long>(ctx->sm_count) * 64)));
+		}
+
 		// FilterWideband + OverlapAndAdd + resize to n, fused: x -> out
 		void wideband_device(ugsdr_ctx* ctx, const float2* x, size_t n, float2* out) {
-			const int w = kDetectWindow, hop = kDetectWindow - kDetectOverlap;
-			const size_t cols = stft_columns(n, w, kDetectOverlap);
-			size_t smem = 0;
-			const int per = columns_per_cta(ctx, w, smem);
+			constexpr int kSlotsPerWarp = 64;
 			WidebandParams p{};
 			p.x = x;
 			p.n = n;
-			p.w = w;
-			p.hop = hop;
-			p.cols = static_cast<int>(cols);
-			p.per_cta = per;
-			p.slots = per - (w / hop - 1);
-			require(p.slots >= 1, "wideband tile too small");
-			p.window = hann_window(ctx, w);
-			p.plan = column_plan(ctx, w);
+			p.cols = static_cast<int>(stft_columns(n, kDetectWindow, kDetectOverlap));
+			p.slots_per_warp = kSlotsPerWarp;
+			p.window = hann_window(ctx, kDetectWindow);
+			p.tw = get_plan(ctx, kDetectWindow).tw;
 			p.out = out;
-			const uint64_t tile = static_cast<uint64_t>(p.slots) * hop;
-			using F = StaticFft<128, 16, 8>;
+			const long long warps = (static_cast<long long>((n + 31) / 32) + kSlotsPerWarp - 1) / kSlotsPerWarp;
+			const long long ctas = (warps + kJamThreads / 32 - 1) / (kJamThreads / 32);
+			require(ctas < (1LL << 31), "signal too long");
 			KernelTimer timer(ctx, "jam_wideband");
-			UG_CUDA(cudaFuncSetAttribute(wideband_kernel<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
-			wideband_kernel<F><<<static_cast<unsigned>((n + tile - 1) / tile), kJamThreads, smem, ctx->stream>>>(p);
+			wideband_kernel<<<static_cast<unsigned>(ctas), kJamThreads, 0, ctx->stream>>>(p);
 			note_launch(ctx);
 		}
 
@@ -651,7 +757,17 @@ namespace ugsdr_gpu {
 			ctx->jam_cand.reserve(lay.bytes);
 			const DetectScratch d = lay.carve(ctx->jam_cand.ptr);
 			UG_CUDA(cudaMemsetAsync(ctx->jam_cand.ptr, 0, lay.zero_bytes, ctx->stream));
-			stft_device(ctx, x, cols, kDetectWindow, kDetectOverlap, false, &d);
+			DetectParams dp{};
+			dp.x = x;
+			dp.cols = static_cast<int>(cols);
+			dp.window = hann_window(ctx, kDetectWindow);
+			dp.tw = get_plan(ctx, kDetectWindow).tw;
+			dp.det = d;
+			{
+				KernelTimer timer(ctx, "jam_stft_detect");
+				detect_kernel<<<grid_for_warps(ctx, static_cast<long long>(cols)), kJamThreads, 0, ctx->stream>>>(dp);
+			}
+			note_launch(ctx);
 			decide_kernel<<<1, 32, 0, ctx->stream>>>(d, cols);
 			jn_sum_kernel<<<kSumCtas, kJamThreads, 0, ctx->stream>>>(d, cols, fs);
 			note_launch(ctx, 2);
@@ -704,7 +820,7 @@ int ugsdr_stft(ugsdr_ctx* ctx, const float* in_iq, size_t n, int window_length, 
 		if (!out_iq)
 			return;
 		const float2* x = stage(ctx, in_iq, n, 0);
-		stft_device(ctx, x, cols, window_length, overlap_length, true, nullptr);
+		stft_device(ctx, x, cols, window_length, overlap_length);
 		UG_CUDA(cudaMemcpyAsync(out_iq, ctx->jam_s.ptr, sizeof(float2) * cols * window_length, cudaMemcpyDeviceToHost, ctx->stream));
 		UG_CUDA(cudaStreamSynchronize(ctx->stream));
 	});
