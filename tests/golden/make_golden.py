@@ -245,6 +245,25 @@ def packed(lib, ref_dir: str) -> dict[str, np.ndarray]:
     return out
 
 
+# real_8 acquisition known answer (test/integration_tests.cpp:253-263, the
+# reference's expected GPS L1 C/A results for its real_8.bin capture: sv id,
+# Doppler Hz, code offset in 38.192 MHz samples; a run passes when >= 4 of
+# them are found within 400 Hz, 237-241)
+REAL8_KAT = [(2, 0, 34213), (5, 6000, 28203), (8, -1000, 4695), (14, 0, 36321), (17, 2000, 20725),
+             (20, 3000, 13404), (21, 0, 6289), (25, 5000, 26828)]
+
+
+def real8(ref_dir: str) -> dict[str, np.ndarray]:
+    """The first 4 ms (FastSearchEngineBase's ms_to_process) of the
+    reference's real_8.bin: real int8 at 38.192 MHz, centre 1575.42 MHz +
+    9.55 MHz (integration_tests.cpp:76), with the known answer."""
+    fs = 38.192e6
+    raw = np.fromfile(Path(ref_dir) / "data" / "real_8.bin", np.int8, count=int(fs / 1e3) * 4)
+    assert raw[0] == -2  # integration_tests.cpp:124-141
+    return {"samples": raw, "fs": np.array(fs), "if_hz": np.array(9.55e6),
+            "kat": np.array(REAL8_KAT, np.float64)}
+
+
 JAMMING_CASES = {  # name -> (fs, n, seed); signals built by jamming_input()
     "clean": (2.048e6, 2048, 11),
     "tone": (2.048e6, 2048, 12),
@@ -321,6 +340,7 @@ def main() -> None:
     np.savez_compressed(HERE / "acq_gps_l1_4mhz.npz", **a)
     np.savez_compressed(HERE / "packed.npz", **packed(lib, ref_dir))
     np.savez_compressed(HERE / "jamming.npz", **jamming(lib))
+    np.savez_compressed(HERE / "real8.npz", **real8(ref_dir))
     for f in sorted(HERE.glob("*.npz")):
         print(f.name, f.stat().st_size)
 

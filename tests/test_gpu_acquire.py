@@ -6,7 +6,7 @@ and SNR within 1e-4 relative of the FP64 oracle."""
 import numpy as np
 import pytest
 
-from conftest import unpack_codes
+from conftest import GOLDEN as GOLDEN_DIR, unpack_codes
 from ugsdr_gb300 import _lib as L
 from ugsdr_gb300 import signals
 
@@ -289,3 +289,44 @@ def test_runtime_four_step_sizes_vs_oracle(ctx, oracle, golden_codes, fs, ms, k)
     assert r.index % samples_per_period == int(o32["index"]) % samples_per_period
     for f in ("level", "mean", "std", "snr", "sigma"):
         assert abs(getattr(r, f) - o64[f]) <= RTOL * abs(o64[f]), (f, getattr(r, f), o64[f])
+
+
+@pytest.mark.parametrize("new_fs", [9.548e6, 1.736e6, 38.192e6])
+def test_real_8_capture_known_answer(ctx, oracle, golden_codes, new_fs):
+    """The reference's real-signal acquisition test (test/integration_tests.cpp
+    :406-409, 253-263, 237-241) on its real_8.bin capture (first 4 ms: real
+    int8 at 38.192 MHz, centre 9.55 MHz above L1): the front end translates
+    by +9.55 MHz at the input rate (dfe.hpp:185, 199) and resamples to the
+    rate AdjustSamplingRate picks for the FSE targets 8.192 / 2.048 / 40.96
+    MHz (fse.hpp:222-240: 9.548, 1.736, 38.192 MHz); 32 GPS C/A codes of
+    4 ms folded to 1 ms, +-6 kHz in 200 Hz.  The known answer passes when
+    >= 4 of its 8 satellites are found within 400 Hz; peaks of those
+    satellites equal the oracle's (at the two lower rates)."""
+    z = np.load(GOLDEN_DIR / "real8.npz")
+    raw = z["samples"]
+    fs, f_if = float(z["fs"]), float(z["if_hz"])
+    ca = unpack_codes(golden_codes, "gps_l1ca")
+    n = int(round(new_fs * 4 / 1000))
+    svs = list(range(32))
+    handles = [ctx.code_put(ca[sv], n, repeats=4) for sv in svs]
+    try:
+        job = ctx.make_job(raw, L.SAMPLES_RI8, new_fs, n, 1, handles, 6000, 200, n_samples=raw.size,
+                           input_sampling_rate=fs, frontend_frequency=f_if, code_offset_ratio=fs / new_fs,
+                           fold_samples=n // 4, fold_coherent=True)
+        res = ctx.acquire(job)
+    finally:
+        for h in handles:
+            ctx.code_release(h)
+    found = [sv for sv, dop, _ in z["kat"]
+             if res[int(sv)].snr > 3.3 and abs(res[int(sv)].doppler - dop) <= 400]
+    assert len(found) >= 4, found
+    if new_fs == fs:
+        return  # the oracle's 152,768-point search is minutes of CPU
+    y = oracle.table_mix(raw.astype(np.complex64), fs, f_if)
+    y = oracle.resample(y, int(new_fs), int(fs))[:n]
+    check = found if new_fs < 5e6 else found[:4]
+    for sv in check:
+        code = oracle.upsample(np.tile(ca[int(sv)], 4), n)
+        o32 = oracle.acquire(y, n, 1, code, new_fs, 6000, 200, reshape=True, coherent=True)
+        o64 = oracle.acquire(y, n, 1, code, new_fs, 6000, 200, reshape=True, coherent=True, double=True)
+        check_vs_oracle(res[int(sv)], o32, o64)
