@@ -266,10 +266,11 @@ def test_large_368280_runtime_plan(ctx, oracle, golden_codes):
     assert abs(r.index % 20460 - 321.5 * 20) <= 2
 
 
-@pytest.mark.parametrize("fs,ms,k", [(4e6, 4, 2), (10.23e6, 12, 1), (6.144e6, 16, 1), (12.5e6, 8, 1)])
+@pytest.mark.parametrize("fs,ms,k", [(4e6, 4, 2), (10.23e6, 12, 1), (6.144e6, 16, 1), (12.5e6, 8, 1), (50e6, 20, 1)])
 def test_runtime_four_step_sizes_vs_oracle(ctx, oracle, golden_codes, fs, ms, k):
-    """Block sizes of the served mix's kind that have no compile-time plan
-    (16,000; 122,760; 98,304; 100,000: runtime four-step splits), a Galileo
+    """Block sizes of the served mix's kind on the runtime four-step splits
+    (16,000; 122,760; 98,304; 100,000) and on runtime columns with the
+    compile-time 1000-point rows (1,000,000 = 1000 x 1000), a Galileo
     E1B BOC(1,1) code repeated over whole 4 ms periods: peak bin exact, peak
     index exact modulo the code period (the replica repeats), levels within
     the FP64 bar."""

@@ -166,6 +166,8 @@ namespace ugsdr_gpu {
 				fn(StaticFft<400, 25, 16>{}, StaticFft<500, 25, 20>{});         // 200,000: 4 ms at 50 MHz
 			else if (n1 == 440 && n2 == 465)  // 204,600: 10 ms at 20.46 MHz; fusing the radix-31 rows spills
 				fn(StaticFft<440, 11, 5, 8>{}, StaticFftPlain<465, 31, 15>{});
+			else if (n2 == 1000)  // 0.75 - 1 M points (15 - 20 ms at 50 MHz): compile-time rows
+				fn(RuntimeFft{}, StaticFft<1000, 10, 10, 10>{});
 			else
 				fn(RuntimeFft{}, RuntimeFft{});
 		}
