@@ -264,6 +264,15 @@ def real8(ref_dir: str) -> dict[str, np.ndarray]:
             "kat": np.array(REAL8_KAT, np.float64)}
 
 
+def iq16(ref_dir: str) -> dict[str, np.ndarray]:
+    """The first 4 ms of the reference's iq_16_plus_16.bin (int16 I/Q at 4 MHz,
+    centre on L1; integration_tests.cpp:75), whose acquisition test asks a
+    non-empty result (401-404)."""
+    raw = np.fromfile(Path(ref_dir) / "data" / "iq_16_plus_16.bin", np.int16, count=16000 * 2).reshape(-1, 2)
+    assert tuple(raw[0]) == (-150, 16)  # integration_tests.cpp:105-122
+    return {"samples": raw, "fs": np.array(4e6)}
+
+
 JAMMING_CASES = {  # name -> (fs, n, seed); signals built by jamming_input()
     "clean": (2.048e6, 2048, 11),
     "tone": (2.048e6, 2048, 12),
@@ -341,6 +350,7 @@ def main() -> None:
     np.savez_compressed(HERE / "packed.npz", **packed(lib, ref_dir))
     np.savez_compressed(HERE / "jamming.npz", **jamming(lib))
     np.savez_compressed(HERE / "real8.npz", **real8(ref_dir))
+    np.savez_compressed(HERE / "iq16.npz", **iq16(ref_dir))
     for f in sorted(HERE.glob("*.npz")):
         print(f.name, f.stat().st_size)
 

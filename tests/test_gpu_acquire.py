@@ -332,3 +332,32 @@ def test_real_8_capture_known_answer(ctx, oracle, golden_codes, new_fs):
         o32 = oracle.acquire(y, n, 1, code, new_fs, 6000, 200, reshape=True, coherent=True)
         o64 = oracle.acquire(y, n, 1, code, new_fs, 6000, 200, reshape=True, coherent=True, double=True)
         check_vs_oracle(res[int(sv)], o32, o64)
+
+
+def test_iq_16_capture_search(ctx, oracle, golden_codes):
+    """The reference's iq_16_plus_16 acquisition test (test/integration_tests
+    .cpp:401-404: 4 MHz int16 I/Q on L1, +-15 kHz, non-empty result; the FSE
+    keeps 4 MHz, fse.hpp:222-240): 32 GPS C/A codes of 4 ms folded to 1 ms.
+    The result is non-empty, and the clear detections (SNR > 4) equal the
+    oracle's peaks."""
+    z = np.load(GOLDEN_DIR / "iq16.npz")
+    raw = z["samples"]
+    fs = float(z["fs"])
+    ca = unpack_codes(golden_codes, "gps_l1ca")
+    n = 16000
+    handles = [ctx.code_put(ca[sv], n, repeats=4) for sv in range(32)]
+    try:
+        job = ctx.make_job(raw, L.SAMPLES_CI16, fs, n, 1, handles, 15000, 200, fold_samples=4000, fold_coherent=True)
+        res = ctx.acquire(job)
+    finally:
+        for h in handles:
+            ctx.code_release(h)
+    assert any(r.snr > 3.3 for r in res)
+    x = to_complex(raw)
+    clear = [sv for sv in range(32) if res[sv].snr > 4.0]
+    assert len(clear) >= 4, clear
+    for sv in clear:
+        code = oracle.upsample(np.tile(ca[sv], 4), n)
+        o32 = oracle.acquire(x, n, 1, code, fs, 15000, 200, reshape=True, coherent=True)
+        o64 = oracle.acquire(x, n, 1, code, fs, 15000, 200, reshape=True, coherent=True, double=True)
+        check_vs_oracle(res[sv], o32, o64)
