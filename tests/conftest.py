@@ -39,6 +39,10 @@ def unpack_codes(fix, name):
 @pytest.fixture(scope="session")
 def lib():
     from ugsdr_gb300 import _lib
+    if not _lib.LIB_PATH.exists() and "UGSDR_CUDA_LIB" not in os.environ:
+        # a fresh checkout: compile it (nvcc cross-compiles without a GPU)
+        from ugsdr_gb300 import build
+        build.build_library()
     return _lib.load()
 
 
