@@ -29,13 +29,13 @@ def build():
     assert r.returncode == 0, r.stderr[-3000:]
 
 
-def test_dropin_compiles_and_links():
+def test_dropin_compiles_and_links(lib):
     build()
     assert BIN.exists()
 
 
 @pytest.mark.gpu
-def test_dropin_runs():
+def test_dropin_runs(lib):
     build()
     r = subprocess.run([str(BIN)], capture_output=True, text=True, timeout=120)
     assert r.returncode == 0 and r.stdout.startswith("ok"), r.stdout + r.stderr
