@@ -904,6 +904,162 @@ def run_jamming(args, world, rank):
     return line
 
 
+# ------------------------------------------------------------- observables
+OBS_CHANNELS = 256
+OBS_EPOCHS = 60_000  # one minute of 1 ms epochs: two LNAV frames for ephemeris decoding
+# algorithmic bytes per channel-epoch: the bank's 88-byte output record read
+# once (the fields Observable needs touch each of its 32-byte sectors) and
+# the 32-byte observable written once
+OBS_BYTES = 88 + 32
+OBS_FS = 20e6
+OBS_CAP = 8192  # candidate epochs kept per channel (random LNAV data give ~5,000 a minute)
+
+
+def observables_outputs(dev):
+    """Tracking-bank outputs of 256 channels x 60,000 epochs synthesised on
+    the device from a fixed seed: prompt I/Q noise plus +-1 navigation
+    symbols, carrier frequency near 2 kHz, loop errors, code phases.  Returns
+    the raw (n_epochs, n_channels, 22) float32 buffer (88-byte records)."""
+    import torch
+    gen = torch.Generator(device=f"cuda:{dev}")
+    gen.manual_seed(7)
+    n_ep, n_ch = OBS_EPOCHS, OBS_CHANNELS
+    rec = torch.zeros((n_ep, n_ch, 22), dtype=torch.float32, device=f"cuda:{dev}")
+    rec[:, :, :10] = torch.randn((n_ep, n_ch, 10), generator=gen, device=f"cuda:{dev}") * 40
+    bits = torch.randint(0, 2, (n_ep // 20 + 1, n_ch), generator=gen, device=f"cuda:{dev}").float() * 2 - 1
+    rec[:, :, 4] += 300 * bits.repeat_interleave(20, dim=0)[:n_ep]
+    d = rec.view(torch.float64)  # (n_ep, n_ch, 11): taps occupy 0..4
+    d[:, :, 5] = 2000.0 + torch.randn((n_ep, n_ch), generator=gen, device=f"cuda:{dev}", dtype=torch.float64)
+    d[:, :, 6] = torch.rand((n_ep, n_ch), generator=gen, device=f"cuda:{dev}", dtype=torch.float64) * 2 * np.pi
+    d[:, :, 7] = 5000.0 + torch.rand((1, n_ch), generator=gen, device=f"cuda:{dev}", dtype=torch.float64) * 1000
+    d[:, :, 8] = 1.023e6
+    d[:, :, 9] = torch.randn((n_ep, n_ch), generator=gen, device=f"cuda:{dev}", dtype=torch.float64) * 0.02
+    return rec
+
+
+def observables_channels():
+    return [dict(fs=OBS_FS, intermediate_frequency=0.0, carrier_frequency=2000.0, carrier_phase=0.0,
+                 preamble_position=100, range_correction_ms=68.0) for _ in range(OBS_CHANNELS)]
+
+
+def observables_cpu_baseline(rows, channels=32):
+    """Observable's arithmetic and the preamble search restated in the oracle
+    (obs_oracle.cpp), one thread, on the first `channels` channels."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import pyoracle
+    t0 = time.perf_counter()
+    for c in range(channels):
+        pyoracle.observables(rows[:, c], OBS_FS, 0.0, 2000.0, 0.0, 100, 68.0)
+        pyoracle.preamble_search(rows["taps"][:, c, 2, 0], pyoracle.NAV_GPS_LNAV, cap=rows.shape[0])
+    dt = time.perf_counter() - t0
+    units = channels * rows.shape[0]
+    return {"value": units / dt, "unit": "channel-epochs/s", "cores": 1, "kind": "port",
+            "sample": f"{channels} channels x {rows.shape[0]} epochs in {dt:.2f}s (oracle observables + "
+                      "preamble search, one thread)"}
+
+
+def run_observables(args, world, rank):
+    """Tracking outputs -> observables: ugsdr_observables (pseudorange,
+    pseudophase, Doppler, SNR) and ugsdr_preamble_search (GPS LNAV) over 256
+    channels x 60,000 epochs per step, outputs resident on the device."""
+    import torch
+    from ugsdr_gb300 import api
+    if args.impl == "reference" and rank != 0:
+        return None
+    dev = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(dev)
+    rec = observables_outputs(dev)
+    n_ep, n_ch = OBS_EPOCHS, OBS_CHANNELS
+    units = n_ep * n_ch
+    workload = (f"observables: Observable arithmetic + FindPreambleGps candidates, {n_ch} channels x {n_ep} "
+                f"epochs of tracking outputs")
+    chans = observables_channels()
+    msgs = [0] * n_ch
+    if args.impl == "reference":
+        rows = rec.cpu().numpy().view(api.TRACK_DTYPE).reshape(n_ep, n_ch)
+        vals = [observables_cpu_baseline(rows) for _ in range(args.warmup + args.steps)][args.warmup:]
+        v = float(np.mean([b["value"] for b in vals]))
+        return {"metric": "observables channel-epochs/s", "value": v, "unit": "channel-epochs/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": units / v * 1e3, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+                "config": {"workload": workload},
+                "cpu_baseline": {k: vals[-1][k] for k in ("value", "unit", "cores", "kind", "sample")},
+                "e2e": {"value": v, "unit": "channel-epochs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    ctx = api.Context(dev)
+    ctx.set_stream(torch.cuda.current_stream().cuda_stream)  # the events below bracket the library's kernels
+    torch.cuda.synchronize()
+    obs = torch.empty((n_ep, n_ch, 4), dtype=torch.float64, device=f"cuda:{dev}")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{dev}")
+    h_rows = torch.empty(rec.shape, dtype=torch.float32, pin_memory=True)
+    h_rows.copy_(rec)
+    h_np = h_rows.numpy().view(api.TRACK_DTYPE).reshape(n_ep, n_ch)
+
+    def timed(k, on_device):
+        times, cands = [], None
+        l0 = ctx.launch_count()
+        for _ in range(k):
+            flush.fill_(1)  # the 1.35 GB records exceed L2 anyway; this evicts the last step's tail
+            torch.cuda.synchronize()
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record()
+            t0 = time.perf_counter()
+            if on_device:
+                api.observables(ctx, rec.data_ptr(), chans, shape=(n_ep, n_ch), out_ptr=obs.data_ptr())
+                cands = api.preamble_search(ctx, rec.data_ptr(), msgs, cap=OBS_CAP, shape=(n_ep, n_ch))
+            else:
+                out = api.observables(ctx, h_np, chans)
+                cands = api.preamble_search(ctx, h_np, msgs, cap=OBS_CAP)
+                del out
+            e.record()
+            e.synchronize()
+            times.append(max(s.elapsed_time(e) / 1e3, time.perf_counter() - t0))
+        return times, (ctx.launch_count() - l0) / k, cands
+
+    timed(args.warmup, True)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    ctx.enable_timing(True)
+    ctx.reset_timing()
+    with ClockSampler() as clk:
+        times, launches, cands = timed(args.steps, True)
+    kt = {name: ctx.kernel_time(name) for name in ("observables", "obs_preamble")}
+    ctx.enable_timing(False)
+    t_step = float(np.mean(times))
+    if world > 1:
+        t = torch.tensor([t_step], device=f"cuda:{dev}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_step = float(t.item())
+    e2e_times, _, _ = timed(max(2, args.steps // 2), False)
+    t_e2e = float(np.mean(e2e_times))
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    per_launch = {name: ms / max(cnt, 1) for name, (cnt, ms) in kt.items()}
+    top_bytes = units * OBS_BYTES
+    achieved = top_bytes / (per_launch["observables"] / 1e3) / 1e9
+    line = {
+        "metric": "observables channel-epochs/s", "value": world * units / t_step, "unit": "channel-epochs/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (device-synthesised tracking outputs, seeded)",
+        "config": {"workload": workload, "channels": n_ch, "epochs": n_ep,
+                   "candidates": int(sum(len(c) for c in cands)), "parallelism": f"replicas x{world}",
+                   "l2": f"records {units * 88 / 1e9:.2f} GB > L2; 256 MB written between steps"},
+        "e2e": {"value": world * units / t_e2e, "unit": "channel-epochs/s", "h2d_bytes_per_step": 2 * units * 88,
+                "d2h_bytes_per_step": units * 32 + 4 * n_ch * (1 + OBS_CAP),
+                "ms_per_step": t_e2e * 1e3},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "kernel": "observables (obs_sigma + obs_segsum + obs_emit)", "achieved": achieved,
+                     "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": None,
+                     "algorithmic_bytes_per_launch": top_bytes, "kernel_ms": per_launch,
+                     "peak_source": "hbm_gbs of MEASURED_PEAKS.json"},
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = observables_cpu_baseline(h_np)
+    return line
+
+
 # ------------------------------------------------------------ CPU reference
 def cpu_baseline(args, jobs, raw, fs, budget_s: float = 20.0):
     """Bounded sample of the same workload on the host cores through the CPU
@@ -975,7 +1131,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--config", choices=sorted(WORKLOADS) + ["track", "jamming"], default="multi")
+    ap.add_argument("--config", choices=sorted(WORKLOADS) + ["track", "jamming", "observables"], default="multi")
     ap.add_argument("--track-seconds", type=float, default=10.0, help="capture length of --config track")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--served", action="store_true", help="run the served request stream instead")
@@ -997,6 +1153,8 @@ def main():
         line = run_track(args, world, rank)
     elif args.config == "jamming":
         line = run_jamming(args, world, rank)
+    elif args.config == "observables":
+        line = run_observables(args, world, rank)
     else:
         line = run_ours(args, world, rank) if args.impl == "ours" else run_reference(args, world, rank)
     if rank == 0 and line is not None:

@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define UGSDR_CUDA_ABI_VERSION 5
+#define UGSDR_CUDA_ABI_VERSION 6
 
 enum ugsdr_status {
 	UGSDR_OK = 0,
@@ -338,7 +338,7 @@ typedef struct ugsdr_track_output {
 	float taps[5][2];
 	double carrier_frequency;
 	double carrier_phase;       /* rad, wrapped */
-	double code_phase;          /* chips */
+	double code_phase;          /* samples (TrackingParameters::code_phases) */
 	double code_frequency;
 	double phase_error;         /* PLL discriminator, cycles */
 	double code_error;          /* DLL discriminator */
@@ -380,6 +380,63 @@ int ugsdr_track_destroy(ugsdr_track_bank* bank);
 int ugsdr_track_refine(ugsdr_ctx* ctx, ugsdr_track_channel* channels, int n_channels, const float* codes,
 	const int* code_lens, int n_codes, int code_len_max, const void* samples, int sample_type, int samples_on_device,
 	size_t n_samples, int* accepted, int* offsets);
+
+/* ------------------------------------------------------- observables */
+/* Tracking outputs -> measurements (src/measurements/observable.hpp), for
+ * every channel of a bank at once.  `outputs` is the n_epochs x n_channels
+ * array ugsdr_track_run / ugsdr_track_run_device wrote ([epoch][channel]),
+ * on the device when outputs_on_device, else host. */
+
+/* Navigation message whose preamble ugsdr_preamble_search looks for. */
+typedef enum ugsdr_nav_message {
+	UGSDR_NAV_GPS_LNAV = 0,     /* 8-bit preamble, 20 ms bits (observable.hpp:90-98) */
+	UGSDR_NAV_GLONASS = 1       /* 40-symbol time mark, 10 ms (observable.hpp:141-151) */
+} ugsdr_nav_message;
+
+/* FindPreambleGps / FindPreambleGlonass's candidate search
+ * (observable.hpp:204-220, 260-277): per channel the navigation symbols
+ * sign(prompt I) (+1 when > 0, else -1) over all n_epochs epochs are
+ * circularly matched-filtered against the preamble upsampled to 1 ms (the
+ * reference's FFT matched filter, 2/N inverse scale, so |y| is twice the
+ * +-1 correlation) and every epoch with |y| above the reference's threshold
+ * (153 GPS, 370 GLONASS) is listed in ascending order.  The correlation is
+ * computed exactly in integers, so the list equals the reference's float
+ * one (|y| is a multiple of 4, the thresholds are not).  messages[c]: a
+ * ugsdr_nav_message per channel.  counts[c] = the number of candidates
+ * (may exceed cap); indexes: n_channels x cap epochs (host), the first
+ * min(counts[c], cap) of row c valid. */
+int ugsdr_preamble_search(ugsdr_ctx* ctx, const ugsdr_track_output* outputs, int outputs_on_device, int n_epochs,
+	int n_channels, const int* messages, int* counts, int* indexes, int cap);
+
+/* Per channel: Observable's constructor inputs (observable.hpp:75-88) and
+ * UpdatePseudoranges' term (327-336). */
+typedef struct ugsdr_observable_channel {
+	double sampling_rate;          /* Hz */
+	double intermediate_frequency; /* Hz */
+	double carrier_frequency;      /* Hz, the tracking channel's value before epoch 0 */
+	double carrier_phase;          /* rad, the tracking channel's value before epoch 0 */
+	long long preamble_position;   /* epoch whose code phase gives the integer-ms offset */
+	double range_correction_ms;    /* added to every pseudorange: UpdatePseudorangeGps/Glonass's
+	                                  time_scale[i] - (i - preamble_position + tow_ms + 2), which
+	                                  does not depend on i; 0 before the time scale is known */
+} ugsdr_observable_channel;
+
+/* One channel-epoch measurement. */
+typedef struct ugsdr_observable {
+	double pseudorange; /* ms: code_phases[i] * 1000 / fs - int32(code_phases[pos] * 1000 / fs) + correction */
+	double pseudophase; /* cycles: -carrier_phase[i] / 2 pi + (i + 1) * IF / 1000 */
+	double doppler;     /* Hz: frequencies[i] - IF */
+	double snr;         /* dB-Hz: 27 + 20 log10(|I_P[i]| / sigma(Q_P)) (CalculateSnr, 55-72) */
+} ugsdr_observable;
+
+/* Observable's per-epoch arithmetic for all channels.  The carrier phase
+ * is the tracking loop's unwrapped phase (carrier_phase before epoch 0, plus
+ * each epoch's carrier_frequency / 1000 and phase_error / 4 cycles), which
+ * the bank outputs wrapped; sigma is SequentialMeanStdDev over the
+ * channel's prompt Q in float, in epoch order.  out: n_epochs x n_channels
+ * ([epoch][channel]), on the device when outputs_on_device, else host. */
+int ugsdr_observables(ugsdr_ctx* ctx, const ugsdr_track_output* outputs, int outputs_on_device, int n_epochs,
+	int n_channels, const ugsdr_observable_channel* channels, ugsdr_observable* out);
 
 /* --------------------------------------------- interference mitigation */
 /* The antijamming stage the digital front end runs after resampling when

@@ -275,3 +275,39 @@ def jamming(x: np.ndarray, fs: float, suppress: bool = True):
                                          _p(jn), 64)
     det = [(int(types[i]), int(bins[i]), float(freqs[i]), float(jn[i])) for i in range(min(cnt, 64))]
     return det, y
+
+
+NAV_GPS_LNAV, NAV_GLONASS = 0, 1
+
+
+def preamble_search(prompt_i: np.ndarray, message: int, cap: int = 4096) -> list[int]:
+    """FindPreambleGps / Glonass's candidate epochs (obs_oracle.cpp), ascending."""
+    fn = load().orc_preamble_search
+    fn.argtypes = [C.c_void_p, C.c_size_t, C.c_int, C.c_void_p, C.c_int]
+    fn.restype = C.c_int
+    x = np.ascontiguousarray(prompt_i, np.float32)
+    idx = np.zeros(cap, np.int32)
+    n = fn(x.ctypes.data, x.size, message, idx.ctypes.data, cap)
+    if n > cap:
+        raise ValueError(f"{n} candidates, more than cap={cap}")
+    return idx[:n].tolist()
+
+
+def observables(rows: np.ndarray, fs: float, intermediate_frequency: float, carrier_frequency0: float,
+                carrier_phase0: float, position: int, correction: float = 0.0) -> np.ndarray:
+    """Observable's arithmetic for one channel (obs_oracle.cpp) from its
+    tracking rows (TRACK_DTYPE-like record array with taps, carrier_frequency,
+    phase_error, code_phase); (n, 4): pseudorange, pseudophase, doppler, snr."""
+    fn = load().orc_observables_f64
+    d = C.c_double
+    fn.argtypes = [C.c_void_p] * 5 + [C.c_size_t, d, d, d, d, C.c_size_t, d, C.c_void_p]
+    fn.restype = None
+    pi = np.ascontiguousarray(rows["taps"][:, 2, 0], np.float32)
+    pq = np.ascontiguousarray(rows["taps"][:, 2, 1], np.float32)
+    f = np.ascontiguousarray(rows["carrier_frequency"], np.float64)
+    err = np.ascontiguousarray(rows["phase_error"], np.float64)
+    cp = np.ascontiguousarray(rows["code_phase"], np.float64)
+    out = np.zeros((len(rows), 4))
+    fn(pi.ctypes.data, pq.ctypes.data, f.ctypes.data, err.ctypes.data, cp.ctypes.data, len(rows), fs,
+       intermediate_frequency, carrier_frequency0, carrier_phase0, position, correction, out.ctypes.data)
+    return out

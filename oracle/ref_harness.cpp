@@ -233,6 +233,28 @@ void ref_mean_std_f32(const float* in, std::size_t n, float* mean, float* sigma)
 	*mean = r.mean;
 	*sigma = r.sigma;
 }
+// FindPreambleGps / FindPreambleGlonass's filter (measurements/observable.hpp:
+// 206-215, 263-272) through the reference's own primitives: the navigation
+// symbols sign(prompt I) as complex, the preamble symbols (restated from
+// observable.hpp:92-94, 143-146: Observable does not compile without IPP)
+// upsampled by SequentialUpsampler and resized to the prompt's length,
+// SequentialMatchedFilter::Filter, SequentialAbs.  out: n magnitudes.
+void ref_preamble_filter_f32(const float* prompt_i, std::size_t n, int message, float* out) {
+	static const float gps[8] = {1, -1, -1, -1, 1, -1, 1, 1};
+	static const float glo[40] = {-1, -1, -1, -1, -1, 1, 1, 1, -1, -1, 1, -1, -1, -1, 1, -1, 1, -1, 1, 1,
+		1, 1, -1, 1, 1, -1, 1, -1, -1, 1, 1, -1, 1, -1, 1, -1, 1, -1, -1, 1};
+	const float* sym = message == 1 ? glo : gps;
+	const std::size_t n_sym = message == 1 ? 40 : 8, up = message == 1 ? 10 : 20;
+	std::vector<std::complex<float>> preamble(sym, sym + n_sym);
+	ugsdr::SequentialUpsampler::Transform(preamble, preamble.size() * up);
+	preamble.resize(n);
+	std::vector<std::complex<float>> bits(n);
+	for (std::size_t i = 0; i < n; ++i)
+		bits[i] = prompt_i[i] > 0 ? 1.f : -1.f;
+	const auto filtered = ugsdr::SequentialMatchedFilter::Filter(std::as_const(bits), preamble);
+	const auto y = ugsdr::SequentialAbs::Transform(filtered);
+	std::memcpy(out, y.data(), sizeof(float) * n);
+}
 // SequentialResampler (resampler.hpp:39-46) on complex samples; returns output length
 std::size_t ref_resample_c32(const float* iq, std::size_t n, float* out, std::size_t cap, std::size_t new_fs, std::size_t old_fs) {
 	auto v = ToComplex(iq, n);

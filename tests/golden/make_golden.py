@@ -6,7 +6,7 @@ by `make -C oracle ref REF_DIR=...` into oracle/_ref/libugsdr_ref.so
 small .npz fixtures.  Only this script needs the reference tree; the tests
 read the committed fixtures.
 
-    python tests/golden/make_golden.py [REF_DIR]
+    python tests/golden/make_golden.py [REF_DIR [FIXTURE ...]]
 """
 from __future__ import annotations
 
@@ -58,6 +58,7 @@ def ref_lib(ref_dir: str) -> C.CDLL:
     lib.ref_bbp_read.argtypes = [C.c_char_p, d, d, sz, vp]
     lib.ref_bbp_read.restype = C.c_long
     lib.ref_nt1065_decode.argtypes = [vp, sz, i, vp]
+    lib.ref_preamble_filter_f32.argtypes = [vp, sz, i, vp]
     lib.ref_stft_f32.argtypes = [vp, sz, vp, sz]
     lib.ref_stft_f32.restype = C.c_long
     lib.ref_istft_f32.argtypes = [vp, sz, vp]
@@ -338,9 +339,77 @@ def jamming(lib) -> dict[str, np.ndarray]:
     return out
 
 
+# navigation-symbol streams for the preamble search: (name, message, epochs,
+# symbol period ms, preamble period in symbols, seed).  GPS LNAV repeats its
+# preamble every subframe (300 bits), the GLONASS time mark every string (2 s).
+PREAMBLE_CASES = [
+    ("gps_two_subframes", 0, 12000, 20, 300, 11),
+    ("gps_inverted", 0, 12000, 20, 300, 12),
+    ("gps_odd_length", 0, 6007, 20, 300, 13),
+    ("gps_shorter_than_preamble", 0, 100, 20, 300, 14),
+    ("gps_zeros", 0, 4000, 20, 300, 15),
+    ("glonass_strings", 1, 8000, 10, 200, 16),
+    ("glonass_odd_length", 1, 4001, 10, 200, 17),
+]
+GPS_PREAMBLE = [1, -1, -1, -1, 1, -1, 1, 1]
+GLONASS_PREAMBLE = [-1, -1, -1, -1, -1, 1, 1, 1, -1, -1, 1, -1, -1, -1, 1, -1, 1, -1, 1, 1,
+                    1, 1, -1, 1, 1, -1, 1, -1, -1, 1, 1, -1, 1, -1, 1, -1, 1, -1, -1, 1]
+
+
+def preamble_input(name: str, message: int, n: int, period_ms: int, every: int, seed: int) -> np.ndarray:
+    """Prompt I (int8 steps) of a channel carrying the message: random symbols
+    with the preamble every `every` symbols from a random start, noise, a few
+    exact zeros (the search's `> 0` test)."""
+    rng = np.random.default_rng(seed)
+    pre = np.array(GLONASS_PREAMBLE if message == 1 else GPS_PREAMBLE)
+    n_sym = -(-n // period_ms)
+    sym = rng.choice([-1, 1], n_sym)
+    for s in range(int(rng.integers(0, every)), n_sym - len(pre), every):
+        sym[s:s + len(pre)] = pre
+    if "inverted" in name:
+        sym = -sym
+    x = np.repeat(sym, period_ms)[:n] * 40 + rng.normal(0, 12, n)
+    if "zeros" in name:
+        x[:] = 0
+    x = np.clip(np.rint(x), -127, 127)
+    x[rng.integers(0, n, max(1, n // 500))] = 0
+    return x.astype(np.int8)
+
+
+def preamble(lib) -> dict[str, np.ndarray]:
+    """The reference's own matched filter + |.| (ref_preamble_filter_f32) over
+    sign(prompt I); candidates = epochs above the reference's threshold."""
+    out = {}
+    for name, message, n, period_ms, every, seed in PREAMBLE_CASES:
+        x = preamble_input(name, message, n, period_ms, every, seed)
+        xf = x.astype(np.float32)
+        y = np.zeros(n, np.float32)
+        lib.ref_preamble_filter_f32(p(xf), n, message, p(y))
+        threshold = 370 if message == 1 else 153
+        idx = np.flatnonzero(y > threshold).astype(np.int32)
+        # |y| is twice an integer correlation: far from the threshold
+        margin = np.min(np.abs(y - threshold))
+        assert margin > 0.5, (name, margin)
+        out[f"{name}/prompt_i"] = x
+        out[f"{name}/message"] = np.int32(message)
+        out[f"{name}/indexes"] = idx
+        out[f"{name}/peak"] = np.float32(y.max())
+    # CalculateSnr's sigma: the reference's SequentialMeanStdDev over a prompt Q
+    q = np.random.default_rng(18).normal(3.0, 40.0, 2000).astype(np.float32)
+    mean, sigma = C.c_float(), C.c_float()
+    lib.ref_mean_std_f32(p(q), q.size, C.byref(mean), C.byref(sigma))
+    out["sigma/prompt_q"] = q
+    out["sigma/value"] = np.float32(sigma.value)
+    return out
+
+
 def main() -> None:
     ref_dir = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     lib = ref_lib(ref_dir)
+    if len(sys.argv) > 2:  # regenerate the named fixtures only, e.g. `preamble`
+        for name in sys.argv[2:]:
+            np.savez_compressed(HERE / f"{name}.npz", **globals()[name](lib))
+        return
     c = codes(lib)
     np.savez_compressed(HERE / "codes.npz", **c)
     k = kats(lib, c)
@@ -351,6 +420,7 @@ def main() -> None:
     np.savez_compressed(HERE / "jamming.npz", **jamming(lib))
     np.savez_compressed(HERE / "real8.npz", **real8(ref_dir))
     np.savez_compressed(HERE / "iq16.npz", **iq16(ref_dir))
+    np.savez_compressed(HERE / "preamble.npz", **preamble(lib))
     for f in sorted(HERE.glob("*.npz")):
         print(f.name, f.stat().st_size)
 

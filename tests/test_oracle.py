@@ -166,3 +166,59 @@ def test_stft_round_trip(oracle):
     np.testing.assert_array_equal(syn, z["istft"])
     x = z["tone_in"]
     np.testing.assert_allclose(syn[96:len(syn) - 96], 4 * x[96:len(syn) - 96], rtol=0, atol=1e-4 * np.abs(x).max())
+
+
+PREAMBLE_CASES = ("gps_two_subframes", "gps_inverted", "gps_odd_length", "gps_shorter_than_preamble", "gps_zeros",
+                  "glonass_strings", "glonass_odd_length")
+
+
+@pytest.mark.parametrize("case", PREAMBLE_CASES)
+def test_preamble_search(oracle, case):
+    """FindPreambleGps / Glonass's candidate epochs: the oracle's FP64 matched
+    filter against the reference's own float one (SequentialMatchedFilter +
+    SequentialAbs over sign(prompt I), thresholds 153 / 370), and both
+    against the exact integer correlation they approximate (|y| = 2 |sum of
+    +-1 products|, so every value is a multiple of 4 away from a threshold
+    that is not)."""
+    z = np.load(Path(__file__).parent / "golden" / "preamble.npz")
+    x = z[f"{case}/prompt_i"].astype(np.float32)
+    msg = int(z[f"{case}/message"])
+    got = oracle.preamble_search(x, msg, cap=len(x))
+    assert got == z[f"{case}/indexes"].tolist()
+    sym = [1, -1, -1, -1, 1, -1, 1, 1] if msg == 0 else None
+    if sym is not None:
+        b = np.where(x > 0, 1, -1)
+        p = np.repeat(sym, 20)[: len(x)]
+        s = np.array([int(np.dot(np.roll(b, -k)[: len(p)], p)) for k in range(len(x))])
+        assert np.flatnonzero(2 * np.abs(s) > 153).tolist() == got
+
+
+def test_observables_oracle(oracle):
+    """Observable's arithmetic (observable.hpp:75-88) on a synthetic history:
+    sigma equals the reference's SequentialMeanStdDev, the SNR follows
+    27 + 20 log10(|I| / sigma) in float, the pseudorange offset is the
+    truncated ms of the preamble epoch, and the phase the reference's radian
+    accumulation."""
+    z = np.load(Path(__file__).parent / "golden" / "preamble.npz")
+    q = z["sigma/prompt_q"]
+    n = len(q)
+    rng = np.random.default_rng(5)
+    rows = np.zeros(n, [("taps", "<f4", (5, 2)), ("carrier_frequency", "<f8"), ("phase_error", "<f8"),
+                        ("code_phase", "<f8")])
+    rows["taps"][:, 2, 0] = rng.normal(0, 300, n).astype(np.float32)
+    rows["taps"][:, 2, 1] = q
+    rows["carrier_frequency"] = 1500.0 + np.cumsum(rng.normal(0, 0.01, n))
+    rows["phase_error"] = rng.normal(0, 0.02, n)
+    rows["code_phase"] = 2345.678 - np.arange(n) * 1e-3
+    fs, if_hz, f0, ph0, pos, corr = 4e6, 1000.0, 1499.5, 0.3, 17, 68.0
+    o = oracle.observables(rows, fs, if_hz, f0, ph0, pos, corr)
+    sigma = z["sigma/value"]
+    snr = np.float32(27) + np.float32(20) * np.log10(np.abs(rows["taps"][:, 2, 0]) / sigma)
+    np.testing.assert_allclose(o[:, 3], snr, rtol=0, atol=1e-5)  # dB: a float ulp near 27
+    s2ms = 1000 / fs
+    off = int(rows["code_phase"][pos] * s2ms)
+    np.testing.assert_array_equal(o[:, 0], rows["code_phase"] * s2ms - off + corr)
+    np.testing.assert_array_equal(o[:, 2], rows["carrier_frequency"] - if_hz)
+    f_prev = np.concatenate([[f0], rows["carrier_frequency"][:-1]])
+    cycles = ph0 / (2 * np.pi) + np.cumsum(f_prev / 1000 + rows["phase_error"] / 4)
+    np.testing.assert_allclose(o[:, 1], -cycles + np.arange(1, n + 1) * if_hz / 1e3, rtol=0, atol=1e-8)

@@ -10,7 +10,7 @@ from pathlib import Path
 
 LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libugsdr_cuda.so"
 
-ABI_VERSION = 5  # UGSDR_CUDA_ABI_VERSION the structs below mirror
+ABI_VERSION = 6  # UGSDR_CUDA_ABI_VERSION the structs below mirror
 
 OK = 0
 E_INVALID = -1
@@ -108,6 +108,20 @@ class TrackOutput(C.Structure):
     ]
 
 
+NAV_GPS_LNAV, NAV_GLONASS = 0, 1
+
+
+class ObservableChannel(C.Structure):
+    _fields_ = [("sampling_rate", C.c_double), ("intermediate_frequency", C.c_double),
+                ("carrier_frequency", C.c_double), ("carrier_phase", C.c_double),
+                ("preamble_position", C.c_longlong), ("range_correction_ms", C.c_double)]
+
+
+class Observable(C.Structure):
+    _fields_ = [("pseudorange", C.c_double), ("pseudophase", C.c_double), ("doppler", C.c_double),
+                ("snr", C.c_double)]
+
+
 SERVE_FIFO, SERVE_RESPONSE_RATIO = 0, 1
 
 INTERFERENCE_NONE, INTERFERENCE_NARROWBAND, INTERFERENCE_WIDEBAND = 0, 1, 2
@@ -165,6 +179,8 @@ SIGNATURES = {
     "ugsdr_track_destroy": (_i, [_vp]),
     "ugsdr_track_refine": (_i, [_vp, C.POINTER(TrackChannel), _i, _vp, C.POINTER(_i), _i, _i, _vp, _i, _i, _sz,
                                 C.POINTER(_i), C.POINTER(_i)]),
+    "ugsdr_preamble_search": (_i, [_vp, _vp, _i, _i, _i, C.POINTER(_i), C.POINTER(_i), C.POINTER(_i), _i]),
+    "ugsdr_observables": (_i, [_vp, _vp, _i, _i, _i, C.POINTER(ObservableChannel), _vp]),
     "ugsdr_stft": (_i, [_vp, _vp, _sz, _i, _i, _vp, C.POINTER(_sz)]),
     "ugsdr_istft": (_i, [_vp, _vp, _sz, _i, _i, _vp]),
     "ugsdr_jamming_detect": (_i, [_vp, _vp, _sz, _d, _i, C.POINTER(JammingDetection), _i, C.POINTER(_i)]),

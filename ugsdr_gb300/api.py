@@ -431,6 +431,66 @@ def track_refine(ctx: Context, channels: list[dict], codes: list[np.ndarray], sa
     return list(acc), list(off), out
 
 
+OBSERVABLE_DTYPE = np.dtype([("pseudorange", "<f8"), ("pseudophase", "<f8"), ("doppler", "<f8"), ("snr", "<f8")])
+
+
+def _outputs_arg(outputs, shape):
+    """(pointer, on_device, n_epochs, n_channels, keep-alive) of tracking-bank
+    outputs: a TRACK_DTYPE array (host) or a device pointer with its shape."""
+    if isinstance(outputs, np.ndarray):
+        if outputs.dtype != TRACK_DTYPE or outputs.ndim != 2 or not outputs.flags.c_contiguous:
+            raise ValueError("outputs must be a contiguous (n_epochs, n_channels) TRACK_DTYPE array")
+        return outputs.ctypes.data, 0, outputs.shape[0], outputs.shape[1], outputs
+    if shape is None:
+        raise ValueError("a device pointer needs shape=(n_epochs, n_channels)")
+    return int(outputs), 1, int(shape[0]), int(shape[1]), None
+
+
+def preamble_search(ctx: Context, outputs, messages: list[int], cap: int = 4096, shape=None) -> list[list[int]]:
+    """ugsdr_preamble_search: per channel the epochs where the navigation
+    symbols match the message's preamble (FindPreambleGps / Glonass's
+    candidates), ascending.  `outputs`: the bank's TRACK_DTYPE rows, or a
+    device pointer with shape=(n_epochs, n_channels)."""
+    ptr, dev, n_ep, n_ch, keep = _outputs_arg(outputs, shape)
+    if len(messages) != n_ch:
+        raise ValueError("one message per channel")
+    msg = (C.c_int * n_ch)(*messages)
+    counts = (C.c_int * n_ch)()
+    idx = np.zeros((n_ch, max(cap, 1)), np.int32)
+    ctx._check(ctx.lib.ugsdr_preamble_search(ctx.h, C.c_void_p(ptr), dev, n_ep, n_ch, msg, counts,
+                                             C.cast(idx.ctypes.data, C.POINTER(C.c_int)), cap))
+    del keep
+    if any(c > cap for c in counts):
+        raise ValueError(f"more than cap={cap} candidates: {max(counts)}")
+    return [idx[c, :counts[c]].tolist() for c in range(n_ch)]
+
+
+def observables(ctx: Context, outputs, channels: list[dict], shape=None, out_ptr: int | None = None):
+    """ugsdr_observables: pseudorange (ms), pseudophase (cycles), Doppler (Hz)
+    and SNR (dB-Hz) per epoch and channel from the bank's outputs.  channels:
+    dicts with fs, carrier_frequency, optional intermediate_frequency,
+    carrier_phase, preamble_position, range_correction_ms.  Host outputs give
+    an (n_epochs, n_channels) OBSERVABLE_DTYPE array; a device pointer (with
+    shape) writes to the device pointer out_ptr and returns None."""
+    ptr, dev, n_ep, n_ch, keep = _outputs_arg(outputs, shape)
+    if len(channels) != n_ch:
+        raise ValueError("one channel description per channel")
+    chs = (L.ObservableChannel * n_ch)()
+    for i, ch in enumerate(channels):
+        chs[i] = L.ObservableChannel(ch["fs"], ch.get("intermediate_frequency", 0.0), ch["carrier_frequency"],
+                                     ch.get("carrier_phase", 0.0), ch.get("preamble_position", 0),
+                                     ch.get("range_correction_ms", 0.0))
+    if dev:
+        if not out_ptr:
+            raise ValueError("device outputs need a device out_ptr")
+        ctx._check(ctx.lib.ugsdr_observables(ctx.h, C.c_void_p(ptr), 1, n_ep, n_ch, chs, C.c_void_p(int(out_ptr))))
+        return None
+    out = np.zeros((n_ep, n_ch), OBSERVABLE_DTYPE)
+    ctx._check(ctx.lib.ugsdr_observables(ctx.h, C.c_void_p(ptr), 0, n_ep, n_ch, chs, C.c_void_p(out.ctypes.data)))
+    del keep
+    return out
+
+
 class Server:
     """Continuous-batching acquisition server (ugsdr_server_*)."""
 

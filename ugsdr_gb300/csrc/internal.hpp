@@ -152,6 +152,8 @@ struct ugsdr_ctx {
 	// outputs): shared by the context's banks, whose calls the context
 	// serialises on its stream, and kept between banks
 	ugsdr_gpu::DevBuf track_samples, track_unpacked, track_out;
+	// observables: staged bank outputs (host callers), observables, scratch
+	ugsdr_gpu::DevBuf obs_in, obs_out, obs_tmp;
 	// copies of host-buffer calls that overlap the context stream's kernels
 	// (created on first use): a stream and per-slot events
 	cudaStream_t copy_stream = nullptr;
