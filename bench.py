@@ -1005,10 +1005,10 @@ def run_observables(args, world, rank):
             t0 = time.perf_counter()
             if on_device:
                 api.observables(ctx, rec.data_ptr(), chans, shape=(n_ep, n_ch), out_ptr=obs.data_ptr())
-                cands = api.preamble_search(ctx, rec.data_ptr(), msgs, cap=OBS_CAP, shape=(n_ep, n_ch))
+                cands = api.preamble_search(ctx, rec.data_ptr(), msgs, cap=OBS_CAP, shape=(n_ep, n_ch), as_arrays=True)
             else:
                 out = api.observables(ctx, h_np, chans)
-                cands = api.preamble_search(ctx, h_np, msgs, cap=OBS_CAP)
+                cands = api.preamble_search(ctx, h_np, msgs, cap=OBS_CAP, as_arrays=True)
                 del out
             e.record()
             e.synchronize()
@@ -1043,7 +1043,7 @@ def run_observables(args, world, rank):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (device-synthesised tracking outputs, seeded)",
         "config": {"workload": workload, "channels": n_ch, "epochs": n_ep,
-                   "candidates": int(sum(len(c) for c in cands)), "parallelism": f"replicas x{world}",
+                   "candidates": int(cands[0].sum()), "parallelism": f"replicas x{world}",
                    "l2": f"records {units * 88 / 1e9:.2f} GB > L2; 256 MB written between steps"},
         "e2e": {"value": world * units / t_e2e, "unit": "channel-epochs/s", "h2d_bytes_per_step": 2 * units * 88,
                 "d2h_bytes_per_step": units * 32 + 4 * n_ch * (1 + OBS_CAP),

@@ -446,22 +446,27 @@ def _outputs_arg(outputs, shape):
     return int(outputs), 1, int(shape[0]), int(shape[1]), None
 
 
-def preamble_search(ctx: Context, outputs, messages: list[int], cap: int = 4096, shape=None) -> list[list[int]]:
+def preamble_search(ctx: Context, outputs, messages: list[int], cap: int = 4096, shape=None, as_arrays: bool = False):
     """ugsdr_preamble_search: per channel the epochs where the navigation
     symbols match the message's preamble (FindPreambleGps / Glonass's
     candidates), ascending.  `outputs`: the bank's TRACK_DTYPE rows, or a
-    device pointer with shape=(n_epochs, n_channels)."""
+    device pointer with shape=(n_epochs, n_channels).  Returns a list of
+    lists, or with as_arrays the (counts, indexes[n_channels, cap]) arrays
+    as the C call fills them."""
     ptr, dev, n_ep, n_ch, keep = _outputs_arg(outputs, shape)
     if len(messages) != n_ch:
         raise ValueError("one message per channel")
-    msg = (C.c_int * n_ch)(*messages)
-    counts = (C.c_int * n_ch)()
-    idx = np.zeros((n_ch, max(cap, 1)), np.int32)
-    ctx._check(ctx.lib.ugsdr_preamble_search(ctx.h, C.c_void_p(ptr), dev, n_ep, n_ch, msg, counts,
-                                             C.cast(idx.ctypes.data, C.POINTER(C.c_int)), cap))
+    msg = np.ascontiguousarray(messages, np.int32)
+    counts = np.zeros(n_ch, np.int32)
+    idx = np.empty((n_ch, max(cap, 1)), np.int32)
+    ip = C.POINTER(C.c_int)
+    ctx._check(ctx.lib.ugsdr_preamble_search(ctx.h, C.c_void_p(ptr), dev, n_ep, n_ch, msg.ctypes.data_as(ip),
+                                             counts.ctypes.data_as(ip), idx.ctypes.data_as(ip), cap))
     del keep
-    if any(c > cap for c in counts):
-        raise ValueError(f"more than cap={cap} candidates: {max(counts)}")
+    if counts.max() > cap:
+        raise ValueError(f"more than cap={cap} candidates: {counts.max()}")
+    if as_arrays:
+        return counts, idx
     return [idx[c, :counts[c]].tolist() for c in range(n_ch)]
 
 

@@ -169,10 +169,24 @@ namespace ugsdr_gpu {
 				const int nx = e0 + 32 + lane;
 				const float v_next = nx < n ? rec(p, nx, c).taps[2][1] : 0.f;
 				const int cnt = min(32, n - e0);
-				for (int j = 0; j < cnt; ++j) {
-					const float x = __shfl_sync(0xffffffffu, v, j);
-					q = __fadd_rn(q, __fmul_rn(x, x));
-					m = __fadd_rn(m, x);
+				if (cnt == 32) {
+					// all 32 shuffles issue ahead of the two serial add chains
+					float x[32];
+#pragma unroll
+					for (int j = 0; j < 32; ++j)
+						x[j] = __shfl_sync(0xffffffffu, v, j);
+#pragma unroll
+					for (int j = 0; j < 32; ++j) {
+						q = __fadd_rn(q, __fmul_rn(x[j], x[j]));
+						m = __fadd_rn(m, x[j]);
+					}
+				}
+				else {
+					for (int j = 0; j < cnt; ++j) {
+						const float x = __shfl_sync(0xffffffffu, v, j);
+						q = __fadd_rn(q, __fmul_rn(x, x));
+						m = __fadd_rn(m, x);
+					}
 				}
 				v = v_next;
 			}
