@@ -937,6 +937,24 @@ def observables_outputs(dev):
     return rec
 
 
+def observables_rows_host(n_ch):
+    """The device synthesis's distribution for `n_ch` channels, drawn on the
+    host with numpy (the reference arm needs no GPU): TRACK_DTYPE rows."""
+    from ugsdr_gb300.api import TRACK_DTYPE
+    rng = np.random.default_rng(7)
+    n_ep = OBS_EPOCHS
+    rows = np.zeros((n_ep, n_ch), TRACK_DTYPE)
+    taps = rng.normal(0, 40, (n_ep, n_ch, 5, 2)).astype(np.float32)
+    taps[:, :, 2, 0] += 300 * np.repeat(rng.choice([-1, 1], (n_ep // 20 + 1, n_ch)), 20, axis=0)[:n_ep]
+    rows["taps"] = taps
+    rows["carrier_frequency"] = 2000.0 + rng.normal(0, 1, (n_ep, n_ch))
+    rows["carrier_phase"] = rng.random((n_ep, n_ch)) * 2 * np.pi
+    rows["code_phase"] = 5000.0 + rng.random((1, n_ch)) * 1000
+    rows["code_frequency"] = 1.023e6
+    rows["phase_error"] = rng.normal(0, 0.02, (n_ep, n_ch))
+    return rows
+
+
 def observables_channels():
     return [dict(fs=OBS_FS, intermediate_frequency=0.0, carrier_frequency=2000.0, carrier_phase=0.0,
                  preamble_position=100, range_correction_ms=68.0) for _ in range(OBS_CHANNELS)]
@@ -962,21 +980,15 @@ def run_observables(args, world, rank):
     """Tracking outputs -> observables: ugsdr_observables (pseudorange,
     pseudophase, Doppler, SNR) and ugsdr_preamble_search (GPS LNAV) over 256
     channels x 60,000 epochs per step, outputs resident on the device."""
-    import torch
     from ugsdr_gb300 import api
     if args.impl == "reference" and rank != 0:
         return None
-    dev = int(os.environ.get("LOCAL_RANK", 0))
-    torch.cuda.set_device(dev)
-    rec = observables_outputs(dev)
     n_ep, n_ch = OBS_EPOCHS, OBS_CHANNELS
     units = n_ep * n_ch
     workload = (f"observables: Observable arithmetic + FindPreambleGps candidates, {n_ch} channels x {n_ep} "
                 f"epochs of tracking outputs")
-    chans = observables_channels()
-    msgs = [0] * n_ch
     if args.impl == "reference":
-        rows = rec.cpu().numpy().view(api.TRACK_DTYPE).reshape(n_ep, n_ch)
+        rows = observables_rows_host(32)  # the channels the bounded sample times
         vals = [observables_cpu_baseline(rows) for _ in range(args.warmup + args.steps)][args.warmup:]
         v = float(np.mean([b["value"] for b in vals]))
         return {"metric": "observables channel-epochs/s", "value": v, "unit": "channel-epochs/s", "n_gpus": world,
@@ -985,6 +997,12 @@ def run_observables(args, world, rank):
                 "config": {"workload": workload},
                 "cpu_baseline": {k: vals[-1][k] for k in ("value", "unit", "cores", "kind", "sample")},
                 "e2e": {"value": v, "unit": "channel-epochs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    import torch
+    dev = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(dev)
+    rec = observables_outputs(dev)
+    chans = observables_channels()
+    msgs = [0] * n_ch
     ctx = api.Context(dev)
     ctx.set_stream(torch.cuda.current_stream().cuda_stream)  # the events below bracket the library's kernels
     torch.cuda.synchronize()
