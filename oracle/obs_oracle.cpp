@@ -13,9 +13,12 @@
 //     (55-72) and the i-independent UpdatePseudorange term (327-336).
 // The reference's Observable does not compile without Intel IPP here (its
 // src/tracking/tracking_parameters.hpp:47-56 non-IPP configuration has its
-// arguments out of order and a trailing comma), so this file restates it;
-// the primitives it leans on (the matched filter, SequentialMeanStdDev) are
-// checked against the reference's own compiled ones by the tests.
+// arguments out of order and a trailing comma), so this file restates it.
+// Pinned: the candidate search (against the reference's own upsampler,
+// matched filter and abs, tests/golden/preamble.npz) and CalculateSnr's
+// sigma (against its SequentialMeanStdDev).  The constructor's pseudorange /
+// pseudophase / Doppler lines are parity unpinned: restated by reading
+// observable.hpp:75-88 and 327-336, no reference output covers them.
 #include "fft64.hpp"
 
 #include <cmath>
