@@ -6,8 +6,12 @@ capture of int16 I/Q at 50 MHz (synthetic, seeded):
   GLONASS L1OF 14 FDMA channels k = -7..+6 (562.5 kHz spacing), same grid
   Galileo E1B  36 PRNs,  4 ms coherent (200,000-point FFT) x 10 blocks, +-5 kHz / 62.5 Hz (161 bins)
 = 1.254e9 cells per step; one step = the 16 jobs of one capture through
-ugsdr_acquire_batch.  `--config gps_l1_4mhz` runs the 4 MHz / 4000-point
-GPS L1 C/A search instead.
+ugsdr_acquire_batch.  Other lines:
+  --config gps_l1_4mhz | l5_weak | gal_small   other acquisition searches
+  --config track         256-channel tracking bank, 10 s at 20 MHz
+  --config jamming       interference stage, 400 ms at 50 MHz
+  --config observables   observables + preamble search, 256 ch x 60,000 epochs
+  --served               the Poisson request stream through the server
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
