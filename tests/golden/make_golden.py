@@ -350,6 +350,7 @@ PREAMBLE_CASES = [
     ("gps_zeros", 0, 4000, 20, 300, 15),
     ("glonass_strings", 1, 8000, 10, 200, 16),
     ("glonass_odd_length", 1, 4001, 10, 200, 17),
+    ("glonass_shorter_than_preamble", 1, 255, 10, 200, 19),
 ]
 GPS_PREAMBLE = [1, -1, -1, -1, 1, -1, 1, 1]
 GLONASS_PREAMBLE = [-1, -1, -1, -1, -1, 1, 1, 1, -1, -1, 1, -1, -1, -1, 1, -1, 1, -1, 1, 1,
@@ -366,6 +367,10 @@ def preamble_input(name: str, message: int, n: int, period_ms: int, every: int, 
     sym = rng.choice([-1, 1], n_sym)
     for s in range(int(rng.integers(0, every)), n_sym - len(pre), every):
         sym[s:s + len(pre)] = pre
+    if "shorter" in name and message == 1:
+        # the prompt is the cut preamble itself, rotated: the circular
+        # filter finds it across the wrap
+        sym = np.roll(pre[:n_sym], int(rng.integers(1, n_sym)))
     if "inverted" in name:
         sym = -sym
     x = np.repeat(sym, period_ms)[:n] * 40 + rng.normal(0, 12, n)

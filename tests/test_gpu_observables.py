@@ -4,7 +4,7 @@ observable.hpp.
 
   * Preamble candidates: the fixture lists come from the reference's own
     matched filter (tests/golden/preamble.npz); the device lists must equal
-    them exactly, for GPS LNAV and GLONASS, odd lengths, a prompt shorter than
+    them exactly, for GPS LNAV and GLONASS, odd lengths, prompts shorter than
     the preamble, an inverted stream and an all-zero prompt.
   * Observable arithmetic on a real tracking run: pseudorange and Doppler bit
     for bit (the same double operations), SNR within a float ulp of 27 dB
@@ -24,7 +24,7 @@ from ugsdr_gb300 import signals
 pytestmark = pytest.mark.gpu
 GOLDEN = Path(__file__).parent / "golden" / "preamble.npz"
 CASES = ("gps_two_subframes", "gps_inverted", "gps_odd_length", "gps_shorter_than_preamble", "gps_zeros",
-         "glonass_strings", "glonass_odd_length")
+         "glonass_strings", "glonass_odd_length", "glonass_shorter_than_preamble")
 
 
 def bank_rows(prompt_i: np.ndarray) -> np.ndarray:

@@ -169,7 +169,7 @@ def test_stft_round_trip(oracle):
 
 
 PREAMBLE_CASES = ("gps_two_subframes", "gps_inverted", "gps_odd_length", "gps_shorter_than_preamble", "gps_zeros",
-                  "glonass_strings", "glonass_odd_length")
+                  "glonass_strings", "glonass_odd_length", "glonass_shorter_than_preamble")
 
 
 @pytest.mark.parametrize("case", PREAMBLE_CASES)
