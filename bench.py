@@ -48,20 +48,27 @@ def log2(x):
 
 
 # ------------------------------------------------------------------ workload
-def galileo_chips():
+# Codes of every workload come from tests/golden/codes.npz, which the
+# reference's own PrnGenerator::Get produced (the library's generators are
+# bit-exact against it): both arms read the same chips, and the reference arm
+# never loads the product library.
+def golden_chips(name):
     z = np.load(ROOT / "tests" / "golden" / "codes.npz")
-    n = int(z["galileo_e1b_len"])
-    bits = np.unpackbits(z["galileo_e1b"], axis=1)[:, :n]
+    n = int(z[f"{name}_len"])
+    bits = np.unpackbits(z[name], axis=1)[:, :n]
     return (1.0 - 2.0 * bits).astype(np.float32)
+
+
+def galileo_chips():
+    return golden_chips("galileo_e1b")
 
 
 def multi_workload(seed: int = 2):
     """Jobs (as plain dicts) and the synthetic int16 capture."""
-    from ugsdr_gb300 import _lib as L
-    from ugsdr_gb300 import api, signals
+    from ugsdr_gb300 import signals
     rng = np.random.default_rng(seed)
-    gps = {p: api.prn_code(L.GPS_L1CA, p) for p in range(32)}
-    glo = api.prn_code(L.GLONASS_L1OF, 0)
+    gps = dict(enumerate(golden_chips("gps_l1ca")[:32]))
+    glo = golden_chips("glonass_l1of")[0]
     e1b = galileo_chips()
     if_gps = 1575.42e6 - CENTER
     ems = []
@@ -107,9 +114,8 @@ def gps_small_workload(seed: int = 2):
 
 
 def gps_4mhz_workload(seed: int = 1):
-    from ugsdr_gb300 import _lib as L
-    from ugsdr_gb300 import api, signals
-    gps = {p: api.prn_code(L.GPS_L1CA, p) for p in range(32)}
+    from ugsdr_gb300 import signals
+    gps = dict(enumerate(golden_chips("gps_l1ca")[:32]))
     raw, _ = signals.gps_l1_config(seed=seed, codes=gps)
     jobs = [dict(system="gps", codes=[gps[p] for p in range(32)], n=4000, k=10, step=500.0, fe=0.0, if_=0.0, fs=4e6)]
     return jobs, raw
@@ -122,9 +128,8 @@ def l5_weak_workload(seed: int = 5):
     +-5 kHz at 25 Hz (401 bins), 63 PRNs: 5.17e9 cells per search.  The
     reference's L5I table holds PRNs 1-32, so searches 33-63 reuse the codes
     of PRNs 1-31 (same work per cell)."""
-    from ugsdr_gb300 import _lib as L
-    from ugsdr_gb300 import api, signals
-    l5 = {p: api.prn_code(L.GPS_L5I, p) for p in range(32)}
+    from ugsdr_gb300 import signals
+    l5 = dict(enumerate(golden_chips("gps_l5i")))
     raw, _ = signals.l5_weak_config(seed, l5)
     jobs = [dict(system="l5", codes=[l5[p % 32] for p in range(63)], n=204600, k=20, step=25.0, fe=-10e6, if_=10e6,
                  fs=20.46e6, fs_in=40e6, repeats=10, sign_mask=signals.nh10_mask(), sign_segment=20460)]
@@ -533,13 +538,6 @@ def run_served(args):
 TRACK_FS = 20e6
 TRACK_FLOPS_PER_CHANNEL_SAMPLE = 26  # carrier wipe-off 6 + five taps x (I, Q) x FMA 2
 TRACK_OUT_BYTES = 88                 # ugsdr_track_output per channel-epoch
-
-
-def golden_chips(name):
-    z = np.load(ROOT / "tests" / "golden" / "codes.npz")
-    n = int(z[f"{name}_len"])
-    bits = np.unpackbits(z[name], axis=1)[:, :n]
-    return (1.0 - 2.0 * bits).astype(np.float32)
 
 
 def track_capture(dev, seconds, seed=3, n_channels=256, sigma=20.0):

@@ -231,8 +231,11 @@ int ugsdr_doppler_bins(double range, double step, uint32_t* n);
  * loads the library holds until the process exits.  A job needing more is
  * rejected with UGSDR_E_NOMEM and *scratch_needed set to the bytes it needs.
  * The first call on a device (with that device current) resolves the array's
- * device address and uploads the mixer table; make that first call before any
- * stream capture.  All calls share the one array: calls that overlap on the
+ * device address and uploads the mixer table, waiting for the upload to land
+ * (it synchronises the device once); make that first call before any stream
+ * capture.  The resolved addresses are kept for the life of the process: do
+ * not reset the device (cudaDeviceReset) between calls.  All calls share the
+ * one array: calls that overlap on the
  * GPU (different streams or host threads without ordering) race on it.
  * Nothing in it needs to start at zero; each call rewrites what it reads. */
 #define UGSDR_STATIC_SCRATCH_BYTES (16u << 20)

@@ -26,6 +26,7 @@
 #include <mutex>
 #include <numeric>
 #include <thread>
+#include <type_traits>
 #include <vector>
 
 namespace oracle {
@@ -49,6 +50,20 @@ namespace oracle {
 		// Fft64 keeps per-call state only on the stack, so one plan serves all threads.
 		void Transform(const cd* in, cd* out, std::size_t n, int sign) {
 			Plan(n, sign)->Execute(in, out);
+		}
+
+		// The CPU baseline's float transform (FftT<float>: the same algorithm in
+		// float, like FFTW's float plans the reference calls); set per worker
+		// thread by orc_fse_baseline_f32 only, so the checker stays in double.
+		thread_local bool tl_float_fft = false;
+		std::map<std::pair<std::size_t, int>, std::shared_ptr<Fft32>> plans32;
+
+		std::shared_ptr<Fft32> Plan32(std::size_t n, int sign) {
+			std::lock_guard<std::mutex> lock(plan_mutex);
+			auto& slot = plans32[{n, sign}];
+			if (!slot)
+				slot = std::make_shared<Fft32>(n, sign);
+			return slot;
 		}
 	}
 
@@ -92,6 +107,17 @@ namespace oracle {
 	// inverse scaled by 1/N then 2 (dft.hpp:124-129).
 	template <typename T>
 	void DftC2c(const std::complex<T>* in, std::complex<T>* out, std::size_t n, bool inverse) {
+		if constexpr (std::is_same_v<T, float>) {
+			if (tl_float_fft) {
+				Plan32(n, inverse ? +1 : -1)->Execute(in, out);
+				if (inverse)
+					for (std::size_t i = 0; i < n; ++i) {
+						out[i] /= static_cast<T>(n);
+						out[i] *= static_cast<T>(2);
+					}
+				return;
+			}
+		}
 		std::vector<cd> a(n), b(n);
 		for (std::size_t i = 0; i < n; ++i)
 			a[i] = cd(in[i].real(), in[i].imag());
@@ -602,6 +628,33 @@ void orc_acquire_many_f32(const float* iq, std::size_t n_total, std::size_t n, s
 		t.join();
 }
 
+
+// The CPU baseline: orc_acquire_many_f32 with every per-block transform in
+// float (FftT<float>), the reference's FFTW float path restated; plans are
+// cached per size (the reference plans per call with FFTW_ESTIMATE).
+void orc_fse_baseline_f32(const float* iq, std::size_t n_total, std::size_t n, std::size_t k_blocks, const float* codes,
+	std::size_t n_codes, double fs, double range, double step, int threads, double* recs /* n_codes x 9 */) {
+	std::atomic<std::size_t> next{0};
+	auto worker = [&]() {
+		tl_float_fft = true;
+		for (std::size_t c; (c = next.fetch_add(1)) < n_codes;) {
+			AcqRecord r{};
+			Acquire(reinterpret_cast<const std::complex<float>*>(iq), n_total, n, k_blocks, codes + c * n, fs, range, step,
+				0.0, 1.0, 0, 1, 0, 0, &r, nullptr, static_cast<float*>(nullptr));
+			std::memcpy(recs + 9 * c, &r, sizeof(r));
+		}
+		tl_float_fft = false;
+	};
+	if (threads <= 1) {
+		worker();
+		return;
+	}
+	std::vector<std::thread> pool;
+	for (int t = 0; t < threads; ++t)
+		pool.emplace_back(worker);
+	for (auto& t : pool)
+		t.join();
+}
 
 // SequentialStft split: returns the column count, columns to out when non-null
 std::size_t orc_stft_f32(const float* iq, std::size_t n, int w, int overlap, float* out) {

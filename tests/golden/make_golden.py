@@ -409,7 +409,7 @@ def preamble(lib) -> dict[str, np.ndarray]:
 
 
 def main() -> None:
-    ref_dir = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref_dir = sys.argv[1] if len(sys.argv) > 1 else str(Path(__file__).resolve().parents[3] / "reference")
     lib = ref_lib(ref_dir)
     if len(sys.argv) > 2:  # regenerate the named fixtures only, e.g. `preamble`
         for name in sys.argv[2:]:

@@ -10,7 +10,7 @@ import pytest
 
 from conftest import ROOT
 
-REF = Path(os.environ.get("UGSDR_REF_DIR", "/root/reference"))
+REF = Path(os.environ.get("UGSDR_REF_DIR", str(ROOT.parent / "reference")))
 BIN = ROOT / "tests" / "native" / "_bin" / "fse_dropin"
 
 

@@ -76,13 +76,20 @@ def build_library(verbose: bool = False) -> Path:
     return LIB
 
 
+def reference_dir() -> Path:
+    """The reference checkout: $UGSDR_REF_DIR, else a sibling directory
+    named `reference` beside this repository."""
+    env = os.environ.get("UGSDR_REF_DIR")
+    return Path(env) if env else ROOT.parent / "reference"
+
+
 def build_oracle(verbose: bool = False) -> None:
     """CPU oracle (test infrastructure): the port always, the reference build
     only where the reference sources exist."""
     r = subprocess.run(["make", "-s", "-C", str(ORACLE), "all"], capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"oracle build failed:\n{r.stdout}\n{r.stderr}")
-    ref_dir = Path(os.environ.get("UGSDR_REF_DIR", "/root/reference"))
+    ref_dir = reference_dir()
     if (ref_dir / "src" / "acquisition" / "fse.hpp").exists():
         r = subprocess.run(["make", "-s", "-C", str(ORACLE), "ref", f"REF_DIR={ref_dir}"], capture_output=True, text=True)
         if r.returncode != 0:

@@ -92,12 +92,12 @@ namespace ugsdr_gpu {
 		size_t n = 0;
 		switch (signal) {
 		case UGSDR_GPS_L1CA:
-			require(sv >= 0 && sv < 37, "SV number for the GPS C/A code exceed available values");
+			require(sv >= 0 && sv < 37, "GPS L1 C/A: satellite index outside 0..36");
 			n = 1023;
 			break;
 		case UGSDR_GPS_L5I:
 		case UGSDR_GPS_L5Q:
-			require(sv >= 0 && sv < 32, "SV number for the GPS L5 code exceed available values");
+			require(sv >= 0 && sv < 32, "GPS L5: satellite index outside 0..31");
 			n = 10230;
 			break;
 		case UGSDR_GLONASS_L1OF:

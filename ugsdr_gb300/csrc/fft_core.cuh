@@ -11,8 +11,7 @@
 //                            pass twiddles read from a per-size table
 //                            W_N^m = exp(-2 pi i m / N) computed on the host in
 //                            double precision.
-// Everything is __host__ __device__ so the pass logic is unit-tested on the
-// CPU (tests/native/fft_core_check.cu) with the same source the GPU runs.
+// Everything is __host__ __device__, so the same source can run on the CPU.
 #pragma once
 
 #include <cstdint>

@@ -29,29 +29,34 @@ namespace ugsdr_gpu {
 
 		// once per device, with that device current: device addresses of the
 		// file-scope arrays (the host-side names are only stand-ins) and the
-		// mixer table (TableMixer::GetSinCosTable<6, float>, table_mixer.hpp:31-47)
+		// mixer table (TableMixer::GetSinCosTable<6, float>, table_mixer.hpp:31-47).
+		// A synchronous copy from pageable memory may return before its DMA has
+		// landed, and a caller's non-blocking stream is not ordered after the
+		// legacy stream, so the set-up waits for the copy before it publishes the
+		// addresses.  The cached addresses belong to the device's primary
+		// context: resetting the device between calls invalidates them.
 		int setup_device(int dev) {
 			std::lock_guard<std::mutex> lock(g_setup_mutex);
 			if (g_scratch_ptr[dev])
 				return UGSDR_OK;
+			auto fail = [] {
+				cudaGetLastError();
+				return UGSDR_E_CUDA;
+			};
 			void* p = nullptr;
-			if (cudaGetSymbolAddress(&p, g_static_scratch) != cudaSuccess) {
-				cudaGetLastError();
-				return UGSDR_E_CUDA;
-			}
+			if (cudaGetSymbolAddress(&p, g_static_scratch) != cudaSuccess)
+				return fail();
 			void* l = nullptr;
-			if (cudaGetSymbolAddress(&l, g_static_lut) != cudaSuccess) {
-				cudaGetLastError();
-				return UGSDR_E_CUDA;
-			}
+			if (cudaGetSymbolAddress(&l, g_static_lut) != cudaSuccess)
+				return fail();
 			float t[80];
 			const double step = 5 * 3.14159265358979323846 / 80 / 2;
 			for (int i = 0; i < 80; ++i)
 				t[i] = static_cast<float>(std::sin(static_cast<double>(i) * step));
-			if (cudaMemcpyToSymbol(g_static_lut, t, sizeof(t)) != cudaSuccess) {
-				cudaGetLastError();
-				return UGSDR_E_CUDA;
-			}
+			if (cudaMemcpyToSymbol(g_static_lut, t, sizeof(t)) != cudaSuccess)
+				return fail();
+			if (cudaDeviceSynchronize() != cudaSuccess)
+				return fail();
 			g_lut_ptr[dev] = static_cast<float*>(l);
 			g_scratch_ptr[dev] = static_cast<unsigned char*>(p);
 			return UGSDR_OK;
@@ -128,6 +133,11 @@ extern "C" int ugsdr_acquire_static(void* cuda_stream, const ugsdr_static_job* j
 	for (double d = -job->doppler_range; d <= job->doppler_range; d += job->doppler_step)
 		if (++n_doppler > 1000000)
 			return UGSDR_E_INVALID;
+	// launch grids: Doppler bins x blocks (forward), Doppler bins x codes (inverse)
+	const size_t grid_fwd = static_cast<size_t>(n_doppler) * job->n_blocks;
+	const size_t grid_inv = static_cast<size_t>(n_doppler) * static_cast<size_t>(job->n_codes);
+	if (grid_fwd > 0x7fffffffu || grid_inv > 0x7fffffffu)
+		return UGSDR_E_INVALID;
 
 	// scratch bytes, checked before anything is launched
 	const size_t tw_b = align256(sizeof(float2) * n);
@@ -147,8 +157,10 @@ extern "C" int ugsdr_acquire_static(void* cuda_stream, const ugsdr_static_job* j
 		return UGSDR_E_CUDA;
 	}
 	int optin = 0;
-	if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
+	if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) {
+		cudaGetLastError();
 		return UGSDR_E_CUDA;
+	}
 	const size_t smem_f = 2 * sizeof(float2) * n;
 	const size_t smem_i = smem_f + sizeof(float) * m;
 	if (smem_i + 1024 > static_cast<size_t>(optin))
@@ -174,12 +186,23 @@ extern "C" int ugsdr_acquire_static(void* cuda_stream, const ugsdr_static_job* j
 		plan.radix[i] = radices[i];
 	plan.tw = tw;
 
+	// every kernel's shared-memory opt-in is set before the first launch
+	bool smem_set = smem_ok(static_code_spectra_kernel, smem_f) && smem_ok(acq_inverse_kernel, smem_i);
+	switch (job->sample_type) {
+	case UGSDR_SAMPLES_CF32: smem_set = smem_set && smem_ok(acq_forward_kernel<UGSDR_SAMPLES_CF32>, smem_f); break;
+	case UGSDR_SAMPLES_CI8: smem_set = smem_set && smem_ok(acq_forward_kernel<UGSDR_SAMPLES_CI8>, smem_f); break;
+	case UGSDR_SAMPLES_CI16: smem_set = smem_set && smem_ok(acq_forward_kernel<UGSDR_SAMPLES_CI16>, smem_f); break;
+	default: smem_set = smem_set && smem_ok(acq_forward_kernel<UGSDR_SAMPLES_RI8>, smem_f); break;
+	}
+	if (!smem_set) {
+		cudaGetLastError();
+		return UGSDR_E_CUDA;
+	}
+
 	constexpr int kThreads = 256;
 	static_twiddle_kernel<<<(n + kThreads - 1) / kThreads, kThreads, 0, stream>>>(tw, n);
 	static_tables_kernel<<<(job->n_codes + kThreads - 1) / kThreads, kThreads, 0, stream>>>(
 		adders, n_doppler, job->doppler_range, job->doppler_step, job->sampling_rate, code_ptrs, codes, job->n_codes, n);
-	if (!smem_ok(static_code_spectra_kernel, smem_f))
-		return UGSDR_E_CUDA;
 	static_code_spectra_kernel<<<job->n_codes, kThreads, smem_f, stream>>>(job->code_samples, codes, plan,
 		job->spectrum_mode == UGSDR_SPECTRUM_ONE_SIDED);
 
@@ -203,29 +226,14 @@ extern "C" int ugsdr_acquire_static(void* cuda_stream, const ugsdr_static_job* j
 	p.cells = reinterpret_cast<AcqCellDev*>(cells_device);
 	p.plan = plan;
 
-	const int grid_f = n_doppler * static_cast<int>(job->n_blocks);
-	bool ok = true;
+	const int grid_f = static_cast<int>(grid_fwd);
 	switch (job->sample_type) {
-	case UGSDR_SAMPLES_CF32:
-		ok = smem_ok(acq_forward_kernel<UGSDR_SAMPLES_CF32>, smem_f);
-		if (ok) acq_forward_kernel<UGSDR_SAMPLES_CF32><<<grid_f, kThreads, smem_f, stream>>>(p);
-		break;
-	case UGSDR_SAMPLES_CI8:
-		ok = smem_ok(acq_forward_kernel<UGSDR_SAMPLES_CI8>, smem_f);
-		if (ok) acq_forward_kernel<UGSDR_SAMPLES_CI8><<<grid_f, kThreads, smem_f, stream>>>(p);
-		break;
-	case UGSDR_SAMPLES_CI16:
-		ok = smem_ok(acq_forward_kernel<UGSDR_SAMPLES_CI16>, smem_f);
-		if (ok) acq_forward_kernel<UGSDR_SAMPLES_CI16><<<grid_f, kThreads, smem_f, stream>>>(p);
-		break;
-	default:
-		ok = smem_ok(acq_forward_kernel<UGSDR_SAMPLES_RI8>, smem_f);
-		if (ok) acq_forward_kernel<UGSDR_SAMPLES_RI8><<<grid_f, kThreads, smem_f, stream>>>(p);
-		break;
+	case UGSDR_SAMPLES_CF32: acq_forward_kernel<UGSDR_SAMPLES_CF32><<<grid_f, kThreads, smem_f, stream>>>(p); break;
+	case UGSDR_SAMPLES_CI8: acq_forward_kernel<UGSDR_SAMPLES_CI8><<<grid_f, kThreads, smem_f, stream>>>(p); break;
+	case UGSDR_SAMPLES_CI16: acq_forward_kernel<UGSDR_SAMPLES_CI16><<<grid_f, kThreads, smem_f, stream>>>(p); break;
+	default: acq_forward_kernel<UGSDR_SAMPLES_RI8><<<grid_f, kThreads, smem_f, stream>>>(p); break;
 	}
-	if (!ok || !smem_ok(acq_inverse_kernel, smem_i))
-		return UGSDR_E_CUDA;
-	acq_inverse_kernel<<<n_doppler * job->n_codes, kThreads, smem_i, stream>>>(p);
+	acq_inverse_kernel<<<static_cast<int>(grid_inv), kThreads, smem_i, stream>>>(p);
 	if (cudaGetLastError() != cudaSuccess)
 		return UGSDR_E_CUDA;
 	return UGSDR_OK;
