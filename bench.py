@@ -71,24 +71,29 @@ def multi_workload(seed: int = 2):
     glo = golden_chips("glonass_l1of")[0]
     e1b = galileo_chips()
     if_gps = 1575.42e6 - CENTER
-    ems = []
+    ems, planted = [], {"gps": {}, "glo": {}, "gal": {}}  # code index -> (code phase in chips, residual Doppler)
     for p in rng.choice(32, 8, replace=False):
-        ems.append(signals.Emitter(gps[int(p)], 1.023e6, rng.uniform(0, 1023), if_gps + rng.uniform(-4500, 4500),
-                                   rng.uniform(38, 48), 50.0, rng.uniform(0, 6.28)))
+        ph, dop = rng.uniform(0, 1023), rng.uniform(-4500, 4500)
+        ems.append(signals.Emitter(gps[int(p)], 1.023e6, ph, if_gps + dop, rng.uniform(38, 48), 50.0, rng.uniform(0, 6.28)))
+        planted["gps"][int(p)] = (ph, dop)
     for k in rng.choice(np.arange(-7, 7), 8, replace=False):
         f_if = 1602e6 + int(k) * 0.5625e6 - CENTER
-        ems.append(signals.Emitter(glo, 0.511e6, rng.uniform(0, 511), f_if + rng.uniform(-4500, 4500),
-                                   rng.uniform(38, 48), 50.0, rng.uniform(0, 6.28)))
+        ph, dop = rng.uniform(0, 511), rng.uniform(-4500, 4500)
+        ems.append(signals.Emitter(glo, 0.511e6, ph, f_if + dop, rng.uniform(38, 48), 50.0, rng.uniform(0, 6.28)))
+        planted["glo"][int(k)] = (ph, dop)
     for p in rng.choice(36, 8, replace=False):
-        ems.append(signals.Emitter(e1b[int(p)], 2.046e6,
-                                   rng.uniform(0, 8184), if_gps + rng.uniform(-4500, 4500), rng.uniform(38, 48), 250.0,
-                                   rng.uniform(0, 6.28)))
+        ph, dop = rng.uniform(0, 8184), rng.uniform(-4500, 4500)
+        ems.append(signals.Emitter(e1b[int(p)], 2.046e6, ph, if_gps + dop, rng.uniform(38, 48), 250.0, rng.uniform(0, 6.28)))
+        planted["gal"][int(p)] = (ph, dop)
     raw = signals.synthesize(ems, FS, int(FS * 0.040), SIGMA, "ci16", seed + 100)
-    jobs = [dict(system="gps", codes=[gps[p] for p in range(32)], n=50000, k=40, step=250.0, fe=-if_gps, if_=if_gps)]
+    jobs = [dict(system="gps", codes=[gps[p] for p in range(32)], n=50000, k=40, step=250.0, fe=-if_gps, if_=if_gps,
+                 planted=planted["gps"], chip_rate=1.023e6)]
     for k in range(-7, 7):
         f_if = 1602e6 + k * 0.5625e6 - CENTER
-        jobs.append(dict(system="glo", codes=[glo], n=50000, k=40, step=250.0, fe=-f_if, if_=f_if))
-    jobs.append(dict(system="gal", codes=[e1b[p] for p in range(36)], n=200000, k=10, step=62.5, fe=-if_gps, if_=if_gps))
+        jobs.append(dict(system="glo", codes=[glo], n=50000, k=40, step=250.0, fe=-f_if, if_=f_if, letter=k,
+                         planted={0: planted["glo"][k]} if k in planted["glo"] else {}, chip_rate=0.511e6))
+    jobs.append(dict(system="gal", codes=[e1b[p] for p in range(36)], n=200000, k=10, step=62.5, fe=-if_gps, if_=if_gps,
+                     planted=planted["gal"], chip_rate=2.046e6))
     return jobs, raw
 
 
@@ -1081,67 +1086,128 @@ def run_observables(args, world, rank):
 
 
 # ------------------------------------------------------------ CPU reference
-def cpu_baseline(args, jobs, raw, fs, budget_s: float = 20.0):
-    """Bounded sample of the same workload on the host cores through the CPU
-    restatement of the reference loop (oracle/): for each system, as many
-    codes as threads, 1 Doppler bin, the full K blocks; per-cell time scaled
-    to the whole step."""
+CPU_FFT_NOTE = ("float transforms by the project's iterative Stockham FFT (oracle/fft64.hpp FftT<float>, plans "
+                "cached per size); FFTW is absent here and on the GPU box, so the reference's FFTW build is not timed")
+
+
+def cpu_sample(jobs, raw, fs, threads, codes_per_system=None):
+    """One bounded sample of the workload on the host cores through the CPU
+    restatement of the reference loop (oracle/, ProcessBpsk with per-code,
+    per-Doppler re-mix and two transforms per block): for each system, as
+    many codes as threads (or `codes_per_system`), 1 Doppler bin, the full K
+    blocks (front-end jobs: 4 blocks, the front end timed on the same
+    prefix).  Returns the seconds it took, the cells it searched and the
+    per-cell rate scaled to the whole step."""
     sys.path.insert(0, str(ROOT / "oracle"))
     import pyoracle
-    threads = os.cpu_count() or 1
     x = raw.astype(np.float32)
     x = (x[:, 0] + 1j * x[:, 1]).astype(np.complex64) if raw.ndim == 2 else x.astype(np.complex64)
-    total_t, sample_desc = 0.0, []
-    seen = {}
+    step_t, sample_t, sample_cells, desc = 0.0, 0.0, 0, []
+    per_cell = {}
+    t_start = time.perf_counter()
     for j in jobs:
         key = (j["system"], j["n"], j["k"])
         fs_in = j.get("fs_in", 0.0)
-        # front-end jobs: 4 blocks timed and scaled to K (the oracle resampler
-        # walks every upsampled index, 1023 per input at 40 -> 20.46 MHz)
         ks = min(j["k"], 4) if fs_in else j["k"]
+        t0 = time.perf_counter()
         if fs_in:
             need = int(np.ceil(j["n"] * ks * fs_in / fs)) + 2
-            t0 = time.perf_counter()
             xx = pyoracle.table_mix(x[:need], fs_in, j["fe"]) if j["fe"] else x[:need]
             xx = pyoracle.resample(xx, int(fs), int(fs_in))[: j["n"] * ks]
-            total_t += (time.perf_counter() - t0) * j["k"] / ks  # once per job
         else:
             xx = pyoracle.table_mix(x[: j["n"] * j["k"]], fs, j["fe"]) if j["fe"] else x[: j["n"] * j["k"]]
-        if key not in seen:
-            ncodes = min(len(j["codes"]), threads)
+        t_front = (time.perf_counter() - t0) * j["k"] / ks  # once per job, scaled to K
+        step_t += t_front
+        if key not in per_cell:
+            ncodes = min(len(j["codes"]), codes_per_system or threads)
             codes = np.stack([oracle_code(pyoracle, j, c) for c in j["codes"][:ncodes]])
             t0 = time.perf_counter()
-            pyoracle.acquire_many(xx, j["n"], ks, codes, fs, 0.0, 1.0, threads=threads)
+            pyoracle.fse_baseline(xx, j["n"], ks, codes, fs, 0.0, 1.0, threads=threads)
             dt = time.perf_counter() - t0
-            seen[key] = dt / (ncodes * j["n"]) * j["k"] / ks  # seconds per cell
-            sample_desc.append(f"{j['system']}: {ncodes} codes x 1 Doppler x {j['n']} x {ks} blocks in {dt:.2f}s"
-                               + (f" (scaled to {j['k']} blocks; front end timed on the same prefix)" if ks != j["k"] else ""))
-        total_t += seen[key] * job_cells(j)
+            per_cell[key] = dt / (ncodes * j["n"]) * j["k"] / ks
+            sample_cells += ncodes * j["n"]
+            desc.append(f"{j['system']}: {ncodes} codes x 1 Doppler x {j['n']} x {ks} blocks in {dt:.2f} s"
+                        + (f" (scaled to {j['k']} blocks)" if ks != j["k"] else ""))
+        step_t += per_cell[key] * job_cells(j)
+    sample_t = time.perf_counter() - t_start
     cells = sum(job_cells(j) for j in jobs)
-    return {"value": cells / total_t, "unit": "cells/s", "cores": threads, "kind": "port",
-            "sample": "; ".join(sample_desc) + " -> per-cell time x cells of the full step (project FFT, not FFTW)",
-            "ms_per_step_extrapolated": total_t * 1e3}
+    return {"value": cells / step_t, "sample_seconds": sample_t, "sample_cells": sample_cells,
+            "full_step_seconds_extrapolated": step_t, "sample": "; ".join(desc)}
+
+
+def cpu_anchor_gps_4mhz(threads):
+    """The full-size GPS L1 C/A 4 MHz search (32 PRN x 21 Doppler x 4000 x 10,
+    int8), timed whole on the host cores: no extrapolation."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import pyoracle
+    jobs, raw = gps_4mhz_workload()
+    j = jobs[0]
+    x = raw.astype(np.float32)
+    x = (x[:, 0] + 1j * x[:, 1]).astype(np.complex64)
+    codes = np.stack([oracle_code(pyoracle, j, c) for c in j["codes"]])
+    t0 = time.perf_counter()
+    pyoracle.fse_baseline(x[: j["n"] * j["k"]], j["n"], j["k"], codes, j["fs"], 5000.0, j["step"], threads=threads)
+    dt = time.perf_counter() - t0
+    cells = job_cells(j)
+    return {"workload": WORKLOAD_DESC["gps_l1_4mhz"], "seconds": dt, "cells": cells, "value": cells / dt,
+            "unit": "cells/s", "cores": threads, "extrapolated": False}
+
+
+def repo_libraries():
+    """Shared objects of this repository mapped into this process."""
+    try:
+        maps = Path("/proc/self/maps").read_text().splitlines()
+    except OSError:
+        return []
+    return sorted({l.split()[-1] for l in maps if l.endswith(".so") and str(ROOT) in l})
+
+
+def cpu_baseline(args, jobs, raw, fs):
+    """The ours-arm line's cpu_baseline: one sample on all host threads."""
+    threads = os.cpu_count() or 1
+    b = cpu_sample(jobs, raw, fs, threads)
+    return {"value": b["value"], "unit": "cells/s", "cores": threads, "kind": "port", "extrapolated": True,
+            "sample": b["sample"] + f" ({b['sample_seconds']:.2f} s wall) -> per-cell time x cells of the full step; "
+                      + CPU_FFT_NOTE,
+            "ms_per_step_extrapolated": b["full_step_seconds_extrapolated"] * 1e3}
 
 
 def run_reference(args, world, rank):
+    """The reference path on the host cores: each step is one bounded sample
+    of the workload (cpu_sample) on all host threads; `value` is the per-cell
+    rate of the samples scaled to the workload's cells, `ms_per_step` the
+    measured wall time of one sample step.  Also in the line: the same sample
+    on one thread (the reference as written: par_unseq runs serially in
+    libstdc++ without TBB) and the full-size 4 MHz search timed whole."""
     if rank != 0:
         return None
     jobs, raw = WORKLOADS[args.config]()
     fs = jobs[0].get("fs", FS)
-    vals = []
-    for _ in range(args.warmup + args.steps):
-        vals.append(cpu_baseline(args, jobs, raw, fs))
-    vals = vals[args.warmup:]
-    v = float(np.mean([b["value"] for b in vals]))
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_sample(jobs, raw, fs, threads)
+    vals = [cpu_sample(jobs, raw, fs, threads) for _ in range(args.steps)]
+    v = float(np.median([b["value"] for b in vals]))
+    ms = float(np.median([b["sample_seconds"] for b in vals])) * 1e3
+    one = cpu_sample(jobs, raw, fs, 1, codes_per_system=1)
     cells = sum(job_cells(j) for j in jobs)
     b = vals[-1]
     return {
         "metric": "acq cells/s (PRN x Doppler x code-phase)", "value": v, "unit": "cells/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": cells / v * 1e3, "higher_is_better": True,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
-        "config": {"workload": "same as --impl ours", "cells_per_step": cells},
-        "cpu_baseline": {"value": v, "unit": "cells/s", "cores": b["cores"], "kind": "port", "sample": b["sample"]},
+        "config": {"workload": WORKLOAD_DESC.get(args.config, args.config), "cells_per_step": cells,
+                   "step": "one bounded sample of the workload (1 Doppler bin per code, see cpu_baseline.sample); "
+                           "value = its per-cell rate x the workload's cells (extrapolated)",
+                   "sample_cells_per_step": b["sample_cells"]},
+        "cpu_baseline": {"value": v, "unit": "cells/s", "cores": threads, "kind": "port", "extrapolated": True,
+                         "sample": b["sample"] + "; " + CPU_FFT_NOTE,
+                         "ms_per_full_step_extrapolated": cells / v * 1e3},
+        "single_thread": {"value": one["value"], "unit": "cells/s", "cores": 1, "extrapolated": True,
+                          "sample_seconds": one["sample_seconds"], "sample": one["sample"]},
+        "anchor_full_search": cpu_anchor_gps_4mhz(threads),
         "e2e": {"value": v, "unit": "cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "libraries_loaded": [str(Path(x).relative_to(ROOT)) for x in repo_libraries()],
     }
 
 

@@ -48,6 +48,7 @@ def load() -> C.CDLL:
         "orc_acquire_f32": [vp, sz, sz, sz, vp, d, d, d, d, d, i, i, i, i, vp, vp, vp],
         "orc_acquire_f64": [vp, sz, sz, sz, vp, d, d, d, d, d, i, i, i, i, vp, vp, vp],
         "orc_acquire_many_f32": [vp, sz, sz, sz, vp, sz, d, d, d, d, d, i, i, i, i, i, vp],
+        "orc_fse_baseline_f32": [vp, sz, sz, sz, vp, sz, d, d, d, i, vp],
         "orc_stft_f32": [vp, sz, i, i, vp],
         "orc_istft_f32": [vp, sz, i, i, vp],
         "orc_jamming_process_f32": [vp, sz, d, i, vp, vp, vp, vp, i],
@@ -113,6 +114,17 @@ def acquire_many(iq_complex: np.ndarray, n: int, k_blocks: int, codes: np.ndarra
     recs = np.zeros((c.shape[0], 9))
     lib.orc_acquire_many_f32(_p(x), x.size, n, k_blocks, _p(c), c.shape[0], fs, range_hz, step_hz, 0.0, 1.0,
                              1 if reshape else 0, 1 if coherent else 0, stat, spectrum_mode, threads, _p(recs))
+    return recs
+
+
+def fse_baseline(iq_complex: np.ndarray, n: int, k_blocks: int, codes: np.ndarray, fs: float, range_hz: float,
+                 step_hz: float, threads: int = 1) -> np.ndarray:
+    """The CPU baseline: acquire_many with float transforms (FftT<float>)."""
+    lib = load()
+    x = np.ascontiguousarray(iq_complex, np.complex64)
+    c = np.ascontiguousarray(codes, np.float32)
+    recs = np.zeros((c.shape[0], 9))
+    lib.orc_fse_baseline_f32(_p(x), x.size, n, k_blocks, _p(c), c.shape[0], fs, range_hz, step_hz, threads, _p(recs))
     return recs
 
 

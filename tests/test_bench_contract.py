@@ -24,3 +24,7 @@ def test_reference_arm_line(config, unit):
     assert d["impl"] == "reference" and d["unit"] == unit and d["value"] > 0
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
+    if config == "gps_l1_4mhz":
+        # the reference arm runs the oracle only, never the product library
+        assert d["libraries_loaded"] and not any("libugsdr_cuda" in x for x in d["libraries_loaded"])
+        assert d["anchor_full_search"]["extrapolated"] is False and d["single_thread"]["cores"] == 1
