@@ -122,8 +122,10 @@ int ugsdr_ctx_reset_timing(ugsdr_ctx* ctx);
  * +-1 chips of `sv` (0-based id, as the reference) into out[0..cap).  *len
  * receives the code length even when cap is too small (then UGSDR_E_INVALID).
  * LFSR codes (GPS L1 C/A PRN 1-37, L5I/L5Q PRN 1-32, GLONASS L1OF/L2OF) are
- * generated here; memory codes (Galileo E1B/E1C) return UGSDR_E_UNSUPPORTED:
- * pass their chips to ugsdr_code_put directly. */
+ * generated here; the Galileo E1B/E1C memory codes (sv 0-49, the ICD's
+ * tables built into the library) come as 8,184 sine-BOC(1,1) half-chips
+ * [c, -c] per chip, as MemoryCodes::DecodeBoc returns them
+ * (src/prn_codes/MemoryCodes.hpp:33-40). */
 int ugsdr_prn_code(int signal, int sv, float* out, size_t cap, size_t* len);
 
 /* RepeatCodeNTimes + Upsampler::Transform (src/common.hpp:78-85,

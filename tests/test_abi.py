@@ -32,7 +32,8 @@ def test_abi_version(lib):
 
 
 @pytest.mark.parametrize("name,signal,count", [("gps_l1ca", L.GPS_L1CA, 37), ("gps_l5i", L.GPS_L5I, 32),
-                                               ("gps_l5q", L.GPS_L5Q, 32), ("glonass_l1of", L.GLONASS_L1OF, 1)])
+                                               ("gps_l5q", L.GPS_L5Q, 32), ("glonass_l1of", L.GLONASS_L1OF, 1),
+                                               ("galileo_e1b", L.GALILEO_E1B, 50), ("galileo_e1c", L.GALILEO_E1C, 50)])
 def test_prn_codes_bit_exact(golden_codes, name, signal, count):
     ref = unpack_codes(golden_codes, name)
     assert ref.shape[0] == count
@@ -46,7 +47,10 @@ def test_prn_code_errors(lib):
     # GPS C/A has 37 ids (GpsL1Ca.hpp:22-23 throws beyond)
     assert lib.ugsdr_prn_code(L.GPS_L1CA, 37, buf.ctypes.data, buf.size, C.byref(n)) == L.E_INVALID
     assert lib.ugsdr_prn_code(L.GPS_L5I, 32, buf.ctypes.data, buf.size, C.byref(n)) == L.E_INVALID
-    assert lib.ugsdr_prn_code(L.GALILEO_E1B, 0, buf.ctypes.data, buf.size, C.byref(n)) == L.E_UNSUPPORTED
+    assert lib.ugsdr_prn_code(L.GALILEO_E1B, 50, buf.ctypes.data, buf.size, C.byref(n)) == L.E_INVALID
+    assert lib.ugsdr_prn_code(L.GALILEO_E1C, 0, buf.ctypes.data, buf.size, C.byref(n)) == L.E_INVALID
+    assert n.value == 8184
+    assert lib.ugsdr_prn_code(L.GPS_L2CM, 0, buf.ctypes.data, buf.size, C.byref(n)) == L.E_UNSUPPORTED
     # too small a buffer reports the length
     assert lib.ugsdr_prn_code(L.GPS_L1CA, 0, buf.ctypes.data, 10, C.byref(n)) == L.E_INVALID
     assert n.value == 1023

@@ -113,4 +113,4 @@ def test_multi_constellation_batch_vs_oracle(ctx, oracle):
                 assert abs(r.doppler - j["if_"] - dop) <= j["step"], (where, r.doppler, dop)
                 assert r.snr > 1.5, (where, r.snr)
                 found += 1
-    assert found == 2 + 8 + 1
+    assert found == 1 + 8 + 1  # GPS and Galileo: one planted code each; GLONASS: eight planted letters

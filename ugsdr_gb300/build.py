@@ -55,12 +55,27 @@ def _compile(src: Path, obj: Path, stamp: Path, digest: str, verbose: bool) -> N
     stamp.write_text(key)
 
 
+GALILEO_TABLE = PKG / "data" / "galileo_e1_memory_codes.bin"
+
+
+def _table_source(obj_dir: Path) -> Path:
+    """The Galileo E1B/E1C memory-code table as a C++ array (generated)."""
+    src = obj_dir / "galileo_table.cpp"
+    data = GALILEO_TABLE.read_bytes()
+    body = ",".join(str(b) for b in data)
+    text = ("// generated by ugsdr_gb300/build.py from data/galileo_e1_memory_codes.bin\n"
+            f"extern const unsigned char ugsdr_galileo_e1_table[{len(data)}] = {{{body}}};\n")
+    if not src.exists() or src.read_text() != text:
+        src.write_text(text)
+    return src
+
+
 def build_library(verbose: bool = False) -> Path:
     OUT_DIR.mkdir(exist_ok=True)
     obj_dir = OUT_DIR / "obj"
     obj_dir.mkdir(exist_ok=True)
     digest = _headers_digest()
-    sources = [CSRC / s for s in SOURCES if (CSRC / s).exists()]
+    sources = [CSRC / s for s in SOURCES if (CSRC / s).exists()] + [_table_source(obj_dir)]
     objs = [obj_dir / (s.name + ".o") for s in sources]
     with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
         futs = [ex.submit(_compile, s, o, o.with_suffix(".stamp"), digest, verbose) for s, o in zip(sources, objs)]

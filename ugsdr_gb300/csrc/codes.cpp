@@ -7,13 +7,17 @@
 //   GPS L5I/Q   XA (short-cycled at 8190 chips) xor XB advanced per PRN
 //               (L5.hpp:25-43, GpsL5I.hpp:9-21, GpsL5Q.hpp:9-21; IS-GPS-705 table 3-1)
 //   GLONASS     511-chip m-sequence x^9 + x^5 + 1, output of stage 7 (GlonassOf.hpp:25-36)
-// The delay/advance tables are ICD data and therefore identical to the
-// reference's.  Chips are +-1 with bit b -> 1 - 2b, as the reference emits.
+//   Galileo E1B/E1C  memory codes (Galileo OS SIS ICD tables, the reference's
+//               GalileoMemoryCodes.cpp) embedded from data/, BOC(1,1) expanded
+// The delay/advance tables and memory codes are ICD data and therefore
+// identical to the reference's.  Chips are +-1 with bit b -> 1 - 2b, as the reference emits.
 #include "internal.hpp"
 
 #include <array>
 #include <cmath>
 #include <cstring>
+
+extern const unsigned char ugsdr_galileo_e1_table[51200];
 
 namespace ugsdr_gpu {
 	namespace {
@@ -82,6 +86,19 @@ namespace ugsdr_gpu {
 			write_chips(c, out);
 		}
 
+		// Galileo E1B / E1C: the ICD's memory codes (table data, embedded from
+		// data/galileo_e1_memory_codes.bin: 4,092 chips per code, bit 1 = -1)
+		// as sine-BOC(1,1) half-chips [c, -c] per chip, the form
+		// MemoryCodes::DecodeBoc returns (src/prn_codes/MemoryCodes.hpp:33-40).
+		void galileo_e1(int sv, bool pilot, float* out) {
+			const unsigned char* code = ugsdr_galileo_e1_table + (pilot ? 50 : 0) * 512 + static_cast<size_t>(sv) * 512;
+			for (int i = 0; i < 4092; ++i) {
+				const float c = ((code[i >> 3] >> (7 - (i & 7))) & 1) ? -1.0f : 1.0f;
+				out[2 * i] = c;
+				out[2 * i + 1] = -c;
+			}
+		}
+
 		void glonass_of(float* out) {
 			static const std::vector<uint8_t> m = lfsr_sequence(9, {5, 9}, 7, 511);
 			write_chips(m, out);
@@ -106,7 +123,9 @@ namespace ugsdr_gpu {
 			break;
 		case UGSDR_GALILEO_E1B:
 		case UGSDR_GALILEO_E1C:
-			throw Error(UGSDR_E_UNSUPPORTED, "Galileo memory codes are table data: pass their chips to ugsdr_code_put");
+			require(sv >= 0 && sv < 50, "Galileo E1: satellite index outside 0..49");
+			n = 2 * 4092;
+			break;
 		default:
 			throw Error(UGSDR_E_UNSUPPORTED, "signal not generated by this library");
 		}
@@ -117,6 +136,8 @@ namespace ugsdr_gpu {
 		case UGSDR_GPS_L1CA: gps_ca(sv, out); break;
 		case UGSDR_GPS_L5I: gps_l5(sv, false, out); break;
 		case UGSDR_GPS_L5Q: gps_l5(sv, true, out); break;
+		case UGSDR_GALILEO_E1B: galileo_e1(sv, false, out); break;
+		case UGSDR_GALILEO_E1C: galileo_e1(sv, true, out); break;
 		default: glonass_of(out); break;
 		}
 		return UGSDR_OK;
