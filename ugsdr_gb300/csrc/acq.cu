@@ -4,6 +4,7 @@
 #include "internal.hpp"
 #include "acq_kernels.cuh"
 #include "acq_batched.cuh"
+#include "acq_cols_warp.cuh"
 #include "dfe.cuh"
 #include "fft_plan.hpp"
 
@@ -195,6 +196,30 @@ namespace ugsdr_gpu {
 				rw /= 2;
 		}
 
+		// Column plans of the warp-owned column kernel (unfolded rows): N1 = 400
+		// (200,000-point blocks) and 200 (50,000-point blocks), radix 25 last.
+		using ColsWarp400 = ColsWarpPlan<400, 16, 25, 4, 3>;
+		using ColsWarp200 = ColsWarpPlan<200, 8, 25, 4, 3>;
+		template <class Fn>
+		bool with_cols_warp(int n1, int n2, Fn&& fn) {
+			if (n1 == 400 && n2 == 500)
+				fn(ColsWarp400{});
+			else if (n1 == 200 && n2 == 250)
+				fn(ColsWarp200{});
+			else
+				return false;
+			return true;
+		}
+
+		// columns per column-kernel CTA of the blocked layout (0: natural layout)
+		int blocked_cw(int n1, int n2, int fold_mode) {
+			if (fold_mode != 0 || std::getenv("UGSDR_NO_WARP_COLS"))
+				return 0;
+			int cw = 0;
+			with_cols_warp(n1, n2, [&](auto plan) { cw = decltype(plan)::CW; });
+			return cw;
+		}
+
 		BatchedParams batched_params(ugsdr_ctx* ctx, const AcqParams& base, int n) {
 			const LargePlan& lp = get_large_plan(ctx, n);
 			BatchedParams p{};
@@ -205,6 +230,7 @@ namespace ugsdr_gpu {
 			p.n2 = lp.n2;
 			tile_shape(ctx, lp, p.cw, p.rw);
 			p.ld1 = lp.n1 | 1;  // odd column stride: the 8 columns of a tile fall in distinct banks
+			p.n2p = lp.n2;
 			p.cw_shift = 0;
 			while ((1 << p.cw_shift) < p.cw)
 				++p.cw_shift;
@@ -238,8 +264,8 @@ namespace ugsdr_gpu {
 		// rows per inverse batch: B (rows x K x N complex) within 8 GiB — large
 		// enough that a batch is thousands of CTAs and a search a few hundred
 		// launches at most (the host then never waits on a full launch queue)
-		int batch_rows(const JobLaunchShape& s) {
-			const size_t per_row = sizeof(float2) * static_cast<size_t>(s.n) * s.k;
+		int batch_rows(const JobLaunchShape& s, size_t b_points) {
+			const size_t per_row = sizeof(float2) * b_points * s.k;
 			const size_t budget = static_cast<size_t>(8) << 30;
 			return static_cast<int>(std::max<size_t>(1, std::min<size_t>(s.rows, budget / per_row)));
 		}
@@ -277,14 +303,14 @@ namespace ugsdr_gpu {
 		// walk it, so they agree byte for byte.
 		struct ScratchLayout {
 			size_t bbuf = 0, partials = 0, sums = 0, counters = 0, accg = 0, zcg = 0, total = 0;
-			ScratchLayout(const JobLaunchShape& s, int r_max, int chunks) {
+			ScratchLayout(const JobLaunchShape& s, int r_max, int chunks, size_t b_points) {
 				auto region = [&](size_t bytes) {
 					const size_t at = total;
 					total += (bytes + 255) / 256 * 256;
 					return at;
 				};
 				const size_t r = static_cast<size_t>(r_max);
-				bbuf = region(sizeof(float2) * r * s.k * s.n);
+				bbuf = region(sizeof(float2) * r * s.k * b_points);
 				partials = region(sizeof(float4) * r * chunks);
 				sums = region(sizeof(double2) * r * chunks);
 				counters = region(sizeof(unsigned int) * r);
@@ -297,11 +323,28 @@ namespace ugsdr_gpu {
 		};
 	}
 
+	// B points per (row, block) and column chunks per row of a job shape
+	void inverse_geometry(const BatchedParams& p, int fold_mode, int& cw_blocked, size_t& b_points, int& chunks) {
+		cw_blocked = blocked_cw(p.n1, p.n2, fold_mode);
+		if (cw_blocked) {
+			const int n2p = (p.n2 + cw_blocked - 1) / cw_blocked * cw_blocked;
+			b_points = static_cast<size_t>(p.n1) * n2p;
+			chunks = n2p / cw_blocked;
+		}
+		else {
+			b_points = static_cast<size_t>(p.n1) * p.n2;
+			chunks = chunks_of(p.n2, p.cw);
+		}
+	}
+
 	size_t batched_scratch_bytes(ugsdr_ctx* ctx, const JobLaunchShape& s) {
 		AcqParams base{};
 		base.n = s.n;
 		const BatchedParams p = batched_params(ctx, base, s.n);
-		return ScratchLayout(s, batch_rows(s), chunks_of(p.n2, p.cw)).total;
+		int cwb = 0, chunks = 0;
+		size_t b_points = 0;
+		inverse_geometry(p, s.fold_mode, cwb, b_points, chunks);
+		return ScratchLayout(s, batch_rows(s, b_points), chunks, b_points).total;
 	}
 
 	void large_code_spectrum(ugsdr_ctx* ctx, CodeEntry& e, const float* chips_dev, size_t n_chips, size_t repeats,
@@ -356,9 +399,13 @@ namespace ugsdr_gpu {
 			KernelTimer timer(ctx, "acq_forward_large");
 			launch_forward(ctx, job.sample_type, p, items);
 		}
-		const int r_max = batch_rows(s);
-		const int chunks = chunks_of(p.n2, p.cw);
-		const ScratchLayout lay(s, r_max, chunks);
+		int cw_blocked = 0, chunks = 0;
+		size_t b_points = 0;
+		inverse_geometry(p, s.fold_mode, cw_blocked, b_points, chunks);
+		if (cw_blocked)
+			p.n2p = static_cast<int>(b_points / p.n1);
+		const int r_max = batch_rows(s, b_points);
+		const ScratchLayout lay(s, r_max, chunks, b_points);
 		p.bbuf = reinterpret_cast<float2*>(scratch + lay.bbuf);
 		p.partials = reinterpret_cast<float4*>(scratch + lay.partials);
 		p.sums = reinterpret_cast<double2*>(scratch + lay.sums);
@@ -367,6 +414,48 @@ namespace ugsdr_gpu {
 			p.accg = reinterpret_cast<float*>(scratch + lay.accg);
 			if (s.fold_mode == 2)
 				p.zcg = reinterpret_cast<float2*>(scratch + lay.zcg);
+		}
+		auto run_batches = [&](auto launch_pair) {
+			for (int row0 = 0; row0 < s.rows; row0 += r_max) {
+				p.row0 = row0;
+				p.rows = std::min(r_max, s.rows - row0);
+				UG_CUDA(cudaMemsetAsync(p.counters, 0, sizeof(unsigned int) * p.rows, ctx->stream));
+				if (s.fold_mode) {
+					UG_CUDA(cudaMemsetAsync(p.accg, 0, sizeof(float) * static_cast<size_t>(p.rows) * s.m, ctx->stream));
+					if (s.fold_mode == 2)
+						UG_CUDA(cudaMemsetAsync(p.zcg, 0, sizeof(float2) * static_cast<size_t>(p.rows) * s.k * s.m, ctx->stream));
+				}
+				launch_pair();
+				note_launch(ctx, 2);
+				if (s.fold_mode) {
+					fold_finish_kernel<<<p.rows, kBatchedThreads, 0, ctx->stream>>>(p);
+					note_launch(ctx);
+				}
+			}
+		};
+		if (cw_blocked) {
+			// static row plan + warp-owned columns over the blocked B layout
+			with_large_ffts(p.n1, p.n2, [&](auto, auto f2) {
+				using F2 = decltype(f2);
+				with_cols_warp(p.n1, p.n2, [&](auto plan) {
+					using P = decltype(plan);
+					constexpr int CW = P::CW;
+					// the row plan that pairs with the column plan: N = N1 x N2
+					if constexpr (F2::kHooked && ((P::N1 == 400 && F2::N == 500) || (P::N1 == 200 && F2::N == 250))) {
+						const size_t smem_r = smem_inv_rows<F2>(p);
+						set_smem(inv_rows_kernel<F2, CW>, smem_r);
+						set_smem(inv_cols_warp_kernel<P>, P::smem_bytes());
+						const int t_rows = threads_of<F2>(p.p2, p.rw);
+						require(t_rows <= F2::kRowsMaxThreads, "row kernel needs more threads than its launch bound");
+						KernelTimer timer(ctx, "acq_inverse_large");
+						run_batches([&] {
+							inv_rows_kernel<F2, CW><<<p.rows * chunks_of(p.n1, p.rw), t_rows, smem_r, ctx->stream>>>(p);
+							inv_cols_warp_kernel<P><<<p.rows * chunks, 32 * P::WARPS, P::smem_bytes(), ctx->stream>>>(p);
+						});
+					}
+				});
+			});
+			return;
 		}
 		with_large_ffts(p.n1, p.n2, [&](auto f1, auto f2) {
 			using F1 = decltype(f1);
@@ -379,24 +468,11 @@ namespace ugsdr_gpu {
 			require(t_rows <= F2::kRowsMaxThreads, "row kernel needs more threads than its launch bound");
 			require(t_cols <= F1::kColsMaxThreads, "column kernel needs more threads than its launch bound");
 			KernelTimer timer(ctx, "acq_inverse_large");
-			for (int row0 = 0; row0 < s.rows; row0 += r_max) {
-				p.row0 = row0;
-				p.rows = std::min(r_max, s.rows - row0);
-				UG_CUDA(cudaMemsetAsync(p.counters, 0, sizeof(unsigned int) * p.rows, ctx->stream));
-				if (s.fold_mode) {
-					UG_CUDA(cudaMemsetAsync(p.accg, 0, sizeof(float) * static_cast<size_t>(p.rows) * s.m, ctx->stream));
-					if (s.fold_mode == 2)
-						UG_CUDA(cudaMemsetAsync(p.zcg, 0, sizeof(float2) * static_cast<size_t>(p.rows) * s.k * s.m, ctx->stream));
-				}
+			run_batches([&] {
 				const int row_items = F2::kHooked ? p.rows : p.rows * s.k;  // hooked: each CTA loops over the K blocks
 				inv_rows_kernel<F2><<<row_items * chunks_of(p.n1, p.rw), t_rows, smem_r, ctx->stream>>>(p);
 				inv_cols_kernel<F1><<<p.rows * chunks, t_cols, smem_c, ctx->stream>>>(p);
-				note_launch(ctx, 2);
-				if (s.fold_mode) {
-					fold_finish_kernel<<<p.rows, kBatchedThreads, 0, ctx->stream>>>(p);
-					note_launch(ctx);
-				}
-			}
+			});
 		});
 	}
 

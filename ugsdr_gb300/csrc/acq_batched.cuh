@@ -123,6 +123,7 @@ namespace ugsdr_gpu {
 		AcqParams base;         // n, k_blocks, n_doppler, n_codes, m, fold_mode, stat, one_sided, adders, lut, spectra, codes, cells
 		FftPlanDev p1, p2;      // N1-point, N2-point plans
 		int n1, n2;
+		int n2p;                // blocked B layout (inv_cols_warp_kernel): N2 padded to a multiple of its CW
 		int cw, rw;             // columns per column-kernel CTA (power of two), rows per row-kernel CTA
 		int cw_shift;           // log2(cw)
 		int ld1;                // column-tile stride: N1 rounded up to odd (conflict-free smem)
@@ -472,6 +473,30 @@ namespace ugsdr_gpu {
 			}
 		}
 	};
+	// The same store into the blocked layout B[n2 / CW][k1][n2 % CW] of the
+	// warp-owned column kernel (out: the (row, block) base, N1 x n2p entries).
+	template <int CW>
+	struct InvRowsEmitBlocked {
+		float2* out;
+		int n1, r0;
+		uint32_t n;
+		float inv_n2;  // 2 / N
+		template <int R, int NS>
+		__device__ __forceinline__ void put(int f, int base, const float2 (&v)[R]) const {
+			const uint32_t k1 = static_cast<uint32_t>(r0 + f);
+			float2 w = tw_n((static_cast<uint32_t>(base) * k1) % n, n, inv_n2, true);
+			const float2 step = tw_n((static_cast<uint32_t>(NS) * k1) % n, n, inv_n2, true);
+			float2* o = out + static_cast<size_t>(k1) * CW;
+			const size_t chunk_stride = static_cast<size_t>(n1) * CW;
+#pragma unroll
+			for (int r = 0; r < R; ++r) {
+				const int n2 = base + r * NS;
+				o[static_cast<size_t>(n2 / CW) * chunk_stride + (n2 % CW)] = cmul(v[r], w);
+				w = cmul(w, step);
+			}
+		}
+	};
+
 	// Column stage: the last pass scales each output (1/N, x2 one-sided),
 	// takes |.| or |.|^2 and accumulates it (or, folded, adds it to the row's
 	// fold buffer) instead of storing the transform.
@@ -524,7 +549,9 @@ namespace ugsdr_gpu {
 
 	// hooked plans: grid rows * ceil(N1 / rw), each CTA over the K blocks;
 	// others: grid rows * K * ceil(N1 / rw)
-	template <class F2>
+	// BCW > 0: B goes out in the blocked layout of inv_cols_warp_kernel with
+	// CW = BCW (hooked plans only)
+	template <class F2, int BCW = 0>
 	__global__ void __launch_bounds__(F2::kRowsMaxThreads, F2::kRowsMinBlocks) inv_rows_kernel(BatchedParams p) {
 		extern __shared__ float2 smem[];
 		const AcqParams& q = p.base;
@@ -568,20 +595,28 @@ namespace ugsdr_gpu {
 				cp_async_wait_all();
 				__syncthreads();  // this block's X (and the twiddle table) in shared memory
 				const size_t item = static_cast<size_t>(lrow) * q.k_blocks + blk;
-				const InvRowsEmit emit{p.bbuf + item * n + static_cast<size_t>(r0) * n2, n2, r0, static_cast<uint32_t>(n),
-					2.0f / static_cast<float>(n)};
 				auto next = [&] {  // pass 0 has read xs: the next block's X goes there
 					if (blk + 1 < q.k_blocks) {
 						copy_rows(xs, xg + static_cast<size_t>(blk + 1) * n);
 						cp_async_commit();
 					}
 				};
-				F2::template run_hooked<true, true>(a, b, p2, rw, n2, load, emit, next);
+				if constexpr (BCW > 0) {
+					const InvRowsEmitBlocked<BCW> emit{p.bbuf + item * (static_cast<size_t>(n1) * p.n2p), n1, r0,
+						static_cast<uint32_t>(n), 2.0f / static_cast<float>(n)};
+					F2::template run_hooked<true, true>(a, b, p2, rw, n2, load, emit, next);
+				}
+				else {
+					const InvRowsEmit emit{p.bbuf + item * n + static_cast<size_t>(r0) * n2, n2, r0, static_cast<uint32_t>(n),
+						2.0f / static_cast<float>(n)};
+					F2::template run_hooked<true, true>(a, b, p2, rw, n2, load, emit, next);
+				}
 				// the next iteration's first barrier orders this block's last-pass
 				// reads of `b` before its first pass writes it again
 			}
 			return;
 		}
+		static_assert(BCW == 0 || F2::kHooked, "the blocked B layout needs a hooked row plan");
 		const int item = blockIdx.x / chunks;       // (local row, block)
 		const int r0 = (blockIdx.x - item * chunks) * p.rw;
 		const int rw = min(p.rw, n1 - r0);
