@@ -198,8 +198,11 @@ namespace ugsdr_gpu {
 
 		// Column plans of the warp-owned column kernel (unfolded rows): N1 = 400
 		// (200,000-point blocks) and 200 (50,000-point blocks), radix 25 last.
-		using ColsWarp400 = ColsWarpPlan<400, 16, 25, 4, 3>;
-		using ColsWarp200 = ColsWarpPlan<200, 8, 25, 4, 3>;
+		// two warps per CTA (7 CTAs per SM): the default step measured 100.0 ms,
+		// against 102.1 with four warps for the 200-point columns and 103.5
+		// with four for both
+		using ColsWarp400 = ColsWarpPlan<400, 16, 25, 2, 7>;
+		using ColsWarp200 = ColsWarpPlan<200, 8, 25, 2, 7>;
 		template <class Fn>
 		bool with_cols_warp(int n1, int n2, Fn&& fn) {
 			if (n1 == 400 && n2 == 500)
@@ -443,13 +446,13 @@ namespace ugsdr_gpu {
 					// the row plan that pairs with the column plan: N = N1 x N2
 					if constexpr (F2::kHooked && ((P::N1 == 400 && F2::N == 500) || (P::N1 == 200 && F2::N == 250))) {
 						const size_t smem_r = smem_inv_rows<F2>(p);
-						set_smem(inv_rows_kernel<F2, CW>, smem_r);
+						set_smem(inv_rows_kernel<F2, CW, P::N1>, smem_r);
 						set_smem(inv_cols_warp_kernel<P>, P::smem_bytes());
 						const int t_rows = threads_of<F2>(p.p2, p.rw);
 						require(t_rows <= F2::kRowsMaxThreads, "row kernel needs more threads than its launch bound");
 						KernelTimer timer(ctx, "acq_inverse_large");
 						run_batches([&] {
-							inv_rows_kernel<F2, CW><<<p.rows * chunks_of(p.n1, p.rw), t_rows, smem_r, ctx->stream>>>(p);
+							inv_rows_kernel<F2, CW, P::N1><<<p.rows * chunks_of(p.n1, p.rw), t_rows, smem_r, ctx->stream>>>(p);
 							inv_cols_warp_kernel<P><<<p.rows * chunks, 32 * P::WARPS, P::smem_bytes(), ctx->stream>>>(p);
 						});
 					}

@@ -475,24 +475,37 @@ namespace ugsdr_gpu {
 	};
 	// The same store into the blocked layout B[n2 / CW][k1][n2 % CW] of the
 	// warp-owned column kernel (out: the (row, block) base, N1 x n2p entries).
-	template <int CW>
+	template <int CW, int N1>
 	struct InvRowsEmitBlocked {
 		float2* out;
-		int n1, r0;
+		int r0;
 		uint32_t n;
 		float inv_n2;  // 2 / N
+		// In the last pass base < NS (NB = NS), so when CW divides NS every
+		// output of the butterfly sits a compile-time distance from the first:
+		// n2 = base + r NS lies in chunk base / CW + r NS / CW at column base % CW.
 		template <int R, int NS>
 		__device__ __forceinline__ void put(int f, int base, const float2 (&v)[R]) const {
 			const uint32_t k1 = static_cast<uint32_t>(r0 + f);
 			float2 w = tw_n((static_cast<uint32_t>(base) * k1) % n, n, inv_n2, true);
 			const float2 step = tw_n((static_cast<uint32_t>(NS) * k1) % n, n, inv_n2, true);
-			float2* o = out + static_cast<size_t>(k1) * CW;
-			const size_t chunk_stride = static_cast<size_t>(n1) * CW;
+			constexpr int S = N1 * CW;  // one chunk of the blocked layout
+			if constexpr (NS % CW == 0) {
+				float2* o = out + (k1 * CW + (base / CW) * S + base % CW);
 #pragma unroll
-			for (int r = 0; r < R; ++r) {
-				const int n2 = base + r * NS;
-				o[static_cast<size_t>(n2 / CW) * chunk_stride + (n2 % CW)] = cmul(v[r], w);
-				w = cmul(w, step);
+				for (int r = 0; r < R; ++r) {
+					o[r * (NS / CW) * S] = cmul(v[r], w);
+					w = cmul(w, step);
+				}
+			}
+			else {
+				float2* o = out + k1 * CW;
+#pragma unroll
+				for (int r = 0; r < R; ++r) {
+					const int n2 = base + r * NS;
+					o[(n2 / CW) * S + (n2 % CW)] = cmul(v[r], w);
+					w = cmul(w, step);
+				}
 			}
 		}
 	};
@@ -551,7 +564,7 @@ namespace ugsdr_gpu {
 	// others: grid rows * K * ceil(N1 / rw)
 	// BCW > 0: B goes out in the blocked layout of inv_cols_warp_kernel with
 	// CW = BCW (hooked plans only)
-	template <class F2, int BCW = 0>
+	template <class F2, int BCW = 0, int BN1 = 0>
 	__global__ void __launch_bounds__(F2::kRowsMaxThreads, F2::kRowsMinBlocks) inv_rows_kernel(BatchedParams p) {
 		extern __shared__ float2 smem[];
 		const AcqParams& q = p.base;
@@ -602,7 +615,7 @@ namespace ugsdr_gpu {
 					}
 				};
 				if constexpr (BCW > 0) {
-					const InvRowsEmitBlocked<BCW> emit{p.bbuf + item * (static_cast<size_t>(n1) * p.n2p), n1, r0,
+					const InvRowsEmitBlocked<BCW, BN1> emit{p.bbuf + item * (static_cast<size_t>(n1) * p.n2p), r0,
 						static_cast<uint32_t>(n), 2.0f / static_cast<float>(n)};
 					F2::template run_hooked<true, true>(a, b, p2, rw, n2, load, emit, next);
 				}
