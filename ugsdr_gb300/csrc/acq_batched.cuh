@@ -69,6 +69,7 @@ namespace ugsdr_gpu {
 		static constexpr int N = 0;
 		static constexpr bool kHooked = false;
 		static constexpr int kPasses = 0;
+		static constexpr int kLastNS = 0;
 		static constexpr bool kRowsCompact = false;
 		static constexpr int kRowsMaxThreads = 256;
 		static constexpr int kRowsMinBlocks = 3;
@@ -339,10 +340,9 @@ namespace ugsdr_gpu {
 			for (int r = 0; r < R; ++r) {
 				const int k2 = base + r * NS;
 				const bool zero = one_sided && (r0 + f) + static_cast<int64_t>(n1) * k2 > half;
-				if (code_mode)
-					o[r * NS] = zero ? c2(0.f, 0.f) : c2(v[r].x, -v[r].y);
-				else if (!zero)
-					o[r * NS] = v[r];
+				// signal spectra are written whole: the inverse gather multiplies
+				// by the one-sided code spectrum, zero above N/2, with no test
+				o[r * NS] = code_mode ? (zero ? c2(0.f, 0.f) : c2(v[r].x, -v[r].y)) : v[r];
 			}
 		}
 	};
@@ -418,8 +418,8 @@ namespace ugsdr_gpu {
 				const float2 v = y[e];
 				out[e] = zero ? c2(0.f, 0.f) : c2(v.x, -v.y);
 			}
-			else if (!zero) {
-				out[e] = y[e];  // bins above N/2 are never read in one-sided mode
+			else {
+				out[e] = y[e];  // whole spectrum (see FwdRowsEmit)
 			}
 		}
 	}
@@ -447,24 +447,38 @@ namespace ugsdr_gpu {
 		const float2* xs;
 		const float2* cs;
 		const float2* code_g;
-		int n1, n2, r0, half, one_sided;
-		__device__ __forceinline__ float2 operator()(int f, int k2) const {
-			if (one_sided && (r0 + f) + n1 * k2 > half)
-				return c2(0.f, 0.f);
+		// one-sided: Z = 0 above N/2 because the code spectrum is zero there and
+		// the forward kernels write the whole signal spectrum (finite values)
+		__device__ __forceinline__ float2 operator()(int f, int k2, int n2) const {
 			const int off = f * n2 + k2;
 			return cmul(xs[off], cs ? cs[off] : __ldg(code_g + off));
 		}
 	};
+	struct InvRowsLoadStagedN {
+		InvRowsLoadStaged g;
+		int n2;
+		__device__ __forceinline__ float2 operator()(int f, int k2) const { return g(f, k2, n2); }
+	};
+	// Inter-step twiddle seeds of the row stage, per CTA: for each of its rows
+	// k1 = r0 + f, W_N^{-j k1} for j < NS and W_N^{-NS k1} at j = NS, where NS
+	// is the stride of the plan's last pass (whose butterflies start at base
+	// = j < NS); built once per CTA and reused over the K blocks.
+	__device__ __forceinline__ void build_row_seeds(float2* seeds, int rows, int ns, int r0, uint32_t n) {
+		const float inv_n2 = 2.0f / static_cast<float>(n);
+		for (int e = threadIdx.x; e < rows * (ns + 1); e += blockDim.x) {
+			const int f = e / (ns + 1), j = e - f * (ns + 1);
+			seeds[e] = tw_n((static_cast<uint32_t>(j) * static_cast<uint32_t>(r0 + f)) % n, n, inv_n2, true);
+		}
+	}
+
 	struct InvRowsEmit {
 		float2* out;
 		int n2, r0;
-		uint32_t n;
-		float inv_n2;  // 2 / N
+		const float2* seeds;  // build_row_seeds
 		template <int R, int NS>
 		__device__ __forceinline__ void put(int f, int base, const float2 (&v)[R]) const {
-			const uint32_t k1 = static_cast<uint32_t>(r0 + f);
-			float2 w = tw_n((static_cast<uint32_t>(base) * k1) % n, n, inv_n2, true);
-			const float2 step = tw_n((static_cast<uint32_t>(NS) * k1) % n, n, inv_n2, true);
+			float2 w = seeds[f * (NS + 1) + base];
+			const float2 step = seeds[f * (NS + 1) + NS];
 			float2* o = out + static_cast<size_t>(f) * n2 + base;
 #pragma unroll
 			for (int r = 0; r < R; ++r) {
@@ -479,16 +493,15 @@ namespace ugsdr_gpu {
 	struct InvRowsEmitBlocked {
 		float2* out;
 		int r0;
-		uint32_t n;
-		float inv_n2;  // 2 / N
+		const float2* seeds;  // build_row_seeds
 		// In the last pass base < NS (NB = NS), so when CW divides NS every
 		// output of the butterfly sits a compile-time distance from the first:
 		// n2 = base + r NS lies in chunk base / CW + r NS / CW at column base % CW.
 		template <int R, int NS>
 		__device__ __forceinline__ void put(int f, int base, const float2 (&v)[R]) const {
-			const uint32_t k1 = static_cast<uint32_t>(r0 + f);
-			float2 w = tw_n((static_cast<uint32_t>(base) * k1) % n, n, inv_n2, true);
-			const float2 step = tw_n((static_cast<uint32_t>(NS) * k1) % n, n, inv_n2, true);
+			const int k1 = r0 + f;
+			float2 w = seeds[f * (NS + 1) + base];
+			const float2 step = seeds[f * (NS + 1) + NS];
 			constexpr int S = N1 * CW;  // one chunk of the blocked layout
 			if constexpr (NS % CW == 0) {
 				float2* o = out + (k1 * CW + (base / CW) * S + base % CW);
@@ -603,7 +616,10 @@ namespace ugsdr_gpu {
 				copy_rows(cs, code);
 			copy_rows(xs, xg);
 			cp_async_commit();
-			const InvRowsLoadStaged load{xs, cs, code, n1, n2, r0, half, q.one_sided};
+			const InvRowsLoadStagedN load{InvRowsLoadStaged{xs, cs, code}, n2};
+			// twiddle seeds after the pass tables (N2 entries)
+			float2* seeds = const_cast<float2*>(p2.tw) + F2::N;
+			build_row_seeds(seeds, rw, F2::kLastNS, r0, static_cast<uint32_t>(n));
 			for (int blk = 0; blk < q.k_blocks; ++blk) {
 				cp_async_wait_all();
 				__syncthreads();  // this block's X (and the twiddle table) in shared memory
@@ -615,13 +631,11 @@ namespace ugsdr_gpu {
 					}
 				};
 				if constexpr (BCW > 0) {
-					const InvRowsEmitBlocked<BCW, BN1> emit{p.bbuf + item * (static_cast<size_t>(n1) * p.n2p), r0,
-						static_cast<uint32_t>(n), 2.0f / static_cast<float>(n)};
+					const InvRowsEmitBlocked<BCW, BN1> emit{p.bbuf + item * (static_cast<size_t>(n1) * p.n2p), r0, seeds};
 					F2::template run_hooked<true, true>(a, b, p2, rw, n2, load, emit, next);
 				}
 				else {
-					const InvRowsEmit emit{p.bbuf + item * n + static_cast<size_t>(r0) * n2, n2, r0, static_cast<uint32_t>(n),
-						2.0f / static_cast<float>(n)};
+					const InvRowsEmit emit{p.bbuf + item * n + static_cast<size_t>(r0) * n2, n2, r0, seeds};
 					F2::template run_hooked<true, true>(a, b, p2, rw, n2, load, emit, next);
 				}
 				// the next iteration's first barrier orders this block's last-pass

@@ -171,6 +171,13 @@ namespace ugsdr_gpu {
 	}
 
 	template <int... Rs>
+	constexpr int radix_last() {
+		int l = 1;
+		((l = Rs), ...);
+		return l;
+	}
+
+	template <int... Rs>
 	constexpr int radix_min() {
 		int m = 1 << 30;
 		((m = Rs < m ? Rs : m), ...);
@@ -185,6 +192,8 @@ namespace ugsdr_gpu {
 		static constexpr int N = N_;
 		static constexpr bool kHooked = true;  // kernels fuse their producer/consumer into the first/last pass
 		static constexpr int kPasses = sizeof...(Rs);
+		// stride of the last pass (its butterflies start at base = j < kLastNS)
+		static constexpr int kLastNS = N_ / radix_last<Rs...>();
 		// inverse row kernel launch bounds: a hooked two-pass plan whose widest
 		// pass over 8 rows fits 224 threads runs one shared tile and four CTAs
 		// per SM (72 registers), other plans two tiles and three CTAs
