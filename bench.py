@@ -560,7 +560,7 @@ def track_capture(dev, seconds, seed=3, n_channels=256, sigma=20.0):
     rng = np.random.default_rng(seed)
     fs = TRACK_FS
     device = f"cuda:{dev}" if isinstance(dev, int) else dev
-    gps = [api.prn_code(L.GPS_L1CA, p) for p in range(32)]
+    gps = list(golden_chips("gps_l1ca")[:32])
     e1b, e1c = golden_chips("galileo_e1b"), golden_chips("galileo_e1c")
     codes = gps + list(e1b) + list(e1c)
     rate_of = [1.023e6] * 32 + [2.046e6] * 100

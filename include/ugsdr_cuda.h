@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define UGSDR_CUDA_ABI_VERSION 6
+#define UGSDR_CUDA_ABI_VERSION 7
 
 enum ugsdr_status {
 	UGSDR_OK = 0,
@@ -336,13 +336,20 @@ typedef struct ugsdr_track_config {
 	double dll_bandwidth;           /* Hz (reference 0.7) */
 	double fll_bandwidth;           /* Hz, FLL assist; 0 = off (reference 250) */
 	double integration_time;        /* s; 0.001 (one epoch) is supported */
+	/* Carrier NCO: 0 = 64-bit fixed-point phase, continuous across epochs
+	 * (cycles * 2^64, top 6 bits index the 64-entry LUT); 1 = the reference's:
+	 * the carrier phase in double radians (UpdatePhase, Pll), each epoch's
+	 * wipe-off a fresh 32-bit TableMixer NCO from it (Mixer::Translate,
+	 * src/mixer/mixer.hpp:33-42, nco.hpp:17-20) and the PLL discriminator's
+	 * atan in double, as tracking_parameters.hpp:495-511 computes it. */
+	int nco_mode;
 } ugsdr_track_config;
 
 /* Per channel per epoch output: taps VE, E, P, L, VL as I/Q and loop state. */
 typedef struct ugsdr_track_output {
 	float taps[5][2];
 	double carrier_frequency;
-	double carrier_phase;       /* rad, wrapped */
+	double carrier_phase;       /* rad: wrapped (nco_mode 0), the reference's unwrapped phase (nco_mode 1) */
 	double code_phase;          /* samples (TrackingParameters::code_phases) */
 	double code_frequency;
 	double phase_error;         /* PLL discriminator, cycles */

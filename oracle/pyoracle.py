@@ -158,17 +158,19 @@ TRACK_FIELDS = 21
 
 def track(iq_complex: np.ndarray, spm: int, n_epochs: int, chips: np.ndarray, fs: float, code_frequency: float,
           code_phase: float, carrier_frequency: float, carrier_phase: float = 0.0, early_late: float = 0.25,
-          very_early_late: float = 0.5, pll_bw: float = 25.0, dll_bw: float = 0.7, fll_bw: float = 250.0) -> np.ndarray:
+          very_early_late: float = 0.5, pll_bw: float = 25.0, dll_bw: float = 0.7, fll_bw: float = 250.0,
+          nco_mode: int = 0) -> np.ndarray:
     """FP64 restatement of one tracking channel (track_oracle.cpp); rows of
     VE, E, P, L, VL (re, im), carrier_frequency, carrier_phase, code_phase,
-    code_frequency, phase_error, code_error."""
+    code_frequency, phase_error, code_error.  nco_mode 1: the reference's
+    per-epoch 32-bit TableMixer NCO and radian carrier phase."""
     lib = load()
     fn = lib.orc_track_f64
     fn.argtypes = [C.c_void_p, C.c_size_t, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
     fn.restype = None
     x = np.ascontiguousarray(iq_complex, np.complex64)
     c = np.ascontiguousarray(chips, np.float32)
-    cfg = np.array([early_late, very_early_late, pll_bw, dll_bw, fll_bw, 1e-3])
+    cfg = np.array([early_late, very_early_late, pll_bw, dll_bw, fll_bw, 1e-3, float(nco_mode)])
     ch = np.array([fs, code_frequency, float(len(c)), code_phase, carrier_frequency, carrier_phase])
     out = np.zeros((n_epochs, TRACK_FIELDS))
     fn(x.ctypes.data, spm, n_epochs, c.ctypes.data, len(c), cfg.ctypes.data, ch.ctypes.data, out.ctypes.data)
@@ -177,19 +179,19 @@ def track(iq_complex: np.ndarray, spm: int, n_epochs: int, chips: np.ndarray, fs
 
 def track_taps(iq_epoch: np.ndarray, chips: np.ndarray, fs: float, code_frequency: float, code_phase: float,
                carrier_frequency: float, carrier_phase: float, early_late: float = 0.25,
-               very_early_late: float = 0.5) -> np.ndarray:
+               very_early_late: float = 0.5, nco_mode: int = 0) -> np.ndarray:
     """Open-loop taps of one epoch for a given NCO state (orc_track_taps_f64):
     10 values (VE, E, P, L, VL re/im) + 5 minor partial magnitudes."""
     lib = load()
     fn = lib.orc_track_taps_f64
     d = C.c_double
-    fn.argtypes = [C.c_void_p, C.c_size_t, C.c_void_p, C.c_int, d, d, d, d, d, d, d, d, C.c_void_p]
+    fn.argtypes = [C.c_void_p, C.c_size_t, C.c_void_p, C.c_int, d, d, d, d, d, d, d, d, C.c_int, C.c_void_p]
     fn.restype = None
     x = np.ascontiguousarray(iq_epoch, np.complex64)
     c = np.ascontiguousarray(chips, np.float32)
     out = np.zeros(15)
     fn(x.ctypes.data, x.size, c.ctypes.data, len(c), fs, code_frequency, float(len(c)), code_phase, carrier_frequency,
-       carrier_phase, early_late, very_early_late, out.ctypes.data)
+       carrier_phase, early_late, very_early_late, nco_mode, out.ctypes.data)
     return out
 
 
@@ -225,23 +227,29 @@ def unpack_nt1065(raw: np.ndarray, channel: int) -> np.ndarray:
 
 def track_refine(x: np.ndarray, channels: list[dict], codes: list[np.ndarray]):
     """TrackingParameters::AddSignalImpl's refinement (tracking_parameters.hpp:
-    297-357) with the oracle's primitives, for channels whose code period is
-    1 ms (the oracle's fold block is one ms): returns (accepted, offsets,
-    refined code phases, peak levels)."""
+    297-357) restated: three code periods translated by -carrier_frequency
+    (TableMixer), matched-filtered against one code period upsampled,
+    zero-padded to three and rotated right by the integer code phase (the
+    reference's FFTW filter: one-sided conj code spectrum, FP64 here), |.|
+    folded to one code period, first maximum, offset wrapped to +-period / 2,
+    accepted when within 1e-6 fs samples of a whole ms.  Returns (accepted,
+    offsets, refined code phases, peak levels)."""
     acc, offs, phases, levels = [], [], [], []
     for ch in channels:
         fs = ch["fs"]
         spm = int(fs / 1e3)
         chips = np.asarray(codes[ch["code"]], np.float32)
         period = spm * int(round(len(chips) / ch["code_frequency"] * 1000))
-        assert period == spm
         n = 3 * period
-        y = table_mix(np.ascontiguousarray(x[:n], np.complex64), fs, -ch["carrier_frequency"])
-        replica = np.zeros(n, np.float32)
+        y = table_mix(np.ascontiguousarray(x[:n], np.complex64), fs, -ch["carrier_frequency"]).astype(np.complex128)
+        replica = np.zeros(n, np.float64)
         replica[:period] = upsample(chips, period)
         replica = np.roll(replica, int(ch["code_phase"]))          # std::rotate right by (ptrdiff_t)code_phase
-        rec = acquire(y, n, 1, replica, fs, 0.0, 1.0, reshape=True, coherent=True)
-        off = int(rec["index"])
+        spec = np.fft.fft(replica)
+        spec[n // 2 + 1:] = 0.0                                    # r2c: bins above N/2 stay zero (dft.hpp:37-46)
+        mf = np.abs(np.fft.ifft(np.fft.fft(y) * np.conj(spec)) * 2.0)
+        folded = mf.reshape(3, period).sum(axis=0)
+        off = int(np.argmax(folded))
         if off > period // 2:
             off -= period
         mod = (off + period) % spm
@@ -251,8 +259,25 @@ def track_refine(x: np.ndarray, channels: list[dict], codes: list[np.ndarray]):
         acc.append(1 if ok else 0)
         offs.append(off)
         phases.append(ch["code_phase"] + off if ok else ch["code_phase"])
-        levels.append(rec["level"])
+        levels.append(float(folded.max()))
     return acc, offs, phases, levels
+
+
+def track_loop(taps: np.ndarray, fs: float, code_frequency: float, code_phase: float, carrier_frequency: float,
+               pll_bw: float = 25.0, dll_bw: float = 0.7, fll_bw: float = 250.0) -> np.ndarray:
+    """The oracle's loop update alone (orc_track_loop_f64) on given per-epoch
+    E, P, L taps (rows of 6: re, im): rows of carrier_frequency, carrier_phase
+    (rad), code_phase, code_frequency, phase_error, code_error."""
+    lib = load()
+    fn = lib.orc_track_loop_f64
+    fn.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+    fn.restype = None
+    t = np.ascontiguousarray(taps, np.float64)
+    cfg = np.array([pll_bw, dll_bw, fll_bw, 1e-3, fs, code_frequency])
+    init = np.array([carrier_frequency, 0.0, code_phase])
+    out = np.zeros((t.shape[0], 6))
+    fn(t.ctypes.data, t.shape[0], cfg.ctypes.data, init.ctypes.data, out.ctypes.data)
+    return out
 
 
 def stft(x: np.ndarray, window: int = 128, overlap: int = 96) -> np.ndarray:

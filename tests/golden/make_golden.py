@@ -408,6 +408,64 @@ def preamble(lib) -> dict[str, np.ndarray]:
     return out
 
 
+TRACK_FS = 4e6
+TRACK_MS = 160
+
+
+def track(lib) -> dict[str, np.ndarray]:
+    """The reference's own tracking arithmetic on a seeded capture (int8 I/Q,
+    4 MHz, 160 ms): three GPS L1 C/A channels and one Galileo E1B channel
+    (4 ms code period), each started from an acquisition-like state (code
+    phase to the sample, Doppler to the 50 Hz grid) and run through
+    ref_track_f32 (TrackSingleSatellite with the reference's TableMixer,
+    UpdatePhase, CorrelateSplit, Pll, Dll), and AddSignalImpl's refinement
+    (ref_refine_f32) from a code phase 3 samples off."""
+    d, vp, sz, i = C.c_double, C.c_void_p, C.c_size_t, C.c_int
+    lib.ref_track_f32.argtypes = [vp, sz, i, vp, sz, i, d, d, d, d, vp]
+    lib.ref_refine_f32.argtypes = [vp, sz, i, i, d, d, d, vp]
+    fix = np.load(HERE / "codes.npz")
+    ca, e1b = unpack(fix, "gps_l1ca"), unpack(fix, "galileo_e1b")
+    rng = np.random.default_rng(31)
+    chans = [dict(signal=0, prn=3, chips=ca[3], rate=1.023e6, cn0=47.0, data=50.0),
+             dict(signal=0, prn=11, chips=ca[11], rate=1.023e6, cn0=44.0, data=50.0),
+             dict(signal=0, prn=24, chips=ca[24], rate=1.023e6, cn0=41.0, data=50.0),
+             dict(signal=6, prn=7, chips=e1b[7], rate=2.046e6, cn0=46.0, data=250.0)]
+    ems = []
+    for ch in chans:
+        ch["code_phase_chips"] = rng.uniform(0, len(ch["chips"]))
+        ch["doppler"] = rng.uniform(-3500, 3500)
+        ems.append(signals.Emitter(ch["chips"], ch["rate"], ch["code_phase_chips"], ch["doppler"], ch["cn0"], ch["data"],
+                                   rng.uniform(0, 2 * np.pi)))
+    n = int(TRACK_FS * TRACK_MS / 1000)
+    raw = signals.synthesize(ems, TRACK_FS, n, 20.0, "ci8", 32)
+    x = raw.astype(np.float32)
+    x = np.ascontiguousarray((x[:, 0] + 1j * x[:, 1]).astype(np.complex64))
+    spm = int(TRACK_FS / 1000)
+    out = {"samples": raw, "fs": np.float64(TRACK_FS)}
+    for k, ch in enumerate(chans):
+        period_ms = int(round(len(ch["chips"]) / ch["rate"] * 1000))
+        cp = float(round(ch["code_phase_chips"] / ch["rate"] * TRACK_FS % (period_ms * spm)))
+        cf = round(ch["doppler"] / 50.0) * 50.0
+        full = np.zeros(3 * period_ms * spm, np.float32)
+        rep = np.ascontiguousarray(np.tile(ch["chips"], 3).astype(np.float32))
+        lib.ref_repeat_upsample(p(rep), rep.size, 1, p(full), full.size)
+        res = np.zeros((TRACK_MS, 12))
+        lib.ref_track_f32(p(x), spm, TRACK_MS, p(full), full.size, ch["signal"], TRACK_FS, ch["rate"], cp, cf, p(res))
+        ref3 = np.zeros(4)
+        lib.ref_refine_f32(p(x), x.size, ch["signal"], ch["prn"], TRACK_FS, cp + 3.0, cf, p(ref3))
+        pre = f"ch{k}/"
+        out[pre + "signal"] = np.int32(ch["signal"])
+        out[pre + "prn"] = np.int32(ch["prn"])
+        out[pre + "code_frequency"] = np.float64(ch["rate"])
+        out[pre + "code_phase"] = np.float64(cp)
+        out[pre + "carrier_frequency"] = np.float64(cf)
+        out[pre + "track"] = res
+        out[pre + "refine_code_phase"] = np.float64(cp + 3.0)
+        out[pre + "refine"] = ref3
+    out["channels"] = np.int32(len(chans))
+    return out
+
+
 def main() -> None:
     ref_dir = sys.argv[1] if len(sys.argv) > 1 else str(Path(__file__).resolve().parents[3] / "reference")
     lib = ref_lib(ref_dir)
@@ -426,6 +484,7 @@ def main() -> None:
     np.savez_compressed(HERE / "real8.npz", **real8(ref_dir))
     np.savez_compressed(HERE / "iq16.npz", **iq16(ref_dir))
     np.savez_compressed(HERE / "preamble.npz", **preamble(lib))
+    np.savez_compressed(HERE / "track.npz", **track(lib))
     for f in sorted(HERE.glob("*.npz")):
         print(f.name, f.stat().st_size)
 

@@ -5,7 +5,7 @@ import numpy as np
 from pathlib import Path
 import pytest
 
-from conftest import unpack_codes
+from conftest import GOLDEN, unpack_codes
 
 
 def test_table_mixer_bit_exact(oracle, kats):
@@ -222,3 +222,65 @@ def test_observables_oracle(oracle):
     f_prev = np.concatenate([[f0], rows["carrier_frequency"][:-1]])
     cycles = ph0 / (2 * np.pi) + np.cumsum(f_prev / 1000 + rows["phase_error"] / 4)
     np.testing.assert_allclose(o[:, 1], -cycles + np.arange(1, n + 1) * if_hz / 1e3, rtol=0, atol=1e-8)
+
+
+# ---------------------------------------------------------------- tracking
+def _track_fixture():
+    z = np.load(GOLDEN / "track.npz")
+    raw = z["samples"].astype(np.float32)
+    x = (raw[:, 0] + 1j * raw[:, 1]).astype(np.complex64)
+    fix = np.load(GOLDEN / "codes.npz")
+    chips = {0: unpack_codes(fix, "gps_l1ca"), 6: unpack_codes(fix, "galileo_e1b")}
+    chans = []
+    for k in range(int(z["channels"])):
+        pre = f"ch{k}/"
+        chans.append(dict(signal=int(z[pre + "signal"]), chips=chips[int(z[pre + "signal"])][int(z[pre + "prn"])],
+                          base=float(z[pre + "code_frequency"]), code_phase=float(z[pre + "code_phase"]),
+                          carrier_frequency=float(z[pre + "carrier_frequency"]), track=z[pre + "track"],
+                          refine_code_phase=float(z[pre + "refine_code_phase"]), refine=z[pre + "refine"]))
+    return float(z["fs"]), x, chans
+
+
+def test_track_taps_pinned_to_reference(oracle):
+    """The oracle's per-epoch taps (track_oracle.cpp, the reference NCO mode)
+    from the reference tracker's own state at each epoch equal the
+    reference's E / P / L (CorrelateSplit with TableMixer wipe-off,
+    tracking_parameters.hpp:472-493, tracker.hpp:119-139) to 1e-5 of the
+    epoch's prompt: the reference sums in float, the oracle in double."""
+    fs, x, chans = _track_fixture()
+    spm = int(fs / 1000)
+    for ch in chans:
+        tr = ch["track"]
+        period_ms = int(round(len(ch["chips"]) / ch["base"] * 1000))
+        for e in range(tr.shape[0]):
+            cf, cph, cp = (ch["carrier_frequency"], 0.0, ch["code_phase"]) if e == 0 else (tr[e - 1, 6], tr[e - 1, 7], tr[e - 1, 8])
+            ph = cp - fs / 1e3 * (e % period_ms)
+            o = oracle.track_taps(x[e * spm:(e + 1) * spm], ch["chips"], fs, ch["base"], ph, cf, cph, 0.25, 0.25, nco_mode=1)
+            mine = np.array([o[2] + 1j * o[3], o[4] + 1j * o[5], o[6] + 1j * o[7]])
+            ref = tr[e, 0:6:2] + 1j * tr[e, 1:6:2]
+            assert np.abs(mine - ref).max() <= 1e-5 * abs(ref[1]), (ch["signal"], e, mine, ref)
+
+
+def test_track_loop_pinned_to_reference(oracle):
+    """The oracle's loop update (Pll then Dll in the reference's types and
+    order, UpdatePhase before the taps) fed the reference's taps reproduces
+    the reference's state after every epoch (tracking_parameters.hpp:163-165,
+    495-528): carrier frequency, carrier phase, code phase, code frequency."""
+    fs, _, chans = _track_fixture()
+    for ch in chans:
+        tr = ch["track"]
+        loop = oracle.track_loop(tr[:, :6], fs, ch["base"], ch["code_phase"], ch["carrier_frequency"])
+        for col_loop, col_ref in ((0, 6), (1, 7), (2, 8), (3, 9), (4, 10), (5, 11)):
+            np.testing.assert_allclose(loop[:, col_loop], tr[:, col_ref], rtol=1e-12, atol=1e-12)
+
+
+def test_track_refine_pinned_to_reference(oracle):
+    """AddSignalImpl's refinement restated (pyoracle.track_refine) gives the
+    reference's offset, acceptance and refined code phase on every channel
+    (GPS L1 C/A 1 ms codes and a Galileo E1B 4 ms code)."""
+    fs, x, chans = _track_fixture()
+    channels = [dict(fs=fs, code=i, code_frequency=ch["base"], code_phase=ch["refine_code_phase"],
+                     carrier_frequency=ch["carrier_frequency"]) for i, ch in enumerate(chans)]
+    acc, offs, phases, _ = oracle.track_refine(x, channels, [ch["chips"] for ch in chans])
+    for i, ch in enumerate(chans):
+        assert offs[i] == int(ch["refine"][0]) and acc[i] == int(ch["refine"][1]) and phases[i] == ch["refine"][2], i

@@ -10,7 +10,7 @@ from pathlib import Path
 
 LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libugsdr_cuda.so"
 
-ABI_VERSION = 6  # UGSDR_CUDA_ABI_VERSION the structs below mirror
+ABI_VERSION = 7  # UGSDR_CUDA_ABI_VERSION the structs below mirror
 
 OK = 0
 E_INVALID = -1
@@ -93,6 +93,7 @@ class TrackConfig(C.Structure):
         ("dll_bandwidth", C.c_double),
         ("fll_bandwidth", C.c_double),
         ("integration_time", C.c_double),
+        ("nco_mode", C.c_int),
     ]
 
 

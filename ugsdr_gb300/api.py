@@ -349,7 +349,8 @@ class TrackBank:
     their NCO and loop state stays on the device between run() calls."""
 
     def __init__(self, ctx: Context, channels: list[dict], codes: list[np.ndarray], *, early_late: float = 0.25,
-                 very_early_late: float = 0.5, pll_bw: float = 25.0, dll_bw: float = 0.7, fll_bw: float = 250.0):
+                 very_early_late: float = 0.5, pll_bw: float = 25.0, dll_bw: float = 0.7, fll_bw: float = 250.0,
+                 nco_mode: int = 0):
         self.ctx = ctx
         lens = [len(c) for c in codes]
         lmax = max(lens)
@@ -361,7 +362,7 @@ class TrackBank:
             code_len = lens[ch["code"]] if 0 <= ch["code"] < len(lens) else 0  # the library rejects bad indices
             chs[i] = L.TrackChannel(ch["code"], ch["fs"], ch["code_frequency"], code_len, ch["code_phase"],
                                     ch["carrier_frequency"], ch.get("carrier_phase", 0.0), ch.get("boc", 0))
-        cfg = L.TrackConfig(early_late, very_early_late, pll_bw, dll_bw, fll_bw, 1e-3)
+        cfg = L.TrackConfig(early_late, very_early_late, pll_bw, dll_bw, fll_bw, 1e-3, nco_mode)
         lens_arr = (C.c_int * len(lens))(*lens)
         h = C.c_void_p()
         ctx._check(ctx.lib.ugsdr_track_create(ctx.h, C.byref(cfg), chs, len(channels), _ptr(table), lens_arr, len(codes),

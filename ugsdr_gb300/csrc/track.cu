@@ -60,6 +60,7 @@ namespace ugsdr_gpu {
 			double prev_re, prev_im;
 			unsigned long long phase_fx;
 			long long epoch;
+			double phase_rad;       // nco_mode 1: the reference's carrier phase, rad
 		};
 
 		struct TrackOut {
@@ -82,6 +83,7 @@ namespace ugsdr_gpu {
 			TrackState* states;
 			TrackOut* out;          // [epoch][channel] or null
 			int stage_g;            // cp.async size (16/8/4) when staged: it divides the epoch and chunk byte offsets and the base alignment
+			int nco_mode;           // 0: 64-bit fixed-point carrier NCO; 1: the reference's per-epoch TableMixer NCO
 		};
 
 		__device__ __forceinline__ unsigned long long frac_to_fx(double cycles) {
@@ -99,6 +101,7 @@ namespace ugsdr_gpu {
 			float prev_re, prev_im;
 			unsigned long long phase_fx;
 			long long epoch;
+			double phase_rad;
 		};
 
 		// q - floor(q / m) m for q >= 0 and integer m, by a reciprocal and an
@@ -186,7 +189,8 @@ namespace ugsdr_gpu {
 			LoopState ls{};
 			if (threadIdx.x == 0)
 				ls = LoopState{st->code_phase, st->carrier_freq, st->carrier_phase_error, st->code_nco, st->code_error,
-					st->code_freq, static_cast<float>(st->prev_re), static_cast<float>(st->prev_im), st->phase_fx, st->epoch};
+					st->code_freq, static_cast<float>(st->prev_re), static_cast<float>(st->prev_im), st->phase_fx, st->epoch,
+					st->phase_rad};
 
 			// carrier NCO of GetEpl's Translate(signal, fs, -f, -phase), lane 0
 			auto nco_setup = [&]() {
@@ -197,6 +201,21 @@ namespace ugsdr_gpu {
 				// NumericallyControlledOscillator's order (nco.hpp:17-20): a sample whose
 				// phase lands exactly on a LUT boundary (rational f / fs) then picks
 				// the same entry as the host restatement
+				if (p.nco_mode == 1) {
+					// Mixer::Translate's NCO (mixer.hpp:21-42, nco.hpp:17-20): phase
+					// reduced to [0, 2 pi), 32-bit holder and adder; carried in the
+					// upper half of the 64-bit accumulator, whose top 6 bits are then
+					// the 32-bit NCO's index and whose wrap is its wrap
+					double ph = fmod(-ls.phase_rad, 2 * kPi);
+					if (ph < 0)
+						ph = __dadd_rn(ph, 2 * kPi);
+					const unsigned long long a32 = static_cast<unsigned long long>(__ddiv_rn(__dmul_rn(4294967296.0, f), p.fs));
+					const unsigned long long h32 =
+						static_cast<unsigned long long>(__ddiv_rn(__dmul_rn(4294967296.0, ph), 2 * kPi)) & 0xFFFFFFFFull;
+					s_adder = a32 << 32;
+					s_holder0 = h32 << 32;
+					return;
+				}
 				double av = kTwo64 * f / p.fs;
 				if (av >= kTwo64)
 					av = 0.0;
@@ -403,8 +422,12 @@ namespace ugsdr_gpu {
 					// discriminators in the reference's float types, side by side:
 					// lane 0 PLL atan(imag / real), 1 FLL atan2(cross, dot), 2 |E|, 3 |L|
 					float part = 0.f;
+					double part_d = 0.0;  // nco_mode 1: the reference's double atan of the float ratio
 					if (lane == 0) {
-						part = pr != 0.f ? atanf(__fdiv_rn(pi, pr)) : 0.f;
+						if (p.nco_mode == 1)
+							part_d = pr != 0.f ? atan(static_cast<double>(__fdiv_rn(pi, pr))) : 0.0;
+						else
+							part = pr != 0.f ? atanf(__fdiv_rn(pi, pr)) : 0.f;
 					}
 					else if (lane == 1) {
 						const float cross = __fsub_rn(__fmul_rn(pr, ppi), __fmul_rn(ppr, pi));
@@ -421,24 +444,29 @@ namespace ugsdr_gpu {
 					const float ea = __shfl_sync(0xffffffffu, part, 2);
 					const float la = __shfl_sync(0xffffffffu, part, 3);
 					if (lane == 0) {
-						const double err = static_cast<double>(part) / (kPi * 2.0);
+						const double err = (p.nco_mode == 1 ? part_d : static_cast<double>(part)) / (kPi * 2.0);
 						const double ferr = static_cast<double>(ferr_f) / kPi;
 						// UpdatePhase (tracking_parameters.hpp:163-165) with the pre-update frequency
 						ls.phase_fx += frac_to_fx(ls.carrier_freq * 1e-3);
+						ls.phase_rad = __dadd_rn(ls.phase_rad, __ddiv_rn(__dmul_rn(2 * kPi, ls.carrier_freq), 1000.0));
 						// Pll(prompt) (tracking_parameters.hpp:495-511), loop filter in FP64
-						ls.carrier_freq += p.k1_pll * err - p.k2_pll * ls.carrier_phase_error - p.k3_pll * ferr;
+						// in the reference's operation order, nothing contracted
+						ls.carrier_freq = __dadd_rn(ls.carrier_freq, __dsub_rn(__dsub_rn(__dmul_rn(p.k1_pll, err),
+							__dmul_rn(p.k2_pll, ls.carrier_phase_error)), __dmul_rn(p.k3_pll, ferr)));
 						ls.carrier_phase_error = err;
 						ls.phase_fx += static_cast<unsigned long long>(llrint(err * (kTwo64 / 4.0)));
+						ls.phase_rad = __dadd_rn(ls.phase_rad, __ddiv_rn(__dmul_rn(err, kPi), 2.0));
 						ls.prev_re = pr;
 						ls.prev_im = pi;
 						// Dll(early, late) (tracking_parameters.hpp:513-528)
 						double ce = 0.0;
 						if (ea + la != 0.f)
 							ce = __fdiv_rn(__fsub_rn(ea, la), __fadd_rn(ea, la));
-						ls.code_nco += (p.k1_dll * (ce - ls.code_error) + p.k2_dll * ce) * dll_scale;
+						ls.code_nco = __dadd_rn(ls.code_nco, __dmul_rn(__dadd_rn(__dmul_rn(p.k1_dll, __dsub_rn(ce, ls.code_error)),
+							__dmul_rn(p.k2_dll, ce)), dll_scale));
 						ls.code_error = ce;
-						ls.code_freq = base_freq - ls.code_nco;
-						ls.code_phase -= p.fs / 1000 / 2 * (ls.code_freq * inv_base - 1);
+						ls.code_freq = __dsub_rn(base_freq, ls.code_nco);
+						ls.code_phase = __dsub_rn(ls.code_phase, __dmul_rn(p.fs / 1000 / 2, __dsub_rn(__ddiv_rn(ls.code_freq, base_freq), 1.0)));
 						if (p.out) {
 							TrackOut o;
 							for (int t = 0; t < 5; ++t) {
@@ -446,7 +474,7 @@ namespace ugsdr_gpu {
 								o.taps[t][1] = taps_im[t];
 							}
 							o.carrier_frequency = ls.carrier_freq;
-							o.carrier_phase = static_cast<double>(ls.phase_fx) / kTwo64 * 2 * kPi;
+							o.carrier_phase = p.nco_mode == 1 ? ls.phase_rad : static_cast<double>(ls.phase_fx) / kTwo64 * 2 * kPi;
 							o.code_phase = ls.code_phase;
 							o.code_frequency = ls.code_freq;
 							o.phase_error = err;
@@ -488,6 +516,7 @@ struct ugsdr_track_bank {
 	size_t spm = 0;
 	double offsets[5] = {};
 	double k1_pll = 0, k2_pll = 0, k3_pll = 0, k1_dll = 0, k2_dll = 0;
+	int nco_mode = 0;
 	DevBuf chips, states;
 };
 
@@ -533,6 +562,7 @@ namespace {
 		p.k3_pll = bank->k3_pll;
 		p.k1_dll = bank->k1_dll;
 		p.k2_dll = bank->k2_dll;
+		p.nco_mode = bank->nco_mode;
 		p.chips = bank->chips.as<float>();
 		p.len_max = bank->len_max;
 		p.lut = get_lut(ctx);
@@ -614,6 +644,8 @@ int ugsdr_track_create(ugsdr_ctx* ctx, const ugsdr_track_config* cfg, const ugsd
 		const double tau1 = gain / (wn * wn), tau2 = 2.0 * zeta / wn;
 		b->k1_dll = tau2 / tau1;
 		b->k2_dll = T / tau1;
+		require(cfg->nco_mode == 0 || cfg->nco_mode == 1, "nco_mode must be 0 or 1");
+		b->nco_mode = cfg->nco_mode;
 
 		std::vector<TrackState> st(n_channels);
 		for (int c = 0; c < n_channels; ++c) {
@@ -640,6 +672,7 @@ int ugsdr_track_create(ugsdr_ctx* ctx, const ugsdr_track_config* cfg, const ugsd
 			const double cyc = ch.carrier_phase / (2 * kPi);
 			double fr = (cyc - std::floor(cyc)) * kTwo64;
 			s.phase_fx = fr >= kTwo64 ? 0ull : static_cast<unsigned long long>(fr);
+			s.phase_rad = ch.carrier_phase;
 			st[c] = s;
 		}
 		b->chips.reserve(sizeof(float) * static_cast<size_t>(n_codes) * code_len_max);
