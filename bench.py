@@ -6,7 +6,10 @@ capture of int16 I/Q at 50 MHz (synthetic, seeded):
   GLONASS L1OF 14 FDMA channels k = -7..+6 (562.5 kHz spacing), same grid
   Galileo E1B  36 PRNs,  4 ms coherent (200,000-point FFT) x 10 blocks, +-5 kHz / 62.5 Hz (161 bins)
 = 1.254e9 cells per step; one step = the 16 jobs of one capture through
-ugsdr_acquire_batch.  Other lines:
+ugsdr_acquire_batch.  The default line also carries a `served` section: a
+bounded prefix of the configuration's Poisson request mix through the
+server (p50/p99, served vs sequential ugsdr_acquire) and a short-job stream
+at a load the GPU carries (--no-served skips it).  Other lines:
   --config gps_l1_4mhz | l5_weak | gal_small   other acquisition searches
   --config track         256-channel tracking bank, 10 s at 20 MHz
   --config jamming       interference stage, 400 ms at 50 MHz
@@ -384,6 +387,8 @@ def run_ours(args, world, rank):
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args, jobs, raw, fs)
+    if rank == 0 and world == 1 and args.config == "multi" and not args.no_served:
+        line["served"] = served_section()
     return line
 
 
@@ -398,8 +403,8 @@ def served_requests(seed: int, n_req: int, rate: float = 2000.0):
     from ugsdr_gb300 import _lib as L
     from ugsdr_gb300 import api
     rng = np.random.default_rng(seed)
-    systems = {"gps": ([api.prn_code(L.GPS_L1CA, p) for p in range(37)], 1.023e6, 1),
-               "l5i": ([api.prn_code(L.GPS_L5I, p) for p in range(32)], 10.23e6, 1),
+    systems = {"gps": (list(golden_chips("gps_l1ca")), 1.023e6, 1),
+               "l5i": (list(golden_chips("gps_l5i")), 10.23e6, 1),
                "e1b": (list(galileo_chips()), 2.046e6, 4)}
     rates = [2.046e6, 4e6, 10.23e6, 20.46e6, 50e6]
     reqs, t = [], 0.0
@@ -418,6 +423,72 @@ def served_requests(seed: int, n_req: int, rate: float = 2000.0):
         reqs.append(dict(arrival=t, system=sysname, fs=fs, t_ms=t_ms, k=k, codes=codes, step=1000.0 / (2 * t_ms),
                          stype="ci8" if rng.integers(2) else "ci16", n_sig=int(rng.integers(0, 13))))
     return reqs, systems
+
+
+def run_short_stream(ctx, n_req: int = 200, rate: float = 200.0, seed: int = 9):
+    """Latency at a load the GPU can carry: a Poisson stream of short GPS L1
+    C/A searches (int8 I/Q at 4 MHz, 1 ms x 4 blocks, 8 PRNs, +-5 kHz at
+    500 Hz: 672,000 cells each) through the server, against the same search
+    run alone through ugsdr_acquire."""
+    from ugsdr_gb300 import _lib as L
+    from ugsdr_gb300 import api, signals
+    rng = np.random.default_rng(seed)
+    gps = golden_chips("gps_l1ca")
+    raw, _ = signals.gps_l1_config(seed=seed, codes={p: gps[p] for p in range(32)}, fs=4e6, ms=4, visible=4)
+    jobs, handles = [], []
+    for _ in range(n_req):
+        prns = rng.choice(32, 8, replace=False)
+        hs = [ctx.code_put(gps[int(p)], 4000) for p in prns]
+        handles += hs
+        jobs.append(ctx.make_job(raw, L.SAMPLES_CI8, 4e6, 4000, 4, hs, 5000.0, 500.0))
+    cells = 8 * n_doppler(500.0) * 4000
+    for j in jobs[:5]:
+        ctx.acquire(j)
+    t0 = time.perf_counter()
+    for j in jobs[:50]:
+        ctx.acquire(j)
+    alone_ms = (time.perf_counter() - t0) / 50 * 1e3
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, n_req))
+    srv = api.Server(ctx, max_inflight=4, policy=L.SERVE_RESPONSE_RATIO)
+    t0 = time.perf_counter()
+    tickets, done_at, i = [], {}, 0
+    while len(done_at) < n_req:
+        now = time.perf_counter() - t0
+        while i < n_req and arrivals[i] <= now:
+            tickets.append(srv.submit(jobs[i]))
+            i += 1
+        for k, t in enumerate(tickets):
+            if k not in done_at and srv.poll(t) is not None:
+                done_at[k] = time.perf_counter() - t0
+        time.sleep(0.0002)
+    srv.close()
+    for h in handles:
+        ctx.code_release(h)
+    lat = np.array([done_at[k] - arrivals[k] for k in range(n_req)]) * 1e3
+    return {"workload": "GPS L1 C/A int8 4 MHz, 1 ms x 4 blocks, 8 PRNs, 21 Doppler bins (672,000 cells) per request",
+            "requests": n_req, "rate_req_s": rate, "p50_ms": float(np.percentile(lat, 50)),
+            "p99_ms": float(np.percentile(lat, 99)), "alone_ms": alone_ms,
+            "cells_s": n_req * cells / (max(done_at.values()) - arrivals[0])}
+
+
+def served_section():
+    """The served half of the metric beside the default line: the
+    configuration's request mix (a bounded prefix of the seeded Poisson
+    stream at 2000 req/s) served vs the same requests one after another
+    through ugsdr_acquire, and the short-job stream's latency."""
+    from argparse import Namespace
+    from ugsdr_gb300 import api
+    mix = run_served(Namespace(requests=8, rate=2000.0, inflight=4, policy="response_ratio"))
+    ctx = api.Context(0)
+    try:
+        short = run_short_stream(ctx)
+    finally:
+        ctx.close()
+    keep = ("value", "requests", "p50_ms", "p99_ms", "offered_load", "sequential_cells_s", "served_over_sequential",
+            "max_inflight_seen", "wall_s")
+    return {"mix": {k: mix[k] for k in keep}, "short_jobs": short,
+            "note": "p99 < 20 ms at 2000 req/s of the configuration's mix (mean 3.4e9 cells per request) would need "
+                    "~7e12 cells/s; the short-job stream shows the latency the server gives at a feasible load"}
 
 
 def run_served(args):
@@ -1220,6 +1291,7 @@ def main():
     ap.add_argument("--config", choices=sorted(WORKLOADS) + ["track", "jamming", "observables"], default="multi")
     ap.add_argument("--track-seconds", type=float, default=10.0, help="capture length of --config track")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-served", action="store_true", help="skip the served section of the default line")
     ap.add_argument("--served", action="store_true", help="run the served request stream instead")
     ap.add_argument("--requests", type=int, default=24, help="requests in the served stream")
     ap.add_argument("--inflight", type=int, default=4, help="server slots for the served stream")

@@ -505,7 +505,7 @@ int ugsdr_jamming_suppress(ugsdr_ctx* ctx, float* iq, size_t n, double fs, int s
 	ugsdr_jamming_detection* out, int cap, int* n_detections);
 
 /* ------------------------------------------------------------ serving */
-/* Continuous-batching acquisition server.  A worker thread admits queued jobs
+/* Continuous-batching acquisition and tracking server.  A worker thread admits queued jobs
  * into `max_inflight` slots, each with its own CUDA stream and scratch, as
  * soon as a slot is free and the job's device-memory estimate fits the
  * budget; admitted jobs run concurrently on the device while later requests
@@ -543,6 +543,17 @@ int ugsdr_server_create(ugsdr_ctx* ctx, const ugsdr_server_config* cfg, ugsdr_se
 /* Copies the job description (and the host samples) and returns a ticket;
  * UGSDR_E_QUEUE_FULL when queue_capacity requests are pending. */
 int ugsdr_server_submit(ugsdr_server* server, const ugsdr_acq_job* job, uint64_t* ticket);
+/* Tracking request: advances `bank` (created on the server's context) by
+ * n_epochs epochs of host samples (samples_per_epoch = the bank's rate / 1000;
+ * CF32, CI8, CI16 or RI8), copied at submit; n_epochs x n_channels outputs are
+ * written to `outputs` (host, kept valid by the caller until the ticket is
+ * polled done).  The bank's channels keep their loop and NCO state on the
+ * device between requests, as Tracker::Track keeps its TrackingParameters
+ * between epochs (src/tracking/tracker.hpp:186-197); a bank's requests run one
+ * at a time in submission order, interleaved with acquisition jobs on the
+ * other slots.  Poll the ticket with results = NULL. */
+int ugsdr_server_submit_track(ugsdr_server* server, ugsdr_track_bank* bank, const void* samples, int sample_type,
+	size_t samples_per_epoch, int n_epochs, ugsdr_track_output* outputs, uint64_t* ticket);
 /* Non-blocking: *done = 1 and results[n_codes] filled when the job finished
  * (the ticket is then retired), 0 while pending; a failed job returns its
  * error status (UGSDR_E_NOMEM when its estimate exceeds the budget). */

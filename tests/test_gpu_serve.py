@@ -116,3 +116,52 @@ def test_admission_order(ctx, golden_codes, policy):
     finally:
         for h in long_h + short_h:
             ctx.code_release(h)
+
+
+def test_tracking_requests_same_alone_and_in_mix(ctx, golden_codes):
+    """Tracking requests through the server (ugsdr_server_submit_track): a
+    bank advanced by three consecutive requests (its channels' state kept on
+    the device between them), interleaved with acquisition jobs on the other
+    slots, produces the same outputs, bit for bit, as the same bank run in
+    one call alone (Tracker::Track's epoch loop, tracker.hpp:186-197)."""
+    from ugsdr_gb300.api import TrackBank
+    ca = unpack_codes(golden_codes, "gps_l1ca")
+    codes = {p: ca[p] for p in range(8)}
+    n_ep = 90
+    raw, truth = signals.gps_l1_config(seed=23, codes=codes, fs=4e6, ms=n_ep, visible=3, cn0=(44, 50), max_doppler=3000,
+                                       sample_type="ci16")
+    chans = [dict(code=i, fs=4e6, code_frequency=1.023e6, code_phase=float(round(t["code_phase_samples"])),
+                  carrier_frequency=round(t["doppler"] / 50) * 50.0) for i, t in enumerate(truth)]
+    chips = [ca[t["prn"]] for t in truth]
+    alone_bank = TrackBank(ctx, chans, chips)
+    alone = alone_bank.run(raw, L.SAMPLES_CI16, n_ep)
+    alone_bank.close()
+    jobs, handles = make_jobs(ctx, golden_codes)
+    try:
+        acq_alone = [ctx.acquire(j) for j in jobs]
+        bank = TrackBank(ctx, chans, chips)
+        srv = Server(ctx, max_inflight=4)
+        tickets = []
+        for s in range(3):
+            tickets.append(("acq", s, srv.submit(jobs[s])))
+            tickets.append(("trk", s, srv.submit_track(bank, raw[s * 30 * 4000:(s + 1) * 30 * 4000], L.SAMPLES_CI16, 30)))
+            tickets.append(("acq", s + 3, srv.submit(jobs[s + 3])))
+        srv.drain()
+        parts = {}
+        for kind, idx, t in tickets:
+            out = srv.poll(t)
+            assert out is not None
+            if kind == "trk":
+                parts[idx] = out
+            else:
+                for a, b in zip(acq_alone[idx], out):
+                    assert (a.index, a.doppler_bin, a.level) == (b.index, b.doppler_bin, b.level)
+        served = np.concatenate([parts[0], parts[1], parts[2]])
+        assert served.tobytes() == alone.tobytes()
+        assert srv.stats()["completed"] == 9
+        srv.close()
+        bank.close()
+    finally:
+        for hs in handles:
+            for h in hs:
+                ctx.code_release(h)

@@ -188,6 +188,7 @@ SIGNATURES = {
     "ugsdr_jamming_suppress": (_i, [_vp, _vp, _sz, _d, _i, C.POINTER(JammingDetection), _i, C.POINTER(_i)]),
     "ugsdr_server_create": (_i, [_vp, C.POINTER(ServerConfig), C.POINTER(_vp)]),
     "ugsdr_server_submit": (_i, [_vp, C.POINTER(AcqJob), C.POINTER(_u64)]),
+    "ugsdr_server_submit_track": (_i, [_vp, _vp, _vp, _i, C.c_size_t, _i, _vp, C.POINTER(_u64)]),
     "ugsdr_server_poll": (_i, [_vp, _u64, C.POINTER(AcqResult), C.POINTER(_i)]),
     "ugsdr_server_drain": (_i, [_vp]),
     "ugsdr_server_destroy": (_i, [_vp]),

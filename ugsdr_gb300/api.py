@@ -498,7 +498,7 @@ def observables(ctx: Context, outputs, channels: list[dict], shape=None, out_ptr
 
 
 class Server:
-    """Continuous-batching acquisition server (ugsdr_server_*)."""
+    """Continuous-batching acquisition and tracking server (ugsdr_server_*)."""
 
     def __init__(self, ctx: Context, max_inflight: int = 4, memory_budget: int = 0, queue_capacity: int = 1024,
                  policy: int = L.SERVE_FIFO):
@@ -508,6 +508,7 @@ class Server:
         ctx._check(ctx.lib.ugsdr_server_create(ctx.h, C.byref(cfg), C.byref(h)))
         self.h = h
         self._n_codes: dict[int, int] = {}
+        self._tracks: dict[int, np.ndarray] = {}
 
     def submit(self, job: Job) -> int:
         t = C.c_uint64()
@@ -515,8 +516,26 @@ class Server:
         self._n_codes[t.value] = job.c.n_codes
         return t.value
 
+    def submit_track(self, bank: "TrackBank", samples: np.ndarray, sample_type: int, n_epochs: int) -> int:
+        """A tracking run of `bank` over n_epochs epochs of host samples; poll
+        returns its outputs (n_epochs x n_channels records)."""
+        arr = np.ascontiguousarray(samples)
+        out = np.zeros((n_epochs, bank.n), dtype=TRACK_DTYPE)
+        t = C.c_uint64()
+        self.ctx._check(self.ctx.lib.ugsdr_server_submit_track(self.h, bank.h, _ptr(arr), sample_type, bank.spm, n_epochs,
+                                                               _ptr(out), C.byref(t)))
+        self._tracks[t.value] = out
+        return t.value
+
     def poll(self, ticket: int):
-        """None while pending, else the per-code results (the ticket is retired)."""
+        """None while pending, else the per-code results, or for a tracking
+        request its outputs (the ticket is retired)."""
+        if ticket in self._tracks:
+            done = C.c_int()
+            self.ctx._check(self.ctx.lib.ugsdr_server_poll(self.h, ticket, None, C.byref(done)))
+            if not done.value:
+                return None
+            return self._tracks.pop(ticket)
         n = self._n_codes[ticket]
         res = (L.AcqResult * n)()
         done = C.c_int()

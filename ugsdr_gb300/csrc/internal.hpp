@@ -98,6 +98,11 @@ namespace ugsdr_gpu {
 
 	// Device scratch of one in-flight batch of acquisition jobs (grow-only).
 	// The context owns one; each serving slot owns its own so batches overlap.
+	// tracking banks for the server (track.cu)
+	void track_bank_shape(const ugsdr_track_bank* bank, ugsdr_ctx** ctx, int* n_channels, size_t* spm, double* fs);
+	void track_enqueue_on(ugsdr_track_bank* bank, const void* dev_samples, int sample_type, int n_epochs,
+		ugsdr_track_output* dev_out, cudaStream_t stream);
+
 	struct Workspace {
 		DevBuf samples;    // staged host samples
 		DevBuf spectra;    // forward spectra X[d][b][N]

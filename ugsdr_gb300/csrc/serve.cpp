@@ -1,4 +1,4 @@
-// Continuous-batching acquisition server (ugsdr_server_*).
+// Continuous-batching acquisition and tracking server (ugsdr_server_*).
 //
 // `max_inflight` slots, each with two CUDA streams (normal and highest
 // priority), its own scratch workspace and pinned host staging.  Requests
@@ -12,7 +12,9 @@
 // Admitted searches therefore overlap on the device while new requests keep
 // arriving, and completions are seen while long searches are still being
 // launched.  Code spectra are the context's resident cache, shared by every
-// request.
+// request.  Tracking requests advance a bank (its channels' loop and NCO
+// state stay on the device between requests); a bank's requests are admitted
+// one at a time, in submission order.
 #include "internal.hpp"
 
 #include <chrono>
@@ -22,6 +24,7 @@
 #include <cstring>
 #include <deque>
 #include <list>
+#include <set>
 #include <thread>
 
 using namespace ugsdr_gpu;
@@ -58,8 +61,17 @@ namespace {
 		}
 	};
 
+	// tracking work per second, in the acquisition estimate's units (cell-blocks):
+	// channel-samples count a tenth of a cell-block each
+	constexpr double kTrackWorkPerChannelSample = 0.1;
+
 	struct Request {
 		uint64_t ticket = 0;
+		int kind = 0;               // 0 acquisition job, 1 tracking run of `bank`
+		ugsdr_track_bank* bank = nullptr;
+		int n_epochs = 0, track_type = 0;
+		ugsdr_track_output* outputs = nullptr;  // caller's host array (tracking)
+		size_t sample_bytes = 0, out_bytes = 0;
 		ugsdr_acq_job job{};
 		std::vector<int> codes;
 		std::vector<char> samples;  // host copy (empty for device-resident samples)
@@ -113,19 +125,40 @@ struct ugsdr_server {
 	bool trace = std::getenv("UGSDR_SERVER_TRACE") != nullptr;
 	std::chrono::steady_clock::time_point created = std::chrono::steady_clock::now();
 	double since() const { return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - created).count(); }
+	std::set<ugsdr_track_bank*> busy_banks;  // banks with a request on the device
+
+	// a tracking request may start only when its bank is idle and no earlier
+	// request of the bank is still pending
+	bool eligible(std::deque<Request*>::iterator it) {
+		const Request* r = *it;
+		if (r->kind == 0)
+			return true;
+		if (busy_banks.count(r->bank))
+			return false;
+		for (auto j = pending.begin(); j != it; ++j)
+			if ((*j)->kind == 1 && (*j)->bank == r->bank)
+				return false;
+		return true;
+	}
 
 	// measured cell-blocks per second (a first guess until work has completed)
 	double rate() const { return stats.busy_seconds > 0.05 && done_work > 0 ? done_work / stats.busy_seconds : 5e10; }
 
 	// the pending request to admit next under cfg.policy
 	std::deque<Request*>::iterator pick() {
-		if (cfg.policy != UGSDR_SERVE_RESPONSE_RATIO || pending.size() < 2)
-			return pending.begin();
+		if (cfg.policy != UGSDR_SERVE_RESPONSE_RATIO || pending.size() < 2) {
+			for (auto it = pending.begin(); it != pending.end(); ++it)
+				if (eligible(it))
+					return it;
+			return pending.end();
+		}
 		const double rate = this->rate();
 		const auto now = std::chrono::steady_clock::now();
-		auto best = pending.begin();
+		auto best = pending.end();
 		double best_ratio = -1;
 		for (auto it = pending.begin(); it != pending.end(); ++it) {
+			if (!eligible(it))
+				continue;
 			const double service = std::max((*it)->work / rate, 1e-4);
 			const double wait = std::chrono::duration<double>(now - (*it)->queued).count();
 			const double ratio = (wait + service) / service;
@@ -170,6 +203,17 @@ struct ugsdr_server {
 			if (q != cudaSuccess) {
 				cudaGetLastError();
 				fail(r, UGSDR_E_CUDA, cudaGetErrorString(q));
+				if (r->kind == 1)
+					busy_banks.erase(r->bank);
+				continue;
+			}
+			if (r->kind == 1) {
+				std::memcpy(r->outputs, sl.cells.ptr, r->out_bytes);
+				busy_banks.erase(r->bank);
+				r->done = true;
+				done_work += r->work;
+				++stats.completed;
+				cv_done.notify_all();
 				continue;
 			}
 			r->results.resize(r->job.n_codes);
@@ -201,6 +245,8 @@ struct ugsdr_server {
 		if (!free_slot)
 			return false;
 		const auto pos = pick();
+		if (pos == pending.end())
+			return false;  // only tracking requests whose bank is busy
 		Request* r = *pos;
 		const size_t grow = r->estimate > free_slot->ws.reserved() ? r->estimate - free_slot->ws.reserved() : 0;
 		if (held() + grow > budget) {
@@ -227,10 +273,32 @@ struct ugsdr_server {
 		++stats.inflight;
 		stats.max_inflight_seen = std::max(stats.max_inflight_seen, stats.inflight);
 		const bool urgent = cfg.policy == UGSDR_SERVE_RESPONSE_RATIO && r->work / rate() < kUrgentSeconds;
+		if (r->kind == 1)
+			busy_banks.insert(r->bank);
 		lock.unlock();
 		int fail_status = UGSDR_OK;
 		std::string fail_msg;
 		try {
+			if (r->kind == 1) {
+				// tracking: samples in through the slot's pinned and device
+				// buffers, the bank's run, outputs back to pinned staging
+				std::lock_guard<std::mutex> ctx_lock(ctx->mutex);
+				free_slot->active = free_slot->stream;
+				free_slot->ws.set_stream(free_slot->active);
+				free_slot->samples.reserve(r->sample_bytes);
+				std::memcpy(free_slot->samples.ptr, r->samples.data(), r->sample_bytes);
+				free_slot->ws.samples.reserve(r->sample_bytes);
+				free_slot->ws.cells.reserve(r->out_bytes);
+				free_slot->cells.reserve(r->out_bytes);
+				UG_CUDA(cudaMemcpyAsync(free_slot->ws.samples.ptr, free_slot->samples.ptr, r->sample_bytes, cudaMemcpyHostToDevice,
+					free_slot->active));
+				track_enqueue_on(r->bank, free_slot->ws.samples.ptr, r->track_type, r->n_epochs,
+					free_slot->ws.cells.as<ugsdr_track_output>(), free_slot->active);
+				UG_CUDA(cudaMemcpyAsync(free_slot->cells.ptr, free_slot->ws.cells.ptr, r->out_bytes, cudaMemcpyDeviceToHost,
+					free_slot->active));
+				UG_CUDA(cudaEventRecord(free_slot->event, free_slot->active));
+			}
+			else {
 			ugsdr_acq_job job = r->job;
 			job.codes = r->codes.data();
 			if (!job.samples_on_device) {
@@ -256,6 +324,7 @@ struct ugsdr_server {
 						static_cast<unsigned long long>(r->ticket), r->work, urgent ? 1 : 0, since() - t_admit);
 			}
 			r->job.codes = r->codes.data();
+			}
 		}
 		catch (const Error& e) {
 			fail_status = e.status;
@@ -268,6 +337,8 @@ struct ugsdr_server {
 		lock.lock();
 		free_slot->enqueuing = false;
 		if (fail_status != UGSDR_OK) {
+			if (r->kind == 1)
+				busy_banks.erase(r->bank);
 			free_slot->req = nullptr;
 			if (--stats.inflight == 0)
 				stats.busy_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - busy_since).count();
@@ -371,6 +442,51 @@ int ugsdr_server_submit(ugsdr_server* server, const ugsdr_acq_job* job, uint64_t
 		r->estimate = jobs_device_bytes(ctx, &r->job, 1);  // validates the job too
 		r->work = static_cast<double>(r->job.n_codes) * doppler_grid(r->job.doppler_range, r->job.doppler_step).size() *
 			static_cast<double>(r->job.block_samples) * static_cast<double>(r->job.n_blocks);
+	});
+	if (st != UGSDR_OK)
+		return st;
+	std::lock_guard<std::mutex> lock(server->mu);
+	if (static_cast<int>(server->pending.size()) >= server->cfg.queue_capacity) {
+		ctx->last_error = "serving queue is full";
+		return UGSDR_E_QUEUE_FULL;
+	}
+	r->ticket = server->next_ticket++;
+	r->queued = std::chrono::steady_clock::now();
+	*ticket = r->ticket;
+	server->pending.push_back(r.get());
+	server->requests[r->ticket] = std::move(r);
+	++server->stats.submitted;
+	server->cv_work.notify_one();
+	return UGSDR_OK;
+}
+
+int ugsdr_server_submit_track(ugsdr_server* server, ugsdr_track_bank* bank, const void* samples, int sample_type,
+	size_t samples_per_epoch, int n_epochs, ugsdr_track_output* outputs, uint64_t* ticket) {
+	if (!server || !bank || !ticket)
+		return UGSDR_E_INVALID;
+	ugsdr_ctx* ctx = server->ctx;
+	auto r = std::make_unique<Request>();
+	const int st = guarded(ctx, [&] {
+		ugsdr_ctx* bank_ctx = nullptr;
+		int n_ch = 0;
+		size_t spm = 0;
+		double fs = 0;
+		track_bank_shape(bank, &bank_ctx, &n_ch, &spm, &fs);
+		require(bank_ctx == ctx, "the bank belongs to another context");
+		require(samples && outputs && n_epochs > 0, "null samples or outputs, or no epochs");
+		require(samples_per_epoch == spm, "samples_per_epoch must be the bank's sampling_rate / 1000");
+		require(sample_type >= UGSDR_SAMPLES_CF32 && sample_type <= UGSDR_SAMPLES_RI8,
+			"served tracking takes CF32, CI8, CI16 or RI8 samples");
+		r->kind = 1;
+		r->bank = bank;
+		r->n_epochs = n_epochs;
+		r->track_type = sample_type;
+		r->outputs = outputs;
+		r->sample_bytes = sample_size(sample_type) * spm * static_cast<size_t>(n_epochs);
+		r->out_bytes = sizeof(ugsdr_track_output) * static_cast<size_t>(n_ch) * n_epochs;
+		r->samples.assign(static_cast<const char*>(samples), static_cast<const char*>(samples) + r->sample_bytes);
+		r->estimate = (r->sample_bytes + 255) / 256 * 256 + (r->out_bytes + 255) / 256 * 256;
+		r->work = kTrackWorkPerChannelSample * static_cast<double>(n_ch) * static_cast<double>(spm) * n_epochs;
 	});
 	if (st != UGSDR_OK)
 		return st;

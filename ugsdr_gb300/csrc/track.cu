@@ -608,6 +608,32 @@ namespace {
 	}
 }
 
+namespace ugsdr_gpu {
+	void track_bank_shape(const ugsdr_track_bank* bank, ugsdr_ctx** ctx, int* n_channels, size_t* spm, double* fs) {
+		*ctx = bank->ctx;
+		*n_channels = bank->n_channels;
+		*spm = bank->spm;
+		*fs = bank->fs;
+	}
+
+	// The serving path: n_epochs of device samples on `stream` (the caller
+	// holds the context lock), outputs to device memory.
+	void track_enqueue_on(ugsdr_track_bank* bank, const void* dev_samples, int sample_type, int n_epochs,
+		ugsdr_track_output* dev_out, cudaStream_t stream) {
+		ugsdr_ctx* ctx = bank->ctx;
+		const cudaStream_t saved = ctx->stream;
+		ctx->stream = stream;
+		try {
+			track_enqueue(bank, dev_samples, sample_type, 1, bank->spm, n_epochs, reinterpret_cast<TrackOut*>(dev_out));
+		}
+		catch (...) {
+			ctx->stream = saved;
+			throw;
+		}
+		ctx->stream = saved;
+	}
+}
+
 extern "C" {
 
 int ugsdr_track_create(ugsdr_ctx* ctx, const ugsdr_track_config* cfg, const ugsdr_track_channel* channels, int n_channels,
