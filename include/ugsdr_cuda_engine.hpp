@@ -108,6 +108,9 @@ namespace ugsdr {
 
 			ugsdr_ctx* Context() const { return ctx_; }
 
+			// the capture a later Process() reads (code spectra stay cached)
+			void SetSubbands(std::vector<Subband> subbands) { subbands_ = std::move(subbands); }
+
 			// FastSearchEngineBase::AdjustSamplingRate (fse.hpp:222-240): the
 			// divisor of the rate with whole kHz closest to the target, or the
 			// signal's own rate when the search runs out of candidates

@@ -15,6 +15,7 @@
 #pragma once
 
 #include "ugsdr_cuda.h"
+#include "ugsdr_cuda_engine.hpp"
 
 #ifndef UGSDR_REF_SRC
 #define UGSDR_REF_SRC ..
@@ -316,6 +317,64 @@ namespace ugsdr {
 	private:
 		double fs = 0.0;
 		std::vector<DetectionResult> results;
+	};
+
+	// FastSearchEngineBase's call surface (fse.hpp:450-507) over the batched
+	// engine: constructed on the reference's DigitalFrontend with the Doppler
+	// range and step, Process() reads the same 4 ms (GetSeveralEpochs) and
+	// returns the reference's AcquisitionResult<T> sorted by Sv.  The GPS L1
+	// C/A, L5I/L5Q, GLONASS L1OF and Galileo E1B subbands the frontend has are
+	// searched (the systems cuda::CudaFastSearchEngine covers); unlike the
+	// per-op Cuda* policies inside FastSearchEngineBase, every search of a call
+	// goes to the GPU in one ugsdr_acquire_batch.
+	template <ChannelConfigConcept ChConfig = DefaultChannelConfig, typename T = float>
+	class CudaFastSearchEngineFor {
+	public:
+		CudaFastSearchEngineFor(DigitalFrontend<ChConfig, T>& dfe, double range, double step,
+			double acquisition_sampling_rate = 8192000.0, int device = 0)
+			: digital_frontend(dfe), engine({}, range, step, acquisition_sampling_rate, device) {}
+
+		std::vector<AcquisitionResult<T>> Process(bool plot_results = false, std::size_t ms_offset = 0) {
+			(void)plot_results;
+			auto& epoch = digital_frontend.GetSeveralEpochs(ms_offset, cuda::CudaFastSearchEngine::ms_to_process);
+			const std::pair<Signal, int> signals[] = {{Signal::GpsCoarseAcquisition_L1, UGSDR_GPS_L1CA}, {Signal::Gps_L5I, UGSDR_GPS_L5I},
+				{Signal::Gps_L5Q, UGSDR_GPS_L5Q}, {Signal::GlonassCivilFdma_L1, UGSDR_GLONASS_L1OF}, {Signal::Galileo_E1b, UGSDR_GALILEO_E1B}};
+			std::vector<std::vector<std::complex<float>>> buffers;
+			std::vector<cuda::Subband> subbands;
+			for (const auto& [sig, id] : signals) {
+				if (!digital_frontend.HasSignal(sig))
+					continue;
+				buffers.push_back(cuda_detail::ToF(epoch.GetSubband(sig)));
+				cuda::Subband s;
+				s.signal = id;
+				s.samples = buffers.back().data();
+				s.sample_type = UGSDR_SAMPLES_CF32;
+				s.n_samples = buffers.back().size();
+				s.sampling_rate = digital_frontend.GetSamplingRate(sig);
+				s.central_frequency = digital_frontend.GetCentralFrequency(sig);
+				subbands.push_back(s);
+			}
+			engine.SetSubbands(subbands);
+			const auto found = engine.Process(false, 0);
+			std::vector<AcquisitionResult<T>> dst;
+			for (const auto& r : found) {
+				AcquisitionResult<T> a;
+				a.sv_number.id = r.sv_number.id;
+				a.sv_number.system = static_cast<System>(r.sv_number.system);
+				a.sv_number.signal = static_cast<Signal>(r.sv_number.signal);
+				a.doppler = r.doppler;
+				a.code_offset = r.code_offset;
+				a.level = r.level;
+				a.sigma = r.sigma;
+				a.intermediate_frequency = r.intermediate_frequency;
+				dst.push_back(std::move(a));
+			}
+			return dst;
+		}
+
+	private:
+		DigitalFrontend<ChConfig, T>& digital_frontend;
+		cuda::CudaFastSearchEngine engine;
 	};
 
 	// FseConfig bundle (fse.hpp:36-67, 98-109) on the GPU policies

@@ -10,6 +10,9 @@
 
 using Fse = ugsdr::FastSearchEngineBase<ugsdr::ParametricCudaFseConfig<8192000>, ugsdr::DefaultChannelConfig, float>;
 auto instantiate_process = &Fse::Process;
+// the batched engine on the reference's DigitalFrontend, same call shape
+using BatchedFse = ugsdr::CudaFastSearchEngineFor<ugsdr::DefaultChannelConfig, float>;
+auto instantiate_batched = &BatchedFse::Process;
 
 int main() {
 	// correlator KAT (basic_tests.cpp:72-86) and mixer KAT (321-357) through the policies
@@ -58,5 +61,5 @@ int main() {
 	bad |= cols.size() != (jam.size() - 96) / 32 || back.size() != 128 + (cols.size() - 1) * 32;
 	std::printf("%s correlate=(%g,%g) mf0=%g jamming=%zu worst=%g\n", bad ? "FAIL" : "ok", dst.real(), dst.imag(),
 		mf[0].real(), gd.size(), worst);
-	return bad || instantiate_process == nullptr;
+	return bad || instantiate_process == nullptr || instantiate_batched == nullptr;
 }
