@@ -260,7 +260,7 @@ namespace ugsdr_gpu {
 		template <class F>
 		size_t smem_inv_rows(const BatchedParams& p) {
 			return rows_tiles<F>() * sizeof(float2) * static_cast<size_t>(p.rw) * p.n2 + sizeof(float2) * p.n2 + 16 +
-				sizeof(float2) * static_cast<size_t>(p.rw) * (F::kLastNS + 1);  // twiddle seeds (hooked plans)
+				(F::kHooked ? sizeof(float2) * static_cast<size_t>(p.rw) * (F::kLastNS + 1) : 0);  // twiddle seeds
 		}
 
 		int chunks_of(int total, int per) { return (total + per - 1) / per; }

@@ -466,7 +466,10 @@ namespace ugsdr_gpu {
 							__dmul_rn(p.k2_dll, ce)), dll_scale));
 						ls.code_error = ce;
 						ls.code_freq = __dsub_rn(base_freq, ls.code_nco);
-						ls.code_phase = __dsub_rn(ls.code_phase, __dmul_rn(p.fs / 1000 / 2, __dsub_rn(__ddiv_rn(ls.code_freq, base_freq), 1.0)));
+						// code_freq / base as the reference divides it (nco_mode 1), by the
+						// reciprocal otherwise (one FP64 division less on the epoch's serial path)
+						const double ratio = p.nco_mode == 1 ? __ddiv_rn(ls.code_freq, base_freq) : __dmul_rn(ls.code_freq, inv_base);
+						ls.code_phase = __dsub_rn(ls.code_phase, __dmul_rn(p.fs / 1000 / 2, __dsub_rn(ratio, 1.0)));
 						if (p.out) {
 							TrackOut o;
 							for (int t = 0; t < 5; ++t) {
