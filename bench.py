@@ -294,6 +294,23 @@ def run_ours(args, world, rank):
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{dev}")  # > L2 (129 MB)
     cells = sum(job_cells(j) for j in jobs)
 
+    # four-step tile shapes: measured by the autotuner on this workload's jobs
+    # (Doppler grids cut), before the warm-up and outside the timed region
+    t0 = time.perf_counter()
+    tried = [] if args.no_tune else ctx.autotune(dev_jobs)
+    tune_s = time.perf_counter() - t0
+    tiles = {}
+    for n in sorted({j["n"] for j in jobs if j["n"] > 12000}):
+        t = ctx.tile_shape(n)
+        rule_ms = next((x["ms"] for x in tried if x["block_samples"] == n), None)
+        kept_ms = next((x["ms"] for x in tried if x["block_samples"] == n and
+                        (x["n1"], x["cols"], x["rows"], x["warp_cols"]) == (t["n1"], t["cols"], t["rows"], t["warp_cols"])),
+                       None)
+        tiles[str(n)] = {"split": f"{t['n1']}x{n // t['n1']}", "cols": t["cols"], "rows": t["rows"],
+                         "column_kernel": "warp-owned" if t["warp_cols"] else "tile",
+                         "shapes_timed": sum(1 for x in tried if x["block_samples"] == n),
+                         "rule_ms": rule_ms, "kept_ms": kept_ms}
+
     for _ in range(args.warmup):
         ctx.acquire_batch(dev_jobs)
     torch.cuda.synchronize()
@@ -369,7 +386,10 @@ def run_ours(args, world, rank):
         "data": "synthetic (seeded int16/int8 I/Q captures; Galileo E1B chips from the reference's code tables)",
         "config": {"workload": WORKLOAD_DESC[args.config],
                    "cells_per_step": cells, "jobs_per_step": len(jobs), "parallelism": f"replicas x{world}",
-                   "l2": "flushed between steps (256 MB write); working set > L2"},
+                   "l2": "flushed between steps (256 MB write); working set > L2",
+                   "tiles": {"chosen_by": "rule (--no-tune)" if args.no_tune else
+                             f"ugsdr_autotune ({len(tried)} shapes timed in {tune_s:.1f} s before the warm-up)",
+                             **tiles}},
         "e2e": {"value": world * cells / t_e2e, "unit": "cells/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": t_e2e * 1e3},
         "gpu_launches": launches,
@@ -1292,6 +1312,7 @@ def main():
     ap.add_argument("--track-seconds", type=float, default=10.0, help="capture length of --config track")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-served", action="store_true", help="skip the served section of the default line")
+    ap.add_argument("--no-tune", action="store_true", help="keep the built-in tile rule (skip ugsdr_autotune)")
     ap.add_argument("--served", action="store_true", help="run the served request stream instead")
     ap.add_argument("--requests", type=int, default=24, help="requests in the served stream")
     ap.add_argument("--inflight", type=int, default=4, help="server slots for the served stream")

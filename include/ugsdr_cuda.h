@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define UGSDR_CUDA_ABI_VERSION 7
+#define UGSDR_CUDA_ABI_VERSION 8
 
 enum ugsdr_status {
 	UGSDR_OK = 0,
@@ -215,6 +215,42 @@ int ugsdr_acquire(ugsdr_ctx* ctx, const ugsdr_acq_job* job, ugsdr_acq_result* re
 int ugsdr_acquire_batch(ugsdr_ctx* ctx, const ugsdr_acq_job* jobs, int n_jobs, ugsdr_acq_result* const* results);
 /* Number of Doppler bins the reference loop visits for (range, step). */
 int ugsdr_doppler_bins(double range, double step, uint32_t* n);
+
+/* ------------------------------------------------ four-step tile shapes */
+/* No counterpart in the reference (FFTW plans its own transforms): block
+ * sizes above the single-CTA limit run as N = n1 x (N / n1) four-step
+ * transforms, and these calls read, pin or tune the shape of one size.
+ * A shape changes the kernels' tiling and, through n1, the order of the
+ * float sums: results agree with another shape's within float rounding,
+ * and peaks and Doppler bins are the same on any signal above threshold. */
+typedef struct ugsdr_tile_shape {
+	int n1;          /* split (0 in ugsdr_tile_set: the built-in rule, the largest n1 <= sqrt N that fits) */
+	int cols;        /* columns per column-kernel CTA: 1, 2, 4 or 8 (0: rule) */
+	int rows;        /* rows per row-kernel CTA: 1, 2, 4 or 8 (0: rule) */
+	int warp_cols;   /* 1: warp-owned column kernel where one is compiled for the split, 0: one tile of
+	                    `cols` columns per CTA, -1: rule (the warp-owned kernel where compiled) */
+	int block_samples; /* N the shape is for (filled by ugsdr_tile_get / ugsdr_autotune, ignored by ugsdr_tile_set) */
+	double ms;       /* ugsdr_autotune: device time of the tuning search with this shape */
+} ugsdr_tile_shape;
+/* The shape block_samples runs with now (every field resolved). */
+int ugsdr_tile_get(ugsdr_ctx* ctx, size_t block_samples, ugsdr_tile_shape* shape);
+/* Pins block_samples' shape (NULL: back to the rule), e.g. one an earlier
+ * ugsdr_autotune chose; a shape outside the kernels' shared-memory or launch
+ * limits returns UGSDR_E_UNSUPPORTED and leaves the old one.  A new n1
+ * rebuilds the context's cached code spectra of that size: call it while no
+ * search of that size is in flight. */
+int ugsdr_tile_set(ugsdr_ctx* ctx, size_t block_samples, const ugsdr_tile_shape* shape);
+/* Autotuner: for every block size above the single-CTA limit among `jobs`,
+ * runs those jobs (Doppler grids cut to about 4e9 complex points per search)
+ * with candidate shapes and keeps the fastest: the split (the rule's, the
+ * next smaller divisor, the rule's transposed), then the column kernel and
+ * its width, then the rows per row CTA, each stage from the best so far; the
+ * rule's shape stays unless another is 1.5 % faster.  Each candidate runs
+ * once untimed and twice timed with CUDA events (the best counts).  tried
+ * receives up to max_tried measured shapes, n_tried (may be NULL) their
+ * number.  Same caveat as ugsdr_tile_set for in-flight searches. */
+int ugsdr_autotune(ugsdr_ctx* ctx, const ugsdr_acq_job* jobs, int n_jobs, ugsdr_tile_shape* tried, int max_tried,
+	int* n_tried);
 
 /* ------------------------------------------- allocation-free acquisition */
 /* No counterpart in the reference: an extra entry point of this library.

@@ -10,7 +10,7 @@ from pathlib import Path
 
 LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libugsdr_cuda.so"
 
-ABI_VERSION = 7  # UGSDR_CUDA_ABI_VERSION the structs below mirror
+ABI_VERSION = 8  # UGSDR_CUDA_ABI_VERSION the structs below mirror
 
 OK = 0
 E_INVALID = -1
@@ -70,6 +70,11 @@ class AcqResult(C.Structure):
 
 class AcqCell(C.Structure):
     _fields_ = [("level", C.c_float), ("index", C.c_uint32), ("mean", C.c_float), ("std", C.c_float)]
+
+
+class TileShape(C.Structure):
+    _fields_ = [("n1", C.c_int), ("cols", C.c_int), ("rows", C.c_int), ("warp_cols", C.c_int), ("block_samples", C.c_int),
+                ("ms", C.c_double)]
 
 
 class TrackChannel(C.Structure):
@@ -159,6 +164,9 @@ SIGNATURES = {
     "ugsdr_acquire": (_i, [_vp, C.POINTER(AcqJob), C.POINTER(AcqResult), C.POINTER(AcqCell)]),
     "ugsdr_acquire_batch": (_i, [_vp, C.POINTER(AcqJob), _i, C.POINTER(C.POINTER(AcqResult))]),
     "ugsdr_doppler_bins": (_i, [_d, _d, C.POINTER(_u32)]),
+    "ugsdr_tile_get": (_i, [_vp, _sz, C.POINTER(TileShape)]),
+    "ugsdr_tile_set": (_i, [_vp, _sz, C.POINTER(TileShape)]),
+    "ugsdr_autotune": (_i, [_vp, C.POINTER(AcqJob), _i, C.POINTER(TileShape), _i, C.POINTER(_i)]),
     "ugsdr_mix": (_i, [_vp, _vp, _sz, _d, _d, _d]),
     "ugsdr_dft": (_i, [_vp, _vp, _vp, _sz, _i]),
     "ugsdr_matched_filter_prepare": (_i, [_vp, _vp, _sz, _i, _vp]),

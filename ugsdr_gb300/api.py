@@ -134,6 +134,34 @@ class Context:
         self._check(self.lib.ugsdr_acquire_batch(self.h, arr, len(jobs), ptrs))
         return [[AcqResult.from_c(x) for x in r] for r in res]
 
+    # ----------------------------------------------- four-step tile shapes
+    @staticmethod
+    def _shape_dict(t: L.TileShape) -> dict:
+        return dict(block_samples=t.block_samples, n1=t.n1, cols=t.cols, rows=t.rows, warp_cols=t.warp_cols, ms=t.ms)
+
+    def tile_shape(self, block_samples: int) -> dict:
+        """The four-step shape block_samples runs with (ugsdr_tile_get)."""
+        t = L.TileShape()
+        self._check(self.lib.ugsdr_tile_get(self.h, block_samples, C.byref(t)))
+        return self._shape_dict(t)
+
+    def set_tile_shape(self, block_samples: int, shape: dict | None) -> None:
+        """Pins a shape (a dict as tile_shape / autotune return; None: the rule)."""
+        if shape is None:
+            self._check(self.lib.ugsdr_tile_set(self.h, block_samples, None))
+            return
+        t = L.TileShape(shape.get("n1", 0), shape.get("cols", 0), shape.get("rows", 0), shape.get("warp_cols", -1), block_samples, 0.0)
+        self._check(self.lib.ugsdr_tile_set(self.h, block_samples, C.byref(t)))
+
+    def autotune(self, jobs: list["Job"], max_tried: int = 64) -> list[dict]:
+        """ugsdr_autotune over the jobs' large block sizes; returns every
+        measured shape with its block size and device time."""
+        arr = (L.AcqJob * len(jobs))(*[j.c for j in jobs])
+        tried = (L.TileShape * max_tried)()
+        n = C.c_int()
+        self._check(self.lib.ugsdr_autotune(self.h, arr, len(jobs), tried, max_tried, C.byref(n)))
+        return [self._shape_dict(t) for t in tried[:min(n.value, max_tried)]]
+
     def samples_in(self, sample_type: int, fs: float, nbytes: int) -> int:
         """Samples held by `nbytes` bytes of a capture (BBP DDC: whole epochs)."""
         if sample_type == L.SAMPLES_BBP_DDC:

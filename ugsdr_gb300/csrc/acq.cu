@@ -13,6 +13,7 @@
 #include <cstring>
 #include <functional>
 #include <numeric>
+#include <tuple>
 #include <vector>
 
 namespace ugsdr_gpu {
@@ -100,32 +101,42 @@ namespace ugsdr_gpu {
 		int n = 0, k = 0, m = 0, rows = 0, fold_mode = 0;
 	};
 
+	namespace {
+		// N = a x (n / a) with plans for both factors whose kernels' tiles and
+		// twiddle tables fit with at least min_cols columns (inverse: 3 tiles +
+		// accumulator) and one row (2 tiles)
+		bool split_fits(ugsdr_ctx* ctx, int n, int a, int min_cols) {
+			std::vector<int> r;
+			if (a < 2 || n % a || n / a < 2 || !plan_radices(a, r) || !plan_radices(n / a, r))
+				return false;
+			const size_t budget = ctx->smem_optin - 2048;
+			const size_t cols = (3 * sizeof(float2) + sizeof(float)) * min_cols * static_cast<size_t>(a | 1) + sizeof(float2) * a + 16;
+			const size_t rows = 3 * sizeof(float2) * static_cast<size_t>(n / a) + 16;
+			return cols <= budget && rows <= budget;
+		}
+	}
+
+	// The built-in split: the largest N1 <= sqrt(N) that fits with 4 columns
+	// per CTA; the largest sizes (beyond ~1.8e7 points) fall back to single
+	// columns.
+	int rule_split(ugsdr_ctx* ctx, int n) {
+		for (const int min_cols : {4, 1}) {
+			int best1 = 0;
+			for (int a = 2; static_cast<long>(a) * a <= n; ++a)
+				if (split_fits(ctx, n, a, min_cols))
+					best1 = a;  // increasing a -> closest to sqrt(n) last
+			if (best1 > 0)
+				return best1;
+		}
+		return 0;
+	}
+
 	const LargePlan& get_large_plan(ugsdr_ctx* ctx, int n) {
 		auto it = ctx->large_plans.find(n);
 		if (it != ctx->large_plans.end())
 			return it->second;
-		const size_t budget = ctx->smem_optin - 2048;
-		int best1 = 0;
-		std::vector<int> r;
-		// both kernels' tiles and twiddle tables must fit with at least
-		// 4 columns (inverse: 3 tiles + accumulator) and 1 row (2 tiles); the
-		// largest sizes (beyond ~1.8e7 points) fall back to single columns
-		for (const int min_cols : {4, 1}) {
-			for (int a = 2; static_cast<long>(a) * a <= n; ++a) {
-				if (n % a)
-					continue;
-				const int b = n / a;
-				if (!plan_radices(a, r) || !plan_radices(b, r))
-					continue;
-				const size_t cols = (3 * sizeof(float2) + sizeof(float)) * min_cols * static_cast<size_t>(a | 1) + sizeof(float2) * a + 16;
-				const size_t rows = 3 * sizeof(float2) * static_cast<size_t>(b) + 16;
-				if (cols > budget || rows > budget)
-					continue;
-				best1 = a;  // increasing a -> closest to sqrt(n) last
-			}
-			if (best1 > 0)
-				break;
-		}
+		const auto t = ctx->tiles.find(n);
+		const int best1 = t != ctx->tiles.end() && t->second.n1 > 0 ? t->second.n1 : rule_split(ctx, n);
 		require(best1 > 0, "no four-step split for FFT size " + std::to_string(n), UGSDR_E_UNSUPPORTED);
 		LargePlan lp;
 		lp.n = n;
@@ -194,6 +205,14 @@ namespace ugsdr_gpu {
 			rw = 8;
 			while (rw > 1 && 2 * sizeof(float2) * rw * static_cast<size_t>(lp.n2) + sizeof(float2) * lp.n2 + 16 > (ctx->smem_optin - 2048) / 3)
 				rw /= 2;
+			// a set or tuned shape (checked against the kernels' limits when set)
+			const auto t = ctx->tiles.find(lp.n);
+			if (t != ctx->tiles.end()) {
+				if (t->second.cw > 0)
+					cw = t->second.cw;
+				if (t->second.rw > 0)
+					rw = t->second.rw;
+			}
 		}
 
 		// Column plans of the warp-owned column kernel (unfolded rows): N1 = 400
@@ -215,8 +234,11 @@ namespace ugsdr_gpu {
 		}
 
 		// columns per column-kernel CTA of the blocked layout (0: natural layout)
-		int blocked_cw(int n1, int n2, int fold_mode) {
+		int blocked_cw(ugsdr_ctx* ctx, int n, int n1, int n2, int fold_mode) {
 			if (fold_mode != 0 || std::getenv("UGSDR_NO_WARP_COLS"))
+				return 0;
+			const auto t = ctx->tiles.find(n);
+			if (t != ctx->tiles.end() && t->second.warp_cols == 0)
 				return 0;
 			int cw = 0;
 			with_cols_warp(n1, n2, [&](auto plan) { cw = decltype(plan)::CW; });
@@ -328,8 +350,8 @@ namespace ugsdr_gpu {
 	}
 
 	// B points per (row, block) and column chunks per row of a job shape
-	void inverse_geometry(const BatchedParams& p, int fold_mode, int& cw_blocked, size_t& b_points, int& chunks) {
-		cw_blocked = blocked_cw(p.n1, p.n2, fold_mode);
+	void inverse_geometry(ugsdr_ctx* ctx, const BatchedParams& p, int fold_mode, int& cw_blocked, size_t& b_points, int& chunks) {
+		cw_blocked = blocked_cw(ctx, p.base.n, p.n1, p.n2, fold_mode);
 		if (cw_blocked) {
 			const int n2p = (p.n2 + cw_blocked - 1) / cw_blocked * cw_blocked;
 			b_points = static_cast<size_t>(p.n1) * n2p;
@@ -347,7 +369,7 @@ namespace ugsdr_gpu {
 		const BatchedParams p = batched_params(ctx, base, s.n);
 		int cwb = 0, chunks = 0;
 		size_t b_points = 0;
-		inverse_geometry(p, s.fold_mode, cwb, b_points, chunks);
+		inverse_geometry(ctx, p, s.fold_mode, cwb, b_points, chunks);
 		return ScratchLayout(s, batch_rows(s, b_points), chunks, b_points).total;
 	}
 
@@ -405,7 +427,7 @@ namespace ugsdr_gpu {
 		}
 		int cw_blocked = 0, chunks = 0;
 		size_t b_points = 0;
-		inverse_geometry(p, s.fold_mode, cw_blocked, b_points, chunks);
+		inverse_geometry(ctx, p, s.fold_mode, cw_blocked, b_points, chunks);
 		if (cw_blocked)
 			p.n2p = static_cast<int>(b_points / p.n1);
 		const int r_max = batch_rows(s, b_points);
@@ -505,6 +527,7 @@ namespace ugsdr_gpu {
 			}
 			else {
 				large_code_spectrum(ctx, e, chips.as<float>(), n_chips, repeats, sign_mask, sign_segment);
+				e.n1 = get_large_plan(ctx, n).n1;
 			}
 			UG_CUDA(cudaStreamSynchronize(ctx->stream));
 		}
@@ -956,6 +979,214 @@ namespace ugsdr_gpu {
 		UG_CUDA(cudaStreamSynchronize(ctx->stream));
 		finish_jobs(b, jobs, n_jobs, cells.data(), results, cells_out);
 	}
+
+	// ------------------------------------------------------------ tile tuning
+	namespace {
+		// complex points (rows x K x N) of one tuning search: 20 - 60 ms on the device
+		constexpr double kTunePoints = 4e9;
+		// a tuned shape replaces the rule only when it is this much faster
+		constexpr double kTuneMargin = 0.985;
+
+		ugsdr_tile_shape effective_shape(ugsdr_ctx* ctx, int n) {
+			const LargePlan& lp = get_large_plan(ctx, n);
+			ugsdr_tile_shape t{};
+			tile_shape(ctx, lp, t.cols, t.rows);
+			t.n1 = lp.n1;
+			t.warp_cols = blocked_cw(ctx, n, lp.n1, lp.n2, 0) ? 1 : 0;
+			t.block_samples = n;
+			return t;
+		}
+
+		// every kernel of the block size's current shape within its shared
+		// memory and launch bounds (checked on the host, before any launch)
+		void check_shape(ugsdr_ctx* ctx, int n) {
+			AcqParams base{};
+			base.n = n;
+			const BatchedParams p = batched_params(ctx, base, n);
+			with_large_ffts(p.n1, p.n2, [&](auto f1, auto f2) {
+				using F1 = decltype(f1);
+				using F2 = decltype(f2);
+				const size_t cap = ctx->smem_optin;
+				require(smem_cols(p) <= cap && smem_rows(p, false) <= cap && smem_inv_cols<F1>(p) <= cap &&
+					smem_inv_rows<F2>(p) <= cap, "tile shape exceeds shared memory", UGSDR_E_UNSUPPORTED);
+				require(threads_of<F1>(p.p1, p.cw) <= F1::kColsMaxThreads && threads_of<F2>(p.p2, p.rw) <= F2::kRowsMaxThreads,
+					"tile shape exceeds a kernel's launch bound", UGSDR_E_UNSUPPORTED);
+			});
+		}
+
+		// rebuilds the cached code spectra of block size n whose four-step
+		// layout an earlier split built
+		void refresh_codes(ugsdr_ctx* ctx, int n) {
+			const int n1 = get_large_plan(ctx, n).n1;
+			bool synced = false;
+			for (auto& kv : ctx->codes) {
+				CodeEntry& e = *kv.second;
+				if (!e.large || static_cast<int>(e.n) != n || e.n1 == n1)
+					continue;
+				if (!synced) {
+					UG_CUDA(cudaStreamSynchronize(ctx->stream));  // no search reads the old layout any more
+					synced = true;
+				}
+				build_code_spectrum(ctx, e, e.chips.data(), e.chips.size(), e.repeats, e.sign_mask, e.sign_segment);
+			}
+		}
+
+		// Sets block size n's shape; an unusable shape leaves the old one.
+		void apply_tiles(ugsdr_ctx* ctx, int n, const TileChoice& t) {
+			require(!fits_single_cta(ctx, n), "block size runs on the single-CTA path (no four-step tiles)", UGSDR_E_INVALID);
+			auto pow2 = [](int v) { return v == 0 || v == 1 || v == 2 || v == 4 || v == 8; };
+			require(pow2(t.cw) && pow2(t.rw) && t.warp_cols >= -1 && t.warp_cols <= 1, "tile shape out of range");
+			require(t.n1 == 0 || split_fits(ctx, n, t.n1, 1), "no four-step split " + std::to_string(t.n1) + " for FFT size " +
+				std::to_string(n), UGSDR_E_UNSUPPORTED);
+			const auto it = ctx->tiles.find(n);
+			const TileChoice old = it != ctx->tiles.end() ? it->second : TileChoice{};
+			ctx->tiles[n] = t;
+			ctx->large_plans.erase(n);
+			try {
+				check_shape(ctx, n);
+			}
+			catch (...) {
+				ctx->tiles[n] = old;
+				ctx->large_plans.erase(n);
+				throw;
+			}
+			refresh_codes(ctx, n);
+		}
+
+		struct EventPair {
+			cudaEvent_t a = nullptr, b = nullptr;
+			EventPair() {
+				UG_CUDA(cudaEventCreate(&a));
+				UG_CUDA(cudaEventCreate(&b));
+			}
+			~EventPair() {
+				cudaEventDestroy(a);
+				cudaEventDestroy(b);
+			}
+		};
+
+		// best of `reps` device times (ms) of the jobs as one batch, after one
+		// untimed run (plans, kernel attributes, scratch growth)
+		double time_jobs(ugsdr_ctx* ctx, const std::vector<ugsdr_acq_job>& jobs, int reps) {
+			std::vector<std::vector<ugsdr_acq_result>> res(jobs.size());
+			std::vector<ugsdr_acq_result*> ptrs(jobs.size());
+			for (size_t j = 0; j < jobs.size(); ++j) {
+				res[j].resize(jobs[j].n_codes);
+				ptrs[j] = res[j].data();
+			}
+			const int n_jobs = static_cast<int>(jobs.size());
+			run_jobs(ctx, jobs.data(), n_jobs, ptrs.data(), nullptr);
+			EventPair ev;
+			double best = 1e300;
+			for (int r = 0; r < reps; ++r) {
+				UG_CUDA(cudaEventRecord(ev.a, ctx->stream));
+				run_jobs(ctx, jobs.data(), n_jobs, ptrs.data(), nullptr);
+				UG_CUDA(cudaEventRecord(ev.b, ctx->stream));
+				UG_CUDA(cudaEventSynchronize(ev.b));
+				float ms = 0.f;
+				UG_CUDA(cudaEventElapsedTime(&ms, ev.a, ev.b));
+				best = std::min(best, static_cast<double>(ms));
+			}
+			return best;
+		}
+
+		// splits tried besides the rule's: the next smaller divisor that fits
+		// and the rule's split transposed (N1 above sqrt N)
+		std::vector<int> other_splits(ugsdr_ctx* ctx, int n, int rule) {
+			std::vector<int> out;
+			for (int a = rule - 1; a >= 2; --a)
+				if (split_fits(ctx, n, a, 4)) {
+					out.push_back(a);
+					break;
+				}
+			if (n / rule != rule && split_fits(ctx, n, n / rule, 4))
+				out.push_back(n / rule);
+			return out;
+		}
+
+		// The jobs of block size n with their Doppler grids cut so that one
+		// search is about kTunePoints points.
+		std::vector<ugsdr_acq_job> tuning_jobs(std::vector<ugsdr_acq_job> js, int n) {
+			double pts = 0;
+			for (const auto& j : js)
+				pts += static_cast<double>(j.n_codes) * doppler_grid(j.doppler_range, j.doppler_step).size() * j.n_blocks * n;
+			if (pts <= kTunePoints)
+				return js;
+			const double scale = kTunePoints / pts;
+			for (auto& j : js) {
+				const double nd = static_cast<double>(doppler_grid(j.doppler_range, j.doppler_step).size());
+				const int half = static_cast<int>(std::max(0.0, (nd * scale - 1.0) / 2.0));
+				j.doppler_range = half * j.doppler_step;
+			}
+			return js;
+		}
+	}
+
+	// Times the candidate shapes of each large block size among `jobs` on those
+	// jobs (Doppler grids cut to ~kTunePoints points) and keeps the fastest:
+	// the split first, then the column kernel and its tile width, then the
+	// rows per row CTA, each stage from the best so far.
+	void autotune(ugsdr_ctx* ctx, const ugsdr_acq_job* jobs, int n_jobs, std::vector<ugsdr_tile_shape>& tried) {
+		require(jobs != nullptr && n_jobs >= 1, "no jobs");
+		std::map<int, std::vector<ugsdr_acq_job>> by_size;
+		for (int j = 0; j < n_jobs; ++j) {
+			const JobLaunch L = validate(ctx, jobs[j]);
+			if (L.large)
+				by_size[L.n].push_back(jobs[j]);
+		}
+		for (const auto& [n, all] : by_size) {
+			const std::vector<ugsdr_acq_job> js = tuning_jobs(all, n);
+			std::map<std::tuple<int, int, int, int>, double> seen;
+			auto measure = [&](const TileChoice& t) {
+				try {
+					apply_tiles(ctx, n, t);
+				}
+				catch (const Error&) {
+					return 1e300;  // outside the kernels' limits: never launched
+				}
+				ugsdr_tile_shape eff = effective_shape(ctx, n);
+				const auto key = std::make_tuple(eff.n1, eff.cols, eff.rows, eff.warp_cols);
+				const auto hit = seen.find(key);
+				if (hit != seen.end())
+					return hit->second;
+				eff.ms = time_jobs(ctx, js, 2);
+				seen[key] = eff.ms;
+				tried.push_back(eff);
+				return eff.ms;
+			};
+			const TileChoice rule{};
+			const double rule_ms = measure(rule);
+			TileChoice best = rule;
+			double best_ms = rule_ms;
+			auto consider = [&](const TileChoice& t) {
+				const double ms = measure(t);
+				if (ms < best_ms) {
+					best = t;
+					best_ms = ms;
+				}
+			};
+			for (const int a : other_splits(ctx, n, effective_shape(ctx, n).n1)) {
+				TileChoice t = rule;
+				t.n1 = a;
+				consider(t);
+			}
+			const TileChoice split = best;
+			for (const int wc : {1, 0})
+				for (const int cw : {8, 4, 2}) {
+					TileChoice t = split;
+					t.warp_cols = wc;
+					t.cw = cw;
+					consider(t);
+				}
+			const TileChoice cols = best;
+			for (const int rw : {8, 4, 2}) {
+				TileChoice t = cols;
+				t.rw = rw;
+				consider(t);
+			}
+			apply_tiles(ctx, n, best_ms < kTuneMargin * rule_ms ? best : rule);
+		}
+	}
 }
 
 using namespace ugsdr_gpu;
@@ -976,6 +1207,10 @@ int ugsdr_code_put(ugsdr_ctx* ctx, const float* chips, size_t n_chips, size_t re
 		e->spectrum_mode = spectrum_mode;
 		e->large = !fits_single_cta(ctx, static_cast<int>(samples));
 		build_code_spectrum(ctx, *e, chips, n_chips, repeats, sign_mask, sign_segment);
+		e->chips.assign(chips, chips + n_chips);
+		e->repeats = repeats;
+		e->sign_mask = sign_mask;
+		e->sign_segment = sign_segment;
 		const int h = ctx->next_code++;
 		ctx->codes[h] = std::move(e);
 		*handle = h;
@@ -1012,6 +1247,50 @@ int ugsdr_acquire_batch(ugsdr_ctx* ctx, const ugsdr_acq_job* jobs, int n_jobs, u
 	return guarded(ctx, [&] {
 		require(results != nullptr, "null results");
 		run_jobs(ctx, jobs, n_jobs, results, nullptr);
+	});
+}
+int ugsdr_tile_get(ugsdr_ctx* ctx, size_t block_samples, ugsdr_tile_shape* shape) {
+	if (!ctx)
+		return UGSDR_E_INVALID;
+	std::lock_guard<std::mutex> lock(ctx->mutex);
+	return guarded(ctx, [&] {
+		require(shape != nullptr, "null shape");
+		require(block_samples >= 2 && block_samples <= (1u << 24), "block size out of range");
+		const int n = static_cast<int>(block_samples);
+		require(!fits_single_cta(ctx, n), "block size runs on the single-CTA path (no four-step tiles)", UGSDR_E_INVALID);
+		*shape = effective_shape(ctx, n);
+	});
+}
+
+int ugsdr_tile_set(ugsdr_ctx* ctx, size_t block_samples, const ugsdr_tile_shape* shape) {
+	if (!ctx)
+		return UGSDR_E_INVALID;
+	std::lock_guard<std::mutex> lock(ctx->mutex);
+	return guarded(ctx, [&] {
+		require(block_samples >= 2 && block_samples <= (1u << 24), "block size out of range");
+		TileChoice t{};
+		if (shape) {
+			t.n1 = shape->n1;
+			t.cw = shape->cols;
+			t.rw = shape->rows;
+			t.warp_cols = shape->warp_cols;
+		}
+		apply_tiles(ctx, static_cast<int>(block_samples), t);
+	});
+}
+
+int ugsdr_autotune(ugsdr_ctx* ctx, const ugsdr_acq_job* jobs, int n_jobs, ugsdr_tile_shape* tried, int max_tried, int* n_tried) {
+	if (!ctx)
+		return UGSDR_E_INVALID;
+	std::lock_guard<std::mutex> lock(ctx->mutex);
+	return guarded(ctx, [&] {
+		require(max_tried >= 0 && (tried != nullptr || max_tried == 0), "null tried list");
+		std::vector<ugsdr_tile_shape> all;
+		autotune(ctx, jobs, n_jobs, all);
+		const int n = static_cast<int>(std::min<size_t>(all.size(), static_cast<size_t>(max_tried)));
+		std::copy(all.begin(), all.begin() + n, tried);
+		if (n_tried)
+			*n_tried = static_cast<int>(all.size());
 	});
 }
 }

@@ -182,8 +182,8 @@ namespace ugsdr_gpu {
 		float2* a = smem;
 		float2* b = smem + F::N;
 		const FftPlanDev plan = F::prepare(p.plan, smem + 2 * F::N);
-		if (threadIdx.x < 80)
-			lut[threadIdx.x] = p.lut[threadIdx.x];
+		for (int i = threadIdx.x; i < 80; i += blockDim.x)
+			lut[i] = p.lut[i];
 		__syncthreads();
 		const int d = blockIdx.x / p.k_blocks;
 		const int blk = blockIdx.x - d * p.k_blocks;
@@ -260,8 +260,9 @@ namespace ugsdr_gpu {
 	__global__ void __launch_bounds__(256, 3) fwd_cols_kernel(BatchedParams p) {
 		extern __shared__ float2 smem[];
 		__shared__ float lut[80];
-		if (threadIdx.x < 80 && p.base.lut)
-			lut[threadIdx.x] = p.base.lut[threadIdx.x];
+		// the 80-entry table whatever the block size (64-thread CTAs for 2-column tiles)
+		for (int i = threadIdx.x; i < 80 && p.base.lut; i += blockDim.x)
+			lut[i] = p.base.lut[i];
 		__syncthreads();
 		const int n1 = fft_n<F1>(p.n1), n2 = p.n2;
 		const int chunks = (n2 + p.cw - 1) >> p.cw_shift;

@@ -164,8 +164,8 @@ namespace ugsdr_gpu {
 		float2* b = smem + p.n;
 		const int d = blockIdx.x / p.k_blocks;
 		const int blk = blockIdx.x % p.k_blocks;
-		if (threadIdx.x < 80)
-			lut[threadIdx.x] = p.lut[threadIdx.x];
+		for (int i = threadIdx.x; i < 80; i += blockDim.x)
+			lut[i] = p.lut[i];
 		__syncthreads();
 		const uint32_t adder = p.adders[p.d_base + d];
 		const uint64_t base = static_cast<uint64_t>(blk) * p.n;

@@ -87,11 +87,25 @@ namespace ugsdr_gpu {
 		FftPlanDesc p1, p2;    // N1-point and N2-point plans (the inter-step twiddles are computed in the kernels)
 	};
 
+	// Tile shape of the four-step path for one block size, as set by
+	// ugsdr_tile_set or chosen by ugsdr_autotune (0 / -1: the built-in rule).
+	struct TileChoice {
+		int n1 = 0;         // split N = n1 x N / n1
+		int cw = 0;         // columns per column-kernel CTA (natural layout)
+		int rw = 0;         // rows per row-kernel CTA
+		int warp_cols = -1; // 1: warp-owned column kernel where one is compiled, 0: natural layout
+	};
+
 	struct CodeEntry {
 		size_t n = 0;
 		int spectrum_mode = 0;
 		bool large = false;           // stored in the four-step (k1-major) layout
+		int n1 = 0;                   // large: the split the layout was built with
 		DevBuf spectrum;              // N complex
+		// what built the spectrum, so that a new split can rebuild the layout
+		std::vector<float> chips;
+		size_t repeats = 0, sign_segment = 0;
+		uint32_t sign_mask = 0;
 	};
 
 	struct Plans;  // fft planning (acq.cu)
@@ -139,6 +153,7 @@ struct ugsdr_ctx {
 	std::map<int, std::unique_ptr<ugsdr_gpu::DevBuf>> twiddles;
 	std::map<int, ugsdr_gpu::FftPlanDesc> plans;
 	std::map<int, ugsdr_gpu::LargePlan> large_plans;
+	std::map<int, ugsdr_gpu::TileChoice> tiles;  // per block size (ugsdr_tile_set / ugsdr_autotune)
 
 	// code spectra
 	std::map<int, std::unique_ptr<ugsdr_gpu::CodeEntry>> codes;

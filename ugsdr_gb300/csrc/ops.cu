@@ -40,8 +40,8 @@ namespace ugsdr_gpu {
 		// ------------------------------------------------------- kernels
 		__global__ void mix_kernel(float2* x, size_t n, uint32_t adder, uint32_t phase0, const float* lut_g) {
 			__shared__ float lut[80];
-			if (threadIdx.x < 80)
-				lut[threadIdx.x] = lut_g[threadIdx.x];
+			for (int i = threadIdx.x; i < 80; i += blockDim.x)
+				lut[i] = lut_g[i];
 			__syncthreads();
 			for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n; i += static_cast<size_t>(gridDim.x) * blockDim.x)
 				x[i] = table_mix(x[i], i, adder, phase0, lut);

@@ -165,8 +165,8 @@ namespace ugsdr_gpu {
 			TrackState* st = p.states + blockIdx.x;
 			const int len = st->len;
 			const float* chips = p.chips + static_cast<size_t>(st->code) * p.len_max;
-			if (threadIdx.x < 80)
-				s_lut[threadIdx.x] = p.lut[threadIdx.x];
+			for (int i = threadIdx.x; i < 80; i += blockDim.x)
+				s_lut[i] = p.lut[i];
 
 			const int spm = static_cast<int>(p.spm);
 			const int period_ms = st->period_ms;
