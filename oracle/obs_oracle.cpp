@@ -11,14 +11,13 @@
 //     370;
 //   - the Observable constructor (observable.hpp:75-88) with CalculateSnr
 //     (55-72) and the i-independent UpdatePseudorange term (327-336).
-// The reference's Observable does not compile without Intel IPP here (its
-// src/tracking/tracking_parameters.hpp:47-56 non-IPP configuration has its
-// arguments out of order and a trailing comma), so this file restates it.
 // Pinned: the candidate search (against the reference's own upsampler,
-// matched filter and abs, tests/golden/preamble.npz) and CalculateSnr's
-// sigma (against its SequentialMeanStdDev).  The constructor's pseudorange /
-// pseudophase / Doppler lines are parity unpinned: restated by reading
-// observable.hpp:75-88 and 327-336, no reference output covers them.
+// matched filter and abs, tests/golden/preamble.npz), and the constructor's
+// pseudorange / pseudophase / Doppler / SNR with UpdatePseudoranges, bit for
+// bit (SNR within 1e-12) against the reference's own Observable run on its
+// own tracker's histories (tests/golden/observables.npz; the harness
+// compiles a build-time copy of observable.hpp whose only change opens the
+// constructor's access, oracle/patch_tracking.py).
 #include "fft64.hpp"
 
 #include <cmath>

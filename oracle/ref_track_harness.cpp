@@ -11,6 +11,8 @@
 //   TrackingParameters::CorrelateSplit       tracking_parameters.hpp:472-493 (AddWithPhase 89-98)
 //   TrackingParameters::Pll / Dll            tracking_parameters.hpp:495-528 (constants 72-87)
 //   SequentialMatchedFilter::Filter, SequentialAbs, SequentialReshapeAndSum
+//   Observable's constructor and UpdatePseudoranges (measurements/
+//   observable.hpp:55-88, 327-336; the build-time copy opens its access)
 // Tracker::TrackSingleSatellite / GetEpl (src/tracking/tracker.hpp:119-177)
 // and AddSignalImpl's surrounding steps (tracking_parameters.hpp:321-357) are
 // private or need a DigitalFrontend, and MatchedFilterTranslated (297-319)
@@ -23,6 +25,7 @@
 #include "prn_codes/codegen_wrapper.hpp"
 #include "resample/upsampler.hpp"
 #include "patched/tracking/tracking_parameters.hpp"
+#include "patched/measurements/observable.hpp"
 
 #include <algorithm>
 #include <complex>
@@ -152,5 +155,43 @@ void ref_refine_f32(const float* iq, std::size_t n, int signal, int sv, double f
 	out[1] = accepted ? 1.0 : 0.0;
 	out[2] = accepted ? p.code_phase + static_cast<double>(code_offset) : p.code_phase;
 	out[3] = std::abs(value);
+}
+
+// The reference's Observable on one GPS L1 C/A channel's tracking history
+// (what TrackingParameters holds after TrackSingleSatellite: prompt, phases =
+// -carrier_phase / 2 pi as Pll pushes them (tracking_parameters.hpp:509),
+// frequencies, code_phases): the constructor (observable.hpp:75-88) with
+// CalculateSnr (55-72), then TimeScale::UpdateScale for a preamble at
+// `position` and time of week tow_s (timescale.hpp:22-36) and
+// UpdatePseudoranges (UpdatePseudorangeGps, observable.hpp:327-331).
+// CalculateSnr keeps thread_local buffers sized by its first call, so every
+// call of one process passes the same n.  out: n x 4 (pseudorange ms,
+// pseudophase cycles, doppler Hz, snr).
+void ref_observable_f64(const float* prompt_iq, const double* carrier_phase, const double* frequencies,
+	const double* code_phases, std::size_t n, double fs, double intermediate_frequency, std::size_t position,
+	std::size_t tow_s, double* out) {
+	Params p;
+	p.sv.system = ugsdr::System::Gps;
+	p.sv.signal = Signal::GpsCoarseAcquisition_L1;
+	p.sampling_rate = fs;
+	p.intermediate_frequency = intermediate_frequency;
+	for (std::size_t i = 0; i < n; ++i) {
+		p.prompt.emplace_back(prompt_iq[2 * i], prompt_iq[2 * i + 1]);
+		p.phases.push_back(-carrier_phase[i] / (2 * std::numbers::pi));
+		p.frequencies.push_back(frequencies[i]);
+		p.code_phases.push_back(code_phases[i]);
+	}
+	ugsdr::TimeScale time_scale(n);
+	time_scale.UpdateScale(position, tow_s * 1000, ugsdr::System::Gps);
+	ugsdr::GpsEphemeris eph;
+	eph.tow = tow_s;
+	ugsdr::Observable obs(p, time_scale, position, eph);
+	obs.UpdatePseudoranges(0);
+	for (std::size_t i = 0; i < n; ++i) {
+		out[4 * i] = obs.pseudorange[i];
+		out[4 * i + 1] = obs.pseudophase[i];
+		out[4 * i + 2] = obs.doppler[i];
+		out[4 * i + 3] = obs.snr[i];
+	}
 }
 }

@@ -59,3 +59,28 @@ def oracle():
     import pyoracle
     pyoracle.load()
     return pyoracle
+
+
+# tracking-bank output rows (ugsdr_track_output) of the reference's own
+# tracking history in tests/golden/track.npz: what the Observable pins feed
+# to the oracle and to ugsdr_observables
+TRACK_ROW = np.dtype([("taps", "<f4", (5, 2)), ("carrier_frequency", "<f8"), ("carrier_phase", "<f8"),
+                      ("code_phase", "<f8"), ("code_frequency", "<f8"), ("phase_error", "<f8"), ("code_error", "<f8")])
+
+
+def reference_track_rows(channels):
+    """(n_epochs, len(channels)) rows from the reference tracker's outputs
+    (make_golden.py track: E, P, L re/im, carrier_frequency, carrier_phase,
+    code_phase, code_frequency, phase residual, code residual per epoch),
+    plus each channel's starting carrier frequency."""
+    z = np.load(GOLDEN / "track.npz")
+    tr = [z[f"ch{k}/track"] for k in channels]
+    rows = np.zeros((tr[0].shape[0], len(channels)), TRACK_ROW)
+    for c, t in enumerate(tr):
+        for tap, col in ((1, 0), (2, 2), (3, 4)):  # E, P, L in the VE/E/P/L/VL slots
+            rows["taps"][:, c, tap, 0] = t[:, col]
+            rows["taps"][:, c, tap, 1] = t[:, col + 1]
+        for name, col in (("carrier_frequency", 6), ("carrier_phase", 7), ("code_phase", 8), ("code_frequency", 9),
+                          ("phase_error", 10), ("code_error", 11)):
+            rows[name][:, c] = t[:, col]
+    return rows, [float(z[f"ch{k}/carrier_frequency"]) for k in channels], float(z["fs"])

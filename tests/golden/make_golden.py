@@ -466,6 +466,31 @@ def track(lib) -> dict[str, np.ndarray]:
     return out
 
 
+OBS_IF, OBS_POSITION, OBS_TOW_S = 1250.0, 37, 345678
+
+
+def observables(lib) -> dict[str, np.ndarray]:
+    """The reference's Observable (ref_observable_f64: its constructor with
+    CalculateSnr, then TimeScale::UpdateScale and UpdatePseudoranges) on the
+    three GPS channels' reference tracking histories in track.npz (prompt,
+    carrier phase, carrier frequency, code phase per epoch), at an IF of
+    1.25 kHz, a preamble at epoch 37 and a time of week of 345678 s."""
+    d, vp, sz = C.c_double, C.c_void_p, C.c_size_t
+    lib.ref_observable_f64.argtypes = [vp, vp, vp, vp, sz, d, d, sz, sz, vp]
+    z = np.load(HERE / "track.npz")
+    fs = float(z["fs"])
+    out = {"intermediate_frequency": np.float64(OBS_IF), "position": np.int64(OBS_POSITION),
+           "tow_s": np.int64(OBS_TOW_S), "channels": np.int32(3)}
+    for k in range(3):  # the GPS L1 C/A channels
+        tr = z[f"ch{k}/track"]
+        piq = np.ascontiguousarray(tr[:, 2:4].astype(np.float32))
+        cph, freq, cp = (np.ascontiguousarray(tr[:, j]) for j in (7, 6, 8))
+        res = np.zeros((len(tr), 4))
+        lib.ref_observable_f64(p(piq), p(cph), p(freq), p(cp), len(tr), fs, OBS_IF, OBS_POSITION, OBS_TOW_S, p(res))
+        out[f"ch{k}"] = res
+    return out
+
+
 def main() -> None:
     ref_dir = sys.argv[1] if len(sys.argv) > 1 else str(Path(__file__).resolve().parents[3] / "reference")
     lib = ref_lib(ref_dir)
@@ -485,6 +510,7 @@ def main() -> None:
     np.savez_compressed(HERE / "iq16.npz", **iq16(ref_dir))
     np.savez_compressed(HERE / "preamble.npz", **preamble(lib))
     np.savez_compressed(HERE / "track.npz", **track(lib))
+    np.savez_compressed(HERE / "observables.npz", **observables(lib))
     for f in sorted(HERE.glob("*.npz")):
         print(f.name, f.stat().st_size)
 

@@ -6,11 +6,15 @@ observable.hpp.
     matched filter (tests/golden/preamble.npz); the device lists must equal
     them exactly, for GPS LNAV and GLONASS, odd lengths, prompts shorter than
     the preamble, an inverted stream and an all-zero prompt.
-  * Observable arithmetic on a real tracking run: pseudorange and Doppler bit
-    for bit (the same double operations), SNR within a float ulp of 27 dB
-    (log10f), pseudophase within 1e-5 cycles (the bank keeps the carrier
-    phase as a 64-bit fraction of a cycle, the reference accumulates radians
-    in double)."""
+  * Observable arithmetic against the reference's own Observable
+    (tests/golden/observables.npz: its constructor, CalculateSnr and
+    UpdatePseudoranges on the reference tracker's histories): pseudorange and
+    Doppler bit for bit, pseudophase within 1e-9 cycles, SNR within 1e-5 dB.
+  * Observable arithmetic on a real tracking run against the oracle:
+    pseudorange and Doppler bit for bit (the same double operations), SNR
+    within a float ulp of 27 dB (log10f), pseudophase within 1e-5 cycles (the
+    bank keeps the carrier phase as a 64-bit fraction of a cycle, the
+    reference accumulates radians in double)."""
 import ctypes as C
 from pathlib import Path
 
@@ -96,6 +100,29 @@ def obs_channels(chans, if_hz):
     return [dict(fs=ch["fs"], intermediate_frequency=if_hz, carrier_frequency=ch["carrier_frequency"],
                  carrier_phase=ch["carrier_phase"], preamble_position=17 + 5 * i, range_correction_ms=68.0 + i)
             for i, ch in enumerate(chans)]
+
+
+def test_observables_match_reference(ctx):
+    """ugsdr_observables on the reference tracker's own outputs (three GPS
+    channels, 160 epochs) against the reference Observable's outputs."""
+    from conftest import reference_track_rows
+    from ugsdr_gb300.api import TRACK_DTYPE, observables
+    z = np.load(GOLDEN.parent / "observables.npz")
+    ref_rows, cf0, fs = reference_track_rows(range(int(z["channels"])))
+    rows = np.zeros(ref_rows.shape, TRACK_DTYPE)
+    for name in TRACK_DTYPE.names:
+        rows[name] = ref_rows[name]
+    och = [dict(fs=fs, intermediate_frequency=float(z["intermediate_frequency"]), carrier_frequency=cf,
+                carrier_phase=0.0, preamble_position=int(z["position"]), range_correction_ms=68.0) for cf in cf0]
+    got = observables(ctx, rows, och)
+    for c in range(rows.shape[1]):
+        ref = z[f"ch{c}"]
+        np.testing.assert_array_equal(got["pseudorange"][:, c], ref[:, 0])
+        np.testing.assert_array_equal(got["doppler"][:, c], ref[:, 2])
+        np.testing.assert_allclose(got["pseudophase"][:, c], ref[:, 1], rtol=0, atol=1e-9)
+        np.testing.assert_allclose(got["snr"][:, c], ref[:, 3], rtol=0, atol=1e-5)
+        print(f"channel {c}: max |d pseudophase| {np.abs(got['pseudophase'][:, c] - ref[:, 1]).max():.1e} cycles, "
+              f"max |d snr| {np.abs(got['snr'][:, c] - ref[:, 3]).max():.1e} dB")
 
 
 def test_observables_match_oracle(ctx, oracle, golden_codes):

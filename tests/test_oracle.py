@@ -284,3 +284,24 @@ def test_track_refine_pinned_to_reference(oracle):
     acc, offs, phases, _ = oracle.track_refine(x, channels, [ch["chips"] for ch in chans])
     for i, ch in enumerate(chans):
         assert offs[i] == int(ch["refine"][0]) and acc[i] == int(ch["refine"][1]) and phases[i] == ch["refine"][2], i
+
+
+def test_observables_pinned_to_reference(oracle):
+    """The oracle's Observable arithmetic (orc_observables_f64) on the
+    reference tracker's own histories gives the reference Observable's
+    outputs (tests/golden/observables.npz: constructor, CalculateSnr,
+    UpdateScale + UpdatePseudoranges; IF 1.25 kHz, preamble at epoch 37,
+    time of week 345678 s): pseudorange, pseudophase and Doppler bit for
+    bit, SNR within 1e-12."""
+    from conftest import reference_track_rows
+    z = np.load(GOLDEN / "observables.npz")
+    rows, cf0, fs = reference_track_rows(range(int(z["channels"])))
+    if_hz, pos = float(z["intermediate_frequency"]), int(z["position"])
+    # UpdatePseudorangeGps after UpdateScale: time_scale[i] - (i - pos + tow_ms + 2) = 70 - 2
+    for c in range(rows.shape[1]):
+        got = oracle.observables(rows[:, c], fs, if_hz, cf0[c], 0.0, pos, 68.0)
+        ref = z[f"ch{c}"]
+        np.testing.assert_array_equal(got[:, 0], ref[:, 0])
+        np.testing.assert_array_equal(got[:, 1], ref[:, 1])
+        np.testing.assert_array_equal(got[:, 2], ref[:, 2])
+        np.testing.assert_allclose(got[:, 3], ref[:, 3], rtol=1e-12, atol=0)
