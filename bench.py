@@ -303,11 +303,11 @@ def run_ours(args, world, rank):
     for n in sorted({j["n"] for j in jobs if j["n"] > 12000}):
         t = ctx.tile_shape(n)
         rule_ms = next((x["ms"] for x in tried if x["block_samples"] == n), None)
-        kept_ms = next((x["ms"] for x in tried if x["block_samples"] == n and
-                        (x["n1"], x["cols"], x["rows"], x["warp_cols"]) == (t["n1"], t["cols"], t["rows"], t["warp_cols"])),
-                       None)
+        key = ("n1", "cols", "rows", "warp_cols", "warp_rows")
+        kept_ms = next((x["ms"] for x in tried if x["block_samples"] == n and all(x[k] == t[k] for k in key)), None)
         tiles[str(n)] = {"split": f"{t['n1']}x{n // t['n1']}", "cols": t["cols"], "rows": t["rows"],
                          "column_kernel": "warp-owned" if t["warp_cols"] else "tile",
+                         "row_kernel": "warp-owned" if t["warp_rows"] else "tile",
                          "shapes_timed": sum(1 for x in tried if x["block_samples"] == n),
                          "rule_ms": rule_ms, "kept_ms": kept_ms}
 

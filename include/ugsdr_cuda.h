@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define UGSDR_CUDA_ABI_VERSION 8
+#define UGSDR_CUDA_ABI_VERSION 9
 
 enum ugsdr_status {
 	UGSDR_OK = 0,
@@ -229,6 +229,8 @@ typedef struct ugsdr_tile_shape {
 	int rows;        /* rows per row-kernel CTA: 1, 2, 4 or 8 (0: rule) */
 	int warp_cols;   /* 1: warp-owned column kernel where one is compiled for the split, 0: one tile of
 	                    `cols` columns per CTA, -1: rule (the warp-owned kernel where compiled) */
+	int warp_rows;   /* 1: warp-owned row kernel (with the warp-owned columns; each warp takes whole rows through
+	                    both passes), 0: rows in CTA tiles of `rows` rows, -1: rule (warp-owned where compiled) */
 	int block_samples; /* N the shape is for (filled by ugsdr_tile_get / ugsdr_autotune, ignored by ugsdr_tile_set) */
 	double ms;       /* ugsdr_autotune: device time of the tuning search with this shape */
 } ugsdr_tile_shape;
@@ -244,7 +246,8 @@ int ugsdr_tile_set(ugsdr_ctx* ctx, size_t block_samples, const ugsdr_tile_shape*
  * runs those jobs (Doppler grids cut to about 4e9 complex points per search)
  * with candidate shapes and keeps the fastest: the split (the rule's, the
  * next smaller divisor, the rule's transposed), then the column kernel and
- * its width, then the rows per row CTA, each stage from the best so far; the
+ * its width, then the row kernel and the rows per row CTA, each stage from
+ * the best so far; the
  * rule's shape stays unless another is 1.5 % faster.  Each candidate runs
  * once untimed and twice timed with CUDA events (the best counts).  tried
  * receives up to max_tried measured shapes, n_tried (may be NULL) their

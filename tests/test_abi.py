@@ -28,7 +28,7 @@ def test_exports_every_header_symbol(lib):
 
 
 def test_abi_version(lib):
-    assert lib.ugsdr_abi_version() == 8  # four-step tile shapes and the autotuner
+    assert lib.ugsdr_abi_version() == 9  # four-step tile shapes (warp-owned rows) and the autotuner
 
 
 @pytest.mark.parametrize("name,signal,count", [("gps_l1ca", L.GPS_L1CA, 37), ("gps_l5i", L.GPS_L5I, 32),

@@ -5,7 +5,7 @@ Every shape the autotuner may pick runs the same search: peak index and
 Doppler bin equal to the oracle's, level, mean, sigma and SNR within 1e-4
 of the FP64 oracle, on the compile-time 200 x 250 split of a 50,000-point
 block (warp-owned and natural column kernels, 8 / 4 / 2 columns, 8 / 4 / 2
-rows) and on the runtime splits of a 16,000-point block (125 x 128, its
+rows, warp-owned and CTA-tile row kernels) and on the runtime splits of a 16,000-point block (125 x 128, its
 transpose, 100 x 160), whose code spectra were cached under another split
 and are rebuilt by the change.  The tuner keeps a shape it measured and
 the search still matches the oracle after tuning."""
@@ -19,7 +19,9 @@ from ugsdr_gb300 import signals
 
 pytestmark = pytest.mark.gpu
 
-SHAPES_50K = [dict(cols=c, rows=r, warp_cols=w) for w in (1, 0) for c in (8, 4, 2) for r in (8, 4, 2)]
+SHAPES_50K = ([dict(cols=c, rows=r, warp_cols=w, warp_rows=0) for w in (1, 0) for c in (8, 4, 2) for r in (8, 4, 2)] +
+              [dict(cols=c, rows=r, warp_cols=1, warp_rows=1) for c in (8, 2) for r in (8, 2)])
+KEY = ("n1", "cols", "rows", "warp_cols", "warp_rows")
 
 
 def gps_50k(golden_codes):
@@ -41,13 +43,13 @@ def test_every_tuner_shape_of_50000_matches_oracle(ctx, oracle, golden_codes):
     handles = [ctx.code_put(ca[p], 50000) for p in prns]
     try:
         rule = ctx.tile_shape(50000)
-        assert (rule["n1"], rule["warp_cols"]) == (200, 1)
+        assert (rule["n1"], rule["warp_cols"], rule["warp_rows"]) == (200, 1, 1)
         job = ctx.make_job(raw, L.SAMPLES_CI16, 50e6, 50000, 2, handles, 1000, 500)
         for shape in SHAPES_50K:
             ctx.set_tile_shape(50000, shape)
             got = ctx.tile_shape(50000)
-            assert (got["cols"], got["rows"], got["warp_cols"], got["n1"]) == \
-                (shape["cols"], shape["rows"], shape["warp_cols"], 200), (shape, got)
+            assert (got["cols"], got["rows"], got["warp_cols"], got["warp_rows"], got["n1"]) == \
+                (shape["cols"], shape["rows"], shape["warp_cols"], shape["warp_rows"], 200), (shape, got)
             res, _ = ctx.acquire(job, cells=True)
             for r, (o32, o64) in zip(res, refs):
                 check_vs_oracle(r, o32, o64)
@@ -114,7 +116,7 @@ def test_autotune_keeps_a_measured_shape(ctx, oracle, golden_codes):
             mine = [t for t in tried if t["block_samples"] == n]
             assert len(mine) >= 4 and all(t["ms"] > 0 for t in mine), mine
             kept = ctx.tile_shape(n)
-            key = lambda t: (t["n1"], t["cols"], t["rows"], t["warp_cols"])
+            key = lambda t: tuple(t[k] for k in KEY)
             assert key(kept) in {key(t) for t in mine}
             best = min(t["ms"] for t in mine)
             kept_ms = [t["ms"] for t in mine if key(t) == key(kept)][0]

@@ -10,7 +10,7 @@ from pathlib import Path
 
 LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libugsdr_cuda.so"
 
-ABI_VERSION = 8  # UGSDR_CUDA_ABI_VERSION the structs below mirror
+ABI_VERSION = 9  # UGSDR_CUDA_ABI_VERSION the structs below mirror
 
 OK = 0
 E_INVALID = -1
@@ -73,7 +73,8 @@ class AcqCell(C.Structure):
 
 
 class TileShape(C.Structure):
-    _fields_ = [("n1", C.c_int), ("cols", C.c_int), ("rows", C.c_int), ("warp_cols", C.c_int), ("block_samples", C.c_int),
+    _fields_ = [("n1", C.c_int), ("cols", C.c_int), ("rows", C.c_int), ("warp_cols", C.c_int), ("warp_rows", C.c_int),
+                ("block_samples", C.c_int),
                 ("ms", C.c_double)]
 
 

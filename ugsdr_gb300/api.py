@@ -137,7 +137,8 @@ class Context:
     # ----------------------------------------------- four-step tile shapes
     @staticmethod
     def _shape_dict(t: L.TileShape) -> dict:
-        return dict(block_samples=t.block_samples, n1=t.n1, cols=t.cols, rows=t.rows, warp_cols=t.warp_cols, ms=t.ms)
+        return dict(block_samples=t.block_samples, n1=t.n1, cols=t.cols, rows=t.rows, warp_cols=t.warp_cols,
+                    warp_rows=t.warp_rows, ms=t.ms)
 
     def tile_shape(self, block_samples: int) -> dict:
         """The four-step shape block_samples runs with (ugsdr_tile_get)."""
@@ -150,7 +151,8 @@ class Context:
         if shape is None:
             self._check(self.lib.ugsdr_tile_set(self.h, block_samples, None))
             return
-        t = L.TileShape(shape.get("n1", 0), shape.get("cols", 0), shape.get("rows", 0), shape.get("warp_cols", -1), block_samples, 0.0)
+        t = L.TileShape(shape.get("n1", 0), shape.get("cols", 0), shape.get("rows", 0), shape.get("warp_cols", -1),
+                        shape.get("warp_rows", -1), block_samples, 0.0)
         self._check(self.lib.ugsdr_tile_set(self.h, block_samples, C.byref(t)))
 
     def autotune(self, jobs: list["Job"], max_tried: int = 64) -> list[dict]:

@@ -233,6 +233,17 @@ namespace ugsdr_gpu {
 			return true;
 		}
 
+		// warp-owned row kernel (with the warp-owned columns): rows per warp —
+		// three 250-point rows (30 of 32 lanes in the radix-25 pass), one
+		// 500-point row (20 of 32) — and four warps per CTA
+		template <int N2>
+		constexpr int kRowsPerWarp = N2 <= 256 ? 3 : 1;
+		constexpr int kRowsWarps = 4;
+		bool warp_rows_on(ugsdr_ctx* ctx, int n) {
+			const auto t = ctx->tiles.find(n);
+			return t == ctx->tiles.end() || t->second.warp_rows != 0;
+		}
+
 		// columns per column-kernel CTA of the blocked layout (0: natural layout)
 		int blocked_cw(ugsdr_ctx* ctx, int n, int n1, int n2, int fold_mode) {
 			if (fold_mode != 0 || std::getenv("UGSDR_NO_WARP_COLS"))
@@ -468,6 +479,20 @@ namespace ugsdr_gpu {
 					constexpr int CW = P::CW;
 					// the row plan that pairs with the column plan: N = N1 x N2
 					if constexpr (F2::kHooked && ((P::N1 == 400 && F2::N == 500) || (P::N1 == 200 && F2::N == 250))) {
+						if (warp_rows_on(ctx, s.n)) {
+							// warp-owned rows: RPW rows per warp, four warps per CTA
+							constexpr int RPW = kRowsPerWarp<F2::N>, W = kRowsWarps;
+							auto rows_kernel = inv_rows_warp_kernel<F2, CW, P::N1, RPW, W>;
+							constexpr size_t smem_r = rows_warp_smem<F2, RPW, W>();
+							set_smem(rows_kernel, smem_r);
+							set_smem(inv_cols_warp_kernel<P>, P::smem_bytes());
+							KernelTimer timer(ctx, "acq_inverse_large");
+							run_batches([&] {
+								rows_kernel<<<p.rows * chunks_of(p.n1, RPW * W), 32 * W, smem_r, ctx->stream>>>(p);
+								inv_cols_warp_kernel<P><<<p.rows * chunks, 32 * P::WARPS, P::smem_bytes(), ctx->stream>>>(p);
+							});
+							return;
+						}
 						const size_t smem_r = smem_inv_rows<F2>(p);
 						set_smem(inv_rows_kernel<F2, CW, P::N1>, smem_r);
 						set_smem(inv_cols_warp_kernel<P>, P::smem_bytes());
@@ -993,6 +1018,9 @@ namespace ugsdr_gpu {
 			tile_shape(ctx, lp, t.cols, t.rows);
 			t.n1 = lp.n1;
 			t.warp_cols = blocked_cw(ctx, n, lp.n1, lp.n2, 0) ? 1 : 0;
+			// the warp-owned row kernel runs with the warp-owned columns of the
+			// 200 x 250 and 400 x 500 splits
+			t.warp_rows = t.warp_cols && warp_rows_on(ctx, n) ? 1 : 0;
 			t.block_samples = n;
 			return t;
 		}
@@ -1035,7 +1063,8 @@ namespace ugsdr_gpu {
 		void apply_tiles(ugsdr_ctx* ctx, int n, const TileChoice& t) {
 			require(!fits_single_cta(ctx, n), "block size runs on the single-CTA path (no four-step tiles)", UGSDR_E_INVALID);
 			auto pow2 = [](int v) { return v == 0 || v == 1 || v == 2 || v == 4 || v == 8; };
-			require(pow2(t.cw) && pow2(t.rw) && t.warp_cols >= -1 && t.warp_cols <= 1, "tile shape out of range");
+			require(pow2(t.cw) && pow2(t.rw) && t.warp_cols >= -1 && t.warp_cols <= 1 && t.warp_rows >= -1 && t.warp_rows <= 1,
+				"tile shape out of range");
 			require(t.n1 == 0 || split_fits(ctx, n, t.n1, 1), "no four-step split " + std::to_string(t.n1) + " for FFT size " +
 				std::to_string(n), UGSDR_E_UNSUPPORTED);
 			const auto it = ctx->tiles.find(n);
@@ -1125,7 +1154,8 @@ namespace ugsdr_gpu {
 	// Times the candidate shapes of each large block size among `jobs` on those
 	// jobs (Doppler grids cut to ~kTunePoints points) and keeps the fastest:
 	// the split first, then the column kernel and its tile width, then the
-	// rows per row CTA, each stage from the best so far.
+	// row kernel (warp-owned or CTA tiles) and the rows per row CTA, each
+	// stage from the best so far.
 	void autotune(ugsdr_ctx* ctx, const ugsdr_acq_job* jobs, int n_jobs, std::vector<ugsdr_tile_shape>& tried) {
 		require(jobs != nullptr && n_jobs >= 1, "no jobs");
 		std::map<int, std::vector<ugsdr_acq_job>> by_size;
@@ -1136,7 +1166,7 @@ namespace ugsdr_gpu {
 		}
 		for (const auto& [n, all] : by_size) {
 			const std::vector<ugsdr_acq_job> js = tuning_jobs(all, n);
-			std::map<std::tuple<int, int, int, int>, double> seen;
+			std::map<std::tuple<int, int, int, int, int>, double> seen;
 			auto measure = [&](const TileChoice& t) {
 				try {
 					apply_tiles(ctx, n, t);
@@ -1145,7 +1175,7 @@ namespace ugsdr_gpu {
 					return 1e300;  // outside the kernels' limits: never launched
 				}
 				ugsdr_tile_shape eff = effective_shape(ctx, n);
-				const auto key = std::make_tuple(eff.n1, eff.cols, eff.rows, eff.warp_cols);
+				const auto key = std::make_tuple(eff.n1, eff.cols, eff.rows, eff.warp_cols, eff.warp_rows);
 				const auto hit = seen.find(key);
 				if (hit != seen.end())
 					return hit->second;
@@ -1179,11 +1209,13 @@ namespace ugsdr_gpu {
 					consider(t);
 				}
 			const TileChoice cols = best;
-			for (const int rw : {8, 4, 2}) {
-				TileChoice t = cols;
-				t.rw = rw;
-				consider(t);
-			}
+			for (const int wr : {1, 0})
+				for (const int rw : {8, 4, 2}) {
+					TileChoice t = cols;
+					t.warp_rows = wr;
+					t.rw = rw;
+					consider(t);
+				}
 			apply_tiles(ctx, n, best_ms < kTuneMargin * rule_ms ? best : rule);
 		}
 	}
@@ -1274,6 +1306,7 @@ int ugsdr_tile_set(ugsdr_ctx* ctx, size_t block_samples, const ugsdr_tile_shape*
 			t.cw = shape->cols;
 			t.rw = shape->rows;
 			t.warp_cols = shape->warp_cols;
+			t.warp_rows = shape->warp_rows;
 		}
 		apply_tiles(ctx, static_cast<int>(block_samples), t);
 	});

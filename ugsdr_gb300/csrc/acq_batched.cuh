@@ -700,6 +700,76 @@ namespace ugsdr_gpu {
 		}
 	}
 
+	// Warp-owned row stage (two-pass hooked row plans): each warp of the CTA
+	// takes RPW of the CTA's RPW x WARPS rows through both passes for all K
+	// blocks with only __syncwarp between its passes — its X rows (the next
+	// block's copied in once pass 0 has read the current one), its code rows
+	// (staged once) and its work tile are private to it; the pass tables and
+	// the twiddle seeds are built once per CTA.  B goes out in the blocked
+	// layout of inv_cols_warp_kernel.  grid: rows * ceil(N1 / (RPW WARPS)).
+	template <class F2, int RPW, int WARPS>
+	constexpr size_t rows_warp_smem() {
+		return sizeof(float2) * (3 * static_cast<size_t>(WARPS) * RPW * F2::N + F2::N + static_cast<size_t>(WARPS) * RPW * (F2::kLastNS + 1)) + 16;
+	}
+	template <class F2, int BCW, int BN1, int RPW, int WARPS>
+	__global__ void __launch_bounds__(32 * WARPS) inv_rows_warp_kernel(BatchedParams p) {
+		static_assert(F2::kHooked && F2::kPasses == 2, "warp-owned rows run two-pass hooked plans (one work tile)");
+		extern __shared__ float2 smem[];
+		constexpr int N2 = F2::N, NS = F2::kLastNS, RW = RPW * WARPS, WT = RPW * N2;
+		const AcqParams& q = p.base;
+		const int n1 = p.n1, n = q.n;
+		const int chunks = (n1 + RW - 1) / RW;
+		const int lrow = blockIdx.x / chunks;
+		const int rc = (blockIdx.x - lrow * chunks) * RW;  // the CTA's first row
+		const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+		const int r0 = rc + warp * RPW;                   // the warp's first row
+		const int rw = max(0, min(RPW, n1 - r0));         // its rows (0: idle)
+		const int row = p.row0 + lrow;
+		const int c = row % q.n_codes;
+		const int d = row / q.n_codes;
+		float2* b = smem + warp * 3 * WT;
+		float2* xs = b + WT;
+		float2* cs = xs + WT;
+		const FftPlanDev p2 = F2::prepare(p.p2, smem + WARPS * 3 * WT);
+		float2* seeds = const_cast<float2*>(p2.tw) + N2;  // after the pass tables (N2 entries)
+		build_row_seeds(seeds, min(RW, n1 - rc), NS, rc, static_cast<uint32_t>(n));
+		__syncthreads();  // pass tables and seeds: the CTA's only barrier
+		if (rw == 0)
+			return;
+		const float2* code = q.codes[c] + static_cast<size_t>(r0) * N2;
+		const float2* xg = q.spectra + static_cast<size_t>(d) * q.k_blocks * n + static_cast<size_t>(r0) * N2;
+		const int elems = rw * N2;
+		const bool wide = (N2 % 2 == 0) && (n % 2 == 0);  // every row start 16-byte aligned
+		auto copy_rows = [&](float2* dst, const float2* src) {
+			if (wide) {
+				for (int e = 2 * lane; e < elems; e += 64)
+					cp_async16(dst + e, src + e);
+			}
+			else {
+				for (int e = lane; e < elems; e += 32)
+					cp_async8(dst + e, src + e);
+			}
+		};
+		copy_rows(cs, code);
+		copy_rows(xs, xg);
+		cp_async_commit();
+		const InvRowsLoadStagedN load{InvRowsLoadStaged{xs, cs, code}, N2};
+		const float2* wseeds = seeds + warp * RPW * (NS + 1);
+		for (int blk = 0; blk < q.k_blocks; ++blk) {
+			cp_async_wait_all();
+			__syncwarp();  // this block's X rows; the previous block's last pass is done with `b`
+			const size_t item = static_cast<size_t>(lrow) * q.k_blocks + blk;
+			auto next = [&] {  // pass 0 has read xs: the next block's X goes there
+				if (blk + 1 < q.k_blocks) {
+					copy_rows(xs, xg + static_cast<size_t>(blk + 1) * n);
+					cp_async_commit();
+				}
+			};
+			const InvRowsEmitBlocked<BCW, BN1> emit{p.bbuf + item * (static_cast<size_t>(n1) * p.n2p), r0, wseeds};
+			F2::template run_hooked_warp<true, true>(b, b, p2, rw, N2, load, emit, next);
+		}
+	}
+
 	// grid: rows * ceil(N2 / cw); shared: 3 * cw * ld1 float2 (input, work, prefetch) + cw * ld1 float
 	template <class F1>
 	__global__ void __launch_bounds__(F1::kColsMaxThreads, F1::kColsMinBlocks) inv_cols_kernel(BatchedParams p) {

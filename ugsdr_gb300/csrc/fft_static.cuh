@@ -75,12 +75,25 @@ namespace ugsdr_gpu {
 	// emit.put<R, NS>(f, base, v) — v[r] is output element base + r * NS —
 	// instead of `out`.  Fusing the producer and consumer into the first and
 	// last passes saves a shared-memory round trip and a barrier each.
-	template <int N, int R, int NS, bool INV, bool FIRST, bool LAST, class Load, class Emit>
+	// The threads that run a pass together: the whole CTA (one __syncthreads
+	// between passes) or one warp owning its transforms (__syncwarp).
+	struct CtaGroup {
+		__device__ static int rank() { return threadIdx.x; }
+		__device__ static int size() { return blockDim.x; }
+		__device__ static void sync() { __syncthreads(); }
+	};
+	struct WarpGroup {
+		__device__ static int rank() { return threadIdx.x & 31; }
+		__device__ static int size() { return 32; }
+		__device__ static void sync() { __syncwarp(); }
+	};
+
+	template <int N, int R, int NS, bool INV, bool FIRST, bool LAST, class Load, class Emit, class G = CtaGroup>
 	__device__ __forceinline__ void hooked_pass(const float2* __restrict__ in, float2* __restrict__ out,
 		const float2* __restrict__ tw, int batch, int ld, Load& load, Emit& emit) {
 		constexpr int NB = N / R;
 		const int total = NB * batch;
-		for (int u = threadIdx.x; u < total; u += blockDim.x) {
+		for (int u = G::rank(); u < total; u += G::size()) {
 			const int f = u / NB;
 			const int j = u - f * NB;
 			const int k = NS == 1 ? 0 : j % NS;
@@ -122,20 +135,20 @@ namespace ugsdr_gpu {
 		__device__ void operator()() const {}
 	};
 
-	template <int N, int NS, bool INV, bool FIRST, int... Rs>
+	template <class G, int N, int NS, bool INV, bool FIRST, int... Rs>
 	struct HookedPasses;
 
-	template <int N, int NS, bool INV, bool FIRST, int R, int... Rest>
-	struct HookedPasses<N, NS, INV, FIRST, R, Rest...> {
+	template <class G, int N, int NS, bool INV, bool FIRST, int R, int... Rest>
+	struct HookedPasses<G, N, NS, INV, FIRST, R, Rest...> {
 		template <class Load, class Emit, class Mid>
 		__device__ static void run(float2* a, float2* b, const float2* tw, int batch, int ld, Load& load, Emit& emit, Mid& mid) {
 			constexpr bool LAST = sizeof...(Rest) == 0;
-			hooked_pass<N, R, NS, INV, FIRST, LAST>(a, b, tw, batch, ld, load, emit);
+			hooked_pass<N, R, NS, INV, FIRST, LAST, Load, Emit, G>(a, b, tw, batch, ld, load, emit);
 			if constexpr (!LAST) {
-				__syncthreads();
+				G::sync();
 				if constexpr (NS == 1)
 					mid();  // pass 0's input tile is free from here on
-				HookedPasses<N, NS * R, INV, false, Rest...>::run(b, a, tw + pass_table_size<NS, R>(), batch, ld, load, emit, mid);
+				HookedPasses<G, N, NS * R, INV, false, Rest...>::run(b, a, tw + pass_table_size<NS, R>(), batch, ld, load, emit, mid);
 			}
 		}
 	};
@@ -230,7 +243,14 @@ namespace ugsdr_gpu {
 		// `mid()` runs after the barrier that ends pass 0.
 		template <bool INV, bool FIRST, class Load, class Emit, class Mid>
 		__device__ static void run_hooked(float2* a, float2* b, const FftPlanDev& plan, int batch, int ld, Load& load, Emit& emit, Mid& mid) {
-			HookedPasses<N_, 1, INV, FIRST, Rs...>::run(a, b, plan.tw, batch, ld, load, emit, mid);
+			HookedPasses<CtaGroup, N_, 1, INV, FIRST, Rs...>::run(a, b, plan.tw, batch, ld, load, emit, mid);
+		}
+		// the same passes run by one warp over its own transforms (tiles private
+		// to the warp; the pass tables shared by the CTA)
+		template <bool INV, bool FIRST, class Load, class Emit, class Mid>
+		__device__ static void run_hooked_warp(float2* a, float2* b, const FftPlanDev& plan, int batch, int ld, Load& load, Emit& emit,
+			Mid& mid) {
+			HookedPasses<WarpGroup, N_, 1, INV, FIRST, Rs...>::run(a, b, plan.tw, batch, ld, load, emit, mid);
 		}
 		template <bool INV, bool FIRST, class Load, class Emit>
 		__device__ static void run_hooked(float2* a, float2* b, const FftPlanDev& plan, int batch, int ld, Load& load, Emit& emit) {

@@ -94,6 +94,7 @@ namespace ugsdr_gpu {
 		int cw = 0;         // columns per column-kernel CTA (natural layout)
 		int rw = 0;         // rows per row-kernel CTA
 		int warp_cols = -1; // 1: warp-owned column kernel where one is compiled, 0: natural layout
+		int warp_rows = -1; // 1: warp-owned row kernel with the warp-owned columns, 0: CTA row tiles
 	};
 
 	struct CodeEntry {

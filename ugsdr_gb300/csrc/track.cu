@@ -21,21 +21,25 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <map>
+#include <type_traits>
+#include <vector>
 
 namespace ugsdr_gpu {
 	namespace {
 		constexpr int kTrackThreads = 256;
-		constexpr int kWinChunk = 8192;   // samples per replica window (a multiple of kTrackThreads)
+		constexpr int kWinChunk = 4096;   // samples per chunk at most (a multiple of 4 x kTrackThreads)
 		constexpr int kWinPad = 128;      // window margin: taps within +-kWinPad samples of the prompt
-		constexpr int kMaxChunks = 32;    // chunks per epoch
+		constexpr int kWinFloats = kWinChunk + 2 * kWinPad + 8;  // one window: margins + 16-byte rounding
 		constexpr int kCopyChunkEpochs = 1000;  // host-buffer runs: epochs per overlapped copy
-		constexpr int kStageBytes = 32768;  // one staged sample chunk (two buffers, double-buffered)
+		constexpr int kStageBytes = 16384;  // one staged sample chunk (two buffers, double-buffered)
+		constexpr double kMaxRate = 131.072e6;  // 32 chunks of 4096 samples per epoch
 
 		template <int ST>
 		constexpr int sample_size() {
 			return ST == UGSDR_SAMPLES_CF32 ? 8 : ST == UGSDR_SAMPLES_CI16 ? 4 : ST == UGSDR_SAMPLES_CI8 ? 2 : 1;
 		}
-		// samples per chunk: the window's 8192, or fewer so a chunk fits one stage buffer
+		// samples per chunk: the window's 4096, or fewer so a chunk fits one stage buffer
 		template <int ST>
 		constexpr int chunk_samples() {
 			return kStageBytes / sample_size<ST>() < kWinChunk ? kStageBytes / sample_size<ST>() : kWinChunk;
@@ -54,6 +58,7 @@ namespace ugsdr_gpu {
 		struct TrackState {
 			// static
 			int code, len, period_ms, pad;
+			long long rep;          // the channel's replica table: offset in floats
 			double base;            // base code frequency
 			// dynamic (FP64 loop state; carrier phase as cycles * 2^64)
 			double code_phase, carrier_freq, carrier_phase_error, code_nco, code_error, code_freq;
@@ -77,8 +82,7 @@ namespace ugsdr_gpu {
 			double fs;
 			double offsets[5];      // chips: VE, E, P, L, VL
 			double k1_pll, k2_pll, k3_pll, k1_dll, k2_dll;
-			const float* chips;     // [code][len_max]
-			int len_max;
+			const float* replicas;  // replica tables (TrackState::rep)
 			const float* lut;
 			TrackState* states;
 			TrackOut* out;          // [epoch][channel] or null
@@ -115,56 +119,38 @@ namespace ugsdr_gpu {
 			return r;
 		}
 
-		// Full-code index q of the 3-period replica (tracker.hpp:48-49) maps to
-		// chip (q L3 / S3) mod len; an exact (chip, remainder) pair advances by
-		// adding the pair of the step.
-		struct ChipPos {
-			int chip;
-			unsigned int rem;
-		};
-		__device__ __forceinline__ ChipPos chip_add(ChipPos a, ChipPos b, unsigned int s3, int len) {
-			unsigned int r = a.rem + b.rem;
-			int c = a.chip + b.chip;
-			if (r >= s3) {
-				r -= s3;
-				++c;
-			}
-			if (c >= len)
-				c -= len;
-			return {c, r};
-		}
-		__device__ __forceinline__ ChipPos chip_of(unsigned long long q, unsigned long long L3, unsigned long long S3, int len) {
-			const unsigned long long num = q * L3;
-			return {static_cast<int>((num / S3) % static_cast<unsigned long long>(len)), static_cast<unsigned int>(num % S3)};
-		}
+		// correlation of four samples per thread: every tap's sample on the left
+		// of its CorrelateSplit split (kLeft), every one on the right (kRight), or
+		// per tap and with the chunk's bounds checked (kMixed)
+		enum { kLeft = 0, kRight = 1, kMixed = 2 };
 
 		template <int ST, bool STAGED>
 		__global__ void __launch_bounds__(kTrackThreads, 2) track_bank_kernel(TrackParams p) {
-			// The epoch is correlated in chunks of CH samples.  For each chunk the
-			// code replica is written once to s_win, from kWinPad samples before the
-			// prompt's first index; every tap reads it at its own offset (the
-			// replica is periodic in the code period, so a tap across the period
-			// boundary reads the same values).  STAGED: the chunk's samples are
-			// copied into one of two shared buffers by cp.async while the previous
-			// chunk (or the previous epoch's loop update) runs — the samples do not
-			// depend on the loop state, so the copies run one chunk ahead.
+			// The epoch is correlated in chunks of CH samples.  Chunk k's replica
+			// window is one contiguous slice of the channel's replica table (the
+			// code over three periods at the sampling rate, kWinPad samples of
+			// margin on each side), copied by cp.async into one of two shared
+			// windows one chunk ahead; every tap reads it at its own offset.
+			// STAGED: the chunk's samples are copied the same way into one of two
+			// stage buffers — the samples do not depend on the loop state, so they
+			// run one chunk ahead across epochs too, while the first window of an
+			// epoch waits for the loop update that places it.
 			constexpr int CH = chunk_samples<ST>();
 			constexpr int SB = sample_size<ST>();
-			extern __shared__ __align__(16) unsigned char s_stage[];  // STAGED: 2 x kStageBytes
-			__shared__ float s_win[kWinChunk + 2 * kWinPad];
+			extern __shared__ __align__(16) unsigned char s_dyn[];  // 2 windows, then (STAGED) 2 stage buffers
+			float* const s_win = reinterpret_cast<float*>(s_dyn);
+			unsigned char* const s_stage = s_dyn + 2 * kWinFloats * sizeof(float);
 			__shared__ float s_lut[80];
 			__shared__ float s_red[kTrackThreads / 32][20];
 			__shared__ float s_sum[20];
 			__shared__ unsigned long long s_holder0, s_adder;
 			__shared__ int s_mix;
-			__shared__ int s_first_len[5], s_off[5];
+			__shared__ int s_first_len[5], s_off[5], s_split_lo, s_split_hi;
 			__shared__ double s_rel[5];
-			__shared__ ChipPos s_wpos;                     // chip of the window start
-			__shared__ ChipPos s_cpos[kMaxChunks];         // chip step of chunk k's start
+			__shared__ long long s_wstart;  // replica-table index of chunk 0's window
 
 			TrackState* st = p.states + blockIdx.x;
-			const int len = st->len;
-			const float* chips = p.chips + static_cast<size_t>(st->code) * p.len_max;
+			const float* rep = p.replicas + st->rep;
 			for (int i = threadIdx.x; i < 80; i += blockDim.x)
 				s_lut[i] = p.lut[i];
 
@@ -173,14 +159,7 @@ namespace ugsdr_gpu {
 			const double period = static_cast<double>(spm) * period_ms;
 			const double inv_period = 1.0 / period, inv_spm = 1.0 / static_cast<double>(spm);
 			const long long P = static_cast<long long>(spm) * period_ms;
-			const unsigned long long L3 = 3ull * static_cast<unsigned long long>(len);
-			const unsigned long long S3 = static_cast<unsigned long long>(3 * period_ms * p.fs / 1e3);
-			const unsigned int s3 = static_cast<unsigned int>(S3);
-			const ChipPos tid_pos = chip_of(threadIdx.x, L3, S3, len);
-			const ChipPos step_pos = chip_of(blockDim.x, L3, S3, len);
 			const int n_chunks = (spm + CH - 1) / CH;
-			if (threadIdx.x < n_chunks)
-				s_cpos[threadIdx.x] = chip_of(static_cast<unsigned long long>(threadIdx.x) * CH, L3, S3, len);
 			const double spc = p.fs / st->base;
 			const double base_freq = st->base, inv_base = 1.0 / st->base, dll_scale = st->base / 1.023e6;
 			const int lane = threadIdx.x & 31;
@@ -228,6 +207,7 @@ namespace ugsdr_gpu {
 				const double code_phase = __shfl_sync(0xffffffffu, ls.code_phase, 0);
 				const long long epoch = __shfl_sync(0xffffffffu, ls.epoch, 0);
 				long long fp = 0;
+				int fl = 0;
 				if (lane < 5) {
 					const double ph = code_phase - p.fs / 1e3 * static_cast<double>(epoch % period_ms);
 					double q = ph + spc * p.offsets[lane];
@@ -235,11 +215,19 @@ namespace ugsdr_gpu {
 						q += period;
 					if (q > period)
 						q = mod_pos(q, period, inv_period);
-					s_first_len[lane] = static_cast<int>(static_cast<unsigned int>(ceil(q)) % static_cast<unsigned int>(spm));
+					fl = static_cast<int>(static_cast<unsigned int>(ceil(q)) % static_cast<unsigned int>(spm));
+					s_first_len[lane] = fl;
 					fp = static_cast<long long>(ceil(2 * period - q));
 					s_rel[lane] = mod_pos(q, static_cast<double>(spm), inv_spm) * inv_spm;
 				}
 				const long long fp2 = __shfl_sync(0xffffffffu, fp, 2);
+				// the taps' split points span [lo, hi): outside it every tap is on one side
+				int lo = lane < 5 ? fl : spm, hi = lane < 5 ? fl : 0;
+#pragma unroll
+				for (int o = 4; o > 0; o >>= 1) {
+					lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+					hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+				}
 				if (lane < 5) {
 					long long d = fp - fp2;  // reduced to the prompt's code period
 					while (d > P / 2)
@@ -247,16 +235,27 @@ namespace ugsdr_gpu {
 					while (d <= -P / 2)
 						d += P;
 					s_off[lane] = static_cast<int>(d) + kWinPad;
-					if (lane == 2)
-						s_wpos = chip_of(static_cast<unsigned long long>(fp2 - kWinPad), L3, S3, len);
+					if (lane == 2) {
+						// window entry j of the chunk at c0 is full-code index
+						// fp2 - kWinPad + c0 + j, replica-table index fp2 + c0 + j
+						s_wstart = fp2;
+						s_split_lo = lo;
+						s_split_hi = hi;
+					}
 				}
 			};
-			if (warp0) {
-				if (lane == 0)
-					nco_setup();
-				tap_setup();
-			}
-			// copy of global chunk gi = epoch * n_chunks + chunk into stage buffer gi & 1
+			// chunk k's window (n_c + 2 kWinPad entries from table index x0) into
+			// window buf: 16-byte copies from x0 rounded down to 4 entries (the
+			// table is padded for the rounded-up end)
+			auto fetch_window = [&](int buf, long long x0, int n_c) {
+				const long long a0 = x0 & ~3ll;
+				const int n_copy = (static_cast<int>(x0 - a0) + n_c + 2 * kWinPad + 3) & ~3;
+				float* dst = s_win + buf * kWinFloats;
+				const float* src = rep + a0;
+				for (int o = 4 * threadIdx.x; o < n_copy; o += 4 * blockDim.x)
+					cp_async_g<16>(dst + o, src + o);
+			};
+			// samples of global chunk gi = epoch * n_chunks + chunk into stage buffer gi & 1
 			const int total_chunks = p.n_epochs * n_chunks;
 			auto stage = [&](int gi) {
 				const int e = gi / n_chunks;
@@ -276,20 +275,25 @@ namespace ugsdr_gpu {
 					for (int o = threadIdx.x * 4; o < bytes; o += blockDim.x * 4)
 						cp_async_g<4>(dst + o, src + o);
 				}
-				cp_async_commit();
 			};
+			if (warp0) {
+				if (lane == 0)
+					nco_setup();
+				tap_setup();
+			}
 			if constexpr (STAGED)
 				stage(0);
-			__syncthreads();
+			__syncthreads();  // s_wstart of epoch 0
+			fetch_window(0, s_wstart, min(CH, spm));
+			cp_async_commit();
 
 			for (int ep = 0; ep < p.n_epochs; ++ep) {
-				int first_len[5], off[5];
+				int off[5];
 #pragma unroll
-				for (int t = 0; t < 5; ++t) {
-					first_len[t] = s_first_len[t];
+				for (int t = 0; t < 5; ++t)
 					off[t] = s_off[t];
-				}
-				const ChipPos wpos = s_wpos;
+				const long long wstart = s_wstart;
+				const int split_lo = s_split_lo, split_hi = s_split_hi;
 				float acc[20];
 #pragma unroll
 				for (int k = 0; k < 20; ++k)
@@ -303,53 +307,40 @@ namespace ugsdr_gpu {
 					const int c0 = k * CH;
 					const int n_c = min(CH, spm - c0);
 					const int gi = ep * n_chunks + k;
+					cp_async_wait_all();  // this chunk's window and samples (issued one chunk earlier)
+					__syncthreads();      // ... for every thread; the other buffers were last read by chunk gi - 1
+					if (k + 1 < n_chunks) {
+						fetch_window((gi + 1) & 1, wstart + c0 + CH, min(CH, spm - c0 - CH));
+						if constexpr (STAGED)
+							stage(gi + 1);
+						cp_async_commit();
+					}
+					else if (STAGED && gi + 1 < total_chunks) {
+						stage(gi + 1);  // the next epoch's first samples; its window follows the loop update
+						cp_async_commit();
+					}
 					const void* stage_buf = s_stage + (gi & 1) * kStageBytes;
-					// replica window of this chunk: entries j < n_c + 2 kWinPad
-					ChipPos pos = chip_add(chip_add(wpos, s_cpos[k], s3, len), tid_pos, s3, len);
-					const int n_win = n_c + 2 * kWinPad;
-					int j = threadIdx.x;
-					// eight chip-table loads in flight per thread: positions first, then loads
-					for (; j + 7 * static_cast<int>(blockDim.x) < n_win; j += 8 * blockDim.x) {
-						int cj[8];
-#pragma unroll
-						for (int u = 0; u < 8; ++u) {
-							cj[u] = pos.chip;
-							pos = chip_add(pos, step_pos, s3, len);
-						}
-						float vj[8];
-#pragma unroll
-						for (int u = 0; u < 8; ++u)
-							vj[u] = __ldg(chips + cj[u]);
-#pragma unroll
-						for (int u = 0; u < 8; ++u)
-							s_win[j + u * blockDim.x] = vj[u];
-					}
-					for (; j < n_win; j += blockDim.x) {
-						s_win[j] = __ldg(chips + pos.chip);
-						pos = chip_add(pos, step_pos, s3, len);
-					}
-					if constexpr (STAGED)
-						cp_async_wait_all();  // this chunk's samples (issued one chunk earlier)
-					__syncthreads();
-					if constexpr (STAGED) {
-						if (gi + 1 < total_chunks)
-							stage(gi + 1);  // its buffer was last read by chunk gi - 1, before the barrier
-					}
-					// correlate: four samples in flight per thread
-					for (int i0 = threadIdx.x; i0 < n_c; i0 += 4 * kTrackThreads) {
+					const float* win = s_win + (gi & 1) * kWinFloats + static_cast<int>((wstart + c0) & 3ll);
+					const int lo = split_lo - c0, hi = split_hi - c0;  // chunk-relative split span
+					auto correlate4 = [&](int i0, auto mode_tag) {
+						constexpr int MODE = decltype(mode_tag)::value;
 						float2 xs[4];
 #pragma unroll
 						for (int u = 0; u < 4; ++u) {
 							const int i = i0 + u * kTrackThreads;
+							if (MODE == kMixed && i >= n_c) {
+								xs[u] = c2(0.f, 0.f);
+								continue;
+							}
 							if constexpr (STAGED)
-								xs[u] = i < n_c ? load_sample<ST>(stage_buf, i) : c2(0.f, 0.f);
+								xs[u] = load_sample<ST>(stage_buf, i);
 							else
-								xs[u] = i < n_c ? load_sample<ST>(p.samples, base + c0 + i) : c2(0.f, 0.f);
+								xs[u] = load_sample<ST>(p.samples, base + c0 + i);
 						}
 #pragma unroll
 						for (int u = 0; u < 4; ++u) {
 							const int i = i0 + u * kTrackThreads;
-							if (i >= n_c)
+							if (MODE == kMixed && i >= n_c)
 								break;
 							float2 x = xs[u];
 							if (mix) {
@@ -358,12 +349,14 @@ namespace ugsdr_gpu {
 								x = c2(__fsub_rn(__fmul_rn(x.x, c), __fmul_rn(x.y, s)), __fadd_rn(__fmul_rn(x.x, s), __fmul_rn(x.y, c)));
 							}
 							holder += hstep;
-							const int sidx = c0 + i;
 #pragma unroll
 							for (int t = 0; t < 5; ++t) {
-								const float cv = s_win[i + off[t]];
-								// the two CorrelateSplit partial sums (warp-uniform except at the split)
-								if (sidx < first_len[t]) {
+								const float cv = win[i + off[t]];
+								// the two CorrelateSplit partial sums
+								bool left = MODE == kLeft;
+								if constexpr (MODE == kMixed)
+									left = c0 + i < s_first_len[t];
+								if (left) {
 									acc[4 * t] += x.x * cv;
 									acc[4 * t + 1] += x.y * cv;
 								}
@@ -373,8 +366,16 @@ namespace ugsdr_gpu {
 								}
 							}
 						}
+					};
+					for (int i0 = threadIdx.x; i0 < n_c; i0 += 4 * kTrackThreads) {
+						const int i3 = i0 + 3 * kTrackThreads;  // the thread's last sample of the four
+						if (i3 < n_c && i3 < lo)
+							correlate4(i0, std::integral_constant<int, kLeft>{});
+						else if (i3 < n_c && i0 >= hi)
+							correlate4(i0, std::integral_constant<int, kRight>{});
+						else
+							correlate4(i0, std::integral_constant<int, kMixed>{});
 					}
-					__syncthreads();
 				}
 				// block reduction of the 20 partial sums
 #pragma unroll
@@ -491,7 +492,11 @@ namespace ugsdr_gpu {
 					if (ep + 1 < p.n_epochs)
 						tap_setup();
 				}
-				__syncthreads();
+				__syncthreads();  // the next epoch's NCO and taps
+				if (ep + 1 < p.n_epochs) {
+					fetch_window(((ep + 1) * n_chunks) & 1, s_wstart, min(CH, spm));
+					cp_async_commit();
+				}
 			}
 			if (threadIdx.x == 0) {
 				st->code_phase = ls.code_phase;
@@ -514,13 +519,12 @@ using namespace ugsdr_gpu;
 struct ugsdr_track_bank {
 	ugsdr_ctx* ctx = nullptr;
 	int n_channels = 0;
-	int len_max = 0;
 	double fs = 0;
 	size_t spm = 0;
 	double offsets[5] = {};
 	double k1_pll = 0, k2_pll = 0, k3_pll = 0, k1_dll = 0, k2_dll = 0;
 	int nco_mode = 0;
-	DevBuf chips, states;
+	DevBuf replicas, states;
 };
 
 namespace {
@@ -566,8 +570,7 @@ namespace {
 		p.k1_dll = bank->k1_dll;
 		p.k2_dll = bank->k2_dll;
 		p.nco_mode = bank->nco_mode;
-		p.chips = bank->chips.as<float>();
-		p.len_max = bank->len_max;
+		p.replicas = bank->replicas.as<float>();
 		p.lut = get_lut(ctx);
 		p.states = bank->states.as<TrackState>();
 		p.out = dev_out;
@@ -582,16 +585,13 @@ namespace {
 				break;
 			}
 		const dim3 grid(bank->n_channels), block(kTrackThreads);
-		const size_t smem = p.stage_g ? 2 * kStageBytes : 0;
+		const size_t smem_win = 2 * sizeof(float) * kWinFloats;
+		const size_t smem = smem_win + (p.stage_g ? 2 * kStageBytes : 0);
 		KernelTimer timer(ctx, "track_bank");
 		auto launch = [&](auto staged_kernel, auto direct_kernel) {
-			if (p.stage_g) {
-				UG_CUDA(cudaFuncSetAttribute(staged_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
-				staged_kernel<<<grid, block, smem, ctx->stream>>>(p);
-			}
-			else {
-				direct_kernel<<<grid, block, 0, ctx->stream>>>(p);
-			}
+			auto kernel = p.stage_g ? staged_kernel : direct_kernel;
+			UG_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+			kernel<<<grid, block, smem, ctx->stream>>>(p);
 		};
 		switch (sample_type) {
 		case UGSDR_SAMPLES_CF32:
@@ -652,12 +652,10 @@ int ugsdr_track_create(ugsdr_ctx* ctx, const ugsdr_track_config* cfg, const ugsd
 		auto b = std::make_unique<ugsdr_track_bank>();
 		b->ctx = ctx;
 		b->n_channels = n_channels;
-		b->len_max = code_len_max;
 		b->fs = channels[0].sampling_rate;
 		require(b->fs > 0 && std::fmod(b->fs, 1e3) == 0.0, "sampling rate must be a whole number of kHz");
 		b->spm = static_cast<size_t>(b->fs / 1e3);
-		require(b->spm >= 2 * kWinPad && b->spm <= static_cast<size_t>(kMaxChunks) * (kStageBytes / 8),
-			"sampling rate must be between 256 kHz and 131.072 MHz");
+		require(b->spm >= 2 * kWinPad && b->fs <= kMaxRate, "sampling rate must be between 256 kHz and 131.072 MHz");
 		const double el = cfg->early_late_spacing, vel = cfg->very_early_late_spacing;
 		const double offs[5] = {vel, el, 0.0, -el, -vel};
 		std::memcpy(b->offsets, offs, sizeof(offs));
@@ -704,9 +702,38 @@ int ugsdr_track_create(ugsdr_ctx* ctx, const ugsdr_track_config* cfg, const ugsd
 			s.phase_rad = ch.carrier_phase;
 			st[c] = s;
 		}
-		b->chips.reserve(sizeof(float) * static_cast<size_t>(n_codes) * code_len_max);
+		// replica tables, one per (code, period): the code repeated over three
+		// periods and upsampled as Codes::FillCodesImpl does (tracker.hpp:40-50:
+		// full-code index q takes chip floor(q L3 / S3) mod len, L3 = 3 len,
+		// S3 = 3 P), stored from q = -kWinPad to 3 P + kWinPad + 16 (periodic
+		// beyond the three periods), each table 16-byte aligned
+		std::vector<float> tables;
+		std::map<std::pair<int, int>, long long> where;
+		for (auto& s : st) {
+			const auto key = std::make_pair(s.code, s.period_ms);
+			auto it = where.find(key);
+			if (it == where.end()) {
+				const unsigned long long P = b->spm * static_cast<unsigned long long>(s.period_ms);
+				const unsigned long long L3 = 3ull * static_cast<unsigned long long>(s.len), S3 = 3 * P;
+				const size_t n_tab = (3 * P + 2 * kWinPad + 16 + 3) / 4 * 4;
+				const long long at = static_cast<long long>(tables.size());
+				tables.resize(tables.size() + n_tab);
+				const float* chips = codes + static_cast<size_t>(s.code) * code_len_max;
+				for (size_t x = 0; x < n_tab; ++x) {
+					long long q = static_cast<long long>(x) - kWinPad;
+					q %= static_cast<long long>(S3);
+					if (q < 0)
+						q += static_cast<long long>(S3);
+					const unsigned long long chip = (static_cast<unsigned long long>(q) * L3 / S3) % static_cast<unsigned long long>(s.len);
+					tables[static_cast<size_t>(at) + x] = chips[chip];
+				}
+				it = where.emplace(key, at).first;
+			}
+			s.rep = it->second;
+		}
+		b->replicas.reserve(sizeof(float) * tables.size());
 		b->states.reserve(sizeof(TrackState) * n_channels);
-		UG_CUDA(cudaMemcpy(b->chips.ptr, codes, sizeof(float) * static_cast<size_t>(n_codes) * code_len_max, cudaMemcpyHostToDevice));
+		UG_CUDA(cudaMemcpy(b->replicas.ptr, tables.data(), sizeof(float) * tables.size(), cudaMemcpyHostToDevice));
 		UG_CUDA(cudaMemcpy(b->states.ptr, st.data(), sizeof(TrackState) * n_channels, cudaMemcpyHostToDevice));
 		*bank = b.release();
 	});
