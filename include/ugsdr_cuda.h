@@ -243,12 +243,12 @@ int ugsdr_tile_get(ugsdr_ctx* ctx, size_t block_samples, ugsdr_tile_shape* shape
  * search of that size is in flight. */
 int ugsdr_tile_set(ugsdr_ctx* ctx, size_t block_samples, const ugsdr_tile_shape* shape);
 /* Autotuner: for every block size above the single-CTA limit among `jobs`,
- * runs those jobs (Doppler grids cut to about 4e9 complex points per search)
+ * runs those jobs (Doppler grids cut to about 1.6e10 complex points per search)
  * with candidate shapes and keeps the fastest: the split (the rule's, the
  * next smaller divisor, the rule's transposed), then the column kernel and
  * its width, then the row kernel and the rows per row CTA, each stage from
  * the best so far; the
- * rule's shape stays unless another is 1.5 % faster.  Each candidate runs
+ * rule's shape stays unless another is 3 % faster.  Each candidate runs
  * once untimed and twice timed with CUDA events (the best counts).  tried
  * receives up to max_tried measured shapes, n_tried (may be NULL) their
  * number.  Same caveat as ugsdr_tile_set for in-flight searches. */

@@ -121,7 +121,7 @@ def test_autotune_keeps_a_measured_shape(ctx, oracle, golden_codes):
             best = min(t["ms"] for t in mine)
             kept_ms = [t["ms"] for t in mine if key(t) == key(kept)][0]
             if key(kept) != key(mine[0]):  # mine[0]: the rule's shape, measured first
-                assert kept_ms == best and kept_ms < 0.985 * mine[0]["ms"]
+                assert kept_ms == best and kept_ms < 0.97 * mine[0]["ms"]
             print(f"N={n}: kept {kept} of {len(mine)} shapes ({kept_ms:.3f} ms; rule {mine[0]['ms']:.3f} ms)")
         res, _ = ctx.acquire(jobs[0], cells=True)
         for p, r in zip(prns, res):

@@ -1007,10 +1007,14 @@ namespace ugsdr_gpu {
 
 	// ------------------------------------------------------------ tile tuning
 	namespace {
-		// complex points (rows x K x N) of one tuning search: 20 - 60 ms on the device
-		constexpr double kTunePoints = 4e9;
+		// complex points (rows x K x N) of one tuning search, 0.1 - 0.2 s on the
+		// device: many full inverse batches, so that a shape that only wins on
+		// a short search's tail does not get picked (a 4e9-point cut of the
+		// 204,600-point L5 search picked 2-column tiles that ran its full
+		// search 3.5 % slower than the rule)
+		constexpr double kTunePoints = 1.6e10;
 		// a tuned shape replaces the rule only when it is this much faster
-		constexpr double kTuneMargin = 0.985;
+		constexpr double kTuneMargin = 0.97;
 
 		ugsdr_tile_shape effective_shape(ugsdr_ctx* ctx, int n) {
 			const LargePlan& lp = get_large_plan(ctx, n);
