@@ -247,9 +247,9 @@ int ugsdr_tile_set(ugsdr_ctx* ctx, size_t block_samples, const ugsdr_tile_shape*
  * with candidate shapes and keeps the fastest: the split (the rule's, the
  * next smaller divisor, the rule's transposed), then the column kernel and
  * its width, then the row kernel and the rows per row CTA, each stage from
- * the best so far; the
- * rule's shape stays unless another is 3 % faster.  Each candidate runs
- * once untimed and twice timed with CUDA events (the best counts).  tried
+ * the best so far; the rule's shape stays unless another is 3 % faster.
+ * Each candidate runs once untimed and twice timed with CUDA events (the
+ * best counts).  tried
  * receives up to max_tried measured shapes, n_tried (may be NULL) their
  * number.  Same caveat as ugsdr_tile_set for in-flight searches. */
 int ugsdr_autotune(ugsdr_ctx* ctx, const ugsdr_acq_job* jobs, int n_jobs, ugsdr_tile_shape* tried, int max_tried,
