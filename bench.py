@@ -14,6 +14,7 @@ at a load the GPU carries (--no-served skips it).  Other lines:
   --config track         256-channel tracking bank, 10 s at 20 MHz
   --config jamming       interference stage, 400 ms at 50 MHz
   --config observables   observables + preamble search, 256 ch x 60,000 epochs
+  --config dft25         the radix-25 DFT stage: CUDA-core butterfly vs tcgen05 3xTF32
   --served               the Poisson request stream through the server
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
@@ -1302,13 +1303,67 @@ def run_reference(args, world, rank):
     }
 
 
+# ------------------------------------------------------------- DFT stage
+DFT25_TRANSFORMS = 1 << 22  # 1.05e8 points, 839 MB each way (> L2)
+
+
+def run_dft25(args, world, rank):
+    """The radix-25 DFT stage two ways (ugsdr_dft25_batch): the CUDA-core
+    butterfly (the transforms' choice, `value`) and the tcgen05 3xTF32
+    product (`tensor_cores`), each over 2^22 transforms of device data; the
+    kernel times are the entry's CUDA events, best over the steps."""
+    import ctypes as C
+
+    import torch
+    from ugsdr_gb300 import api
+
+    dev = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(dev)
+    ctx = api.Context(dev)
+    n = DFT25_TRANSFORMS
+    x = torch.randn(n * 50, device=f"cuda:{dev}")
+    y = torch.empty_like(x)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{dev}")
+    res = {}
+    with ClockSampler() as clk:
+        for method in (0, 1):
+            times = []
+            for step in range(args.warmup + args.steps):
+                flush.zero_()
+                ms = C.c_float()
+                ctx._check(ctx.lib.ugsdr_dft25_batch(ctx.h, C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()), n, method,
+                                                     C.byref(ms)))
+                if step >= args.warmup:
+                    times.append(ms.value)
+            res[method] = min(times)
+    pts = n * 25
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    gbs = 16 * pts / (res[0] / 1e3) / 1e9  # 8 B read + 8 B written per point
+    ctx.close()
+    return {
+        "metric": "25-point DFT stage points/s", "value": pts / (res[0] / 1e3), "unit": "points/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": res[0], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (normal random complex input on the device)",
+        "config": {"workload": f"{n} forward 25-point DFTs (the radix-25 butterfly of the four-step inverse), "
+                               "device in / out, tiles of 128 transforms staged in shared memory",
+                   "l2": "flushed between steps (256 MB write); data 839 MB each way > L2"},
+        "e2e": None, "gpu_launches": 1,
+        "roofline": {"bound": "hbm", "kernel": "dft25_cuda_kernel", "achieved": gbs, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": gbs / hbm_peak, "traffic": None},
+        "tensor_cores": {"kernel": "dft25_tc_kernel (tcgen05.mma kind::tf32, 3xTF32, M128 N64 K8 x 21 per tile)",
+                         "value": pts / (res[1] / 1e3), "ms_per_step": res[1], "ratio_to_cuda_cores": res[0] / res[1]},
+        "clocks": clk.summary(),
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--config", choices=sorted(WORKLOADS) + ["track", "jamming", "observables"], default="multi")
+    ap.add_argument("--config", choices=sorted(WORKLOADS) + ["track", "jamming", "observables", "dft25"], default="multi")
     ap.add_argument("--track-seconds", type=float, default=10.0, help="capture length of --config track")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-served", action="store_true", help="skip the served section of the default line")
@@ -1334,6 +1389,8 @@ def main():
         line = run_jamming(args, world, rank)
     elif args.config == "observables":
         line = run_observables(args, world, rank)
+    elif args.config == "dft25":
+        line = run_dft25(args, world, rank) if rank == 0 else None
     else:
         line = run_ours(args, world, rank) if args.impl == "ours" else run_reference(args, world, rank)
     if rank == 0 and line is not None:

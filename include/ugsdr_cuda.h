@@ -315,6 +315,14 @@ int ugsdr_mix(ugsdr_ctx* ctx, float* iq, size_t n, double fs, double frequency, 
 /* SequentialDft::Transform on complex data (src/math/dft.hpp:114-135, 211-220):
  * forward unnormalised, inverse scaled 2/N (FFTW path). */
 int ugsdr_dft(ugsdr_ctx* ctx, const float* in_iq, float* out_iq, size_t n, int inverse);
+/* No counterpart in the reference: a measurement entry.  `count` 25-point
+ * forward DFTs (the radix-25 butterfly of the four-step inverse) of device
+ * complex-float data, in[i * 25 + j] -> out[i * 25 + k], computed on the CUDA
+ * cores (the butterfly the transforms use) or on the tensor cores (tcgen05,
+ * 3xTF32 split, one 128 x 64 x 56 product per 128 transforms); kernel_ms
+ * (may be NULL) receives the kernel's CUDA-event time. */
+enum ugsdr_dft25_method { UGSDR_DFT25_CUDA_CORES = 0, UGSDR_DFT25_TENSOR_CORES = 1 };
+int ugsdr_dft25_batch(ugsdr_ctx* ctx, const void* in, void* out, size_t count, int method, float* kernel_ms);
 /* MatchedFilter::PrepareCodeSpectrum (src/matched_filter/matched_filter.hpp:27-30, 49-54). */
 int ugsdr_matched_filter_prepare(ugsdr_ctx* ctx, const float* code, size_t n, int spectrum_mode, float* spectrum_iq);
 /* MatchedFilter::FilterOptimized (matched_filter.hpp:32-35, 56-61), in place. */

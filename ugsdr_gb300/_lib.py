@@ -165,6 +165,7 @@ SIGNATURES = {
     "ugsdr_acquire": (_i, [_vp, C.POINTER(AcqJob), C.POINTER(AcqResult), C.POINTER(AcqCell)]),
     "ugsdr_acquire_batch": (_i, [_vp, C.POINTER(AcqJob), _i, C.POINTER(C.POINTER(AcqResult))]),
     "ugsdr_doppler_bins": (_i, [_d, _d, C.POINTER(_u32)]),
+    "ugsdr_dft25_batch": (_i, [_vp, _vp, _vp, _sz, _i, C.POINTER(C.c_float)]),
     "ugsdr_tile_get": (_i, [_vp, _sz, C.POINTER(TileShape)]),
     "ugsdr_tile_set": (_i, [_vp, _sz, C.POINTER(TileShape)]),
     "ugsdr_autotune": (_i, [_vp, C.POINTER(AcqJob), _i, C.POINTER(TileShape), _i, C.POINTER(_i)]),

@@ -24,7 +24,7 @@ ORACLE = ROOT / "oracle"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "--expt-relaxed-constexpr", "-O3", "-lineinfo", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-ffp-contract=off", "-I", str(ROOT / "include")]
-SOURCES = ["acq.cu", "ops.cu", "ctx.cu", "track.cu", "serve.cpp", "codes.cpp", "noalloc.cu", "refine.cpp", "jamming.cu", "observables.cu"]
+SOURCES = ["acq.cu", "ops.cu", "ctx.cu", "track.cu", "serve.cpp", "codes.cpp", "noalloc.cu", "refine.cpp", "jamming.cu", "observables.cu", "tc_dft.cu"]
 
 
 def nvcc() -> str:
