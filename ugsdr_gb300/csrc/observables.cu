@@ -32,6 +32,7 @@ namespace ugsdr_gpu {
 		constexpr int kMaxPreambleSymbols = 40;
 		constexpr int kMaxPreambleLen = 400;   // symbols x upsampling, GLONASS
 		constexpr double kTwoPi = 6.283185307179586476925286766559;
+		constexpr double kInvTwoPi = 1.0 / kTwoPi;
 
 		// Preambles as +-1 symbols per 20 ms (GPS) or 10 ms (GLONASS):
 		// GetPreambleGps (observable.hpp:92-94), the LNAV preamble 10001011;
@@ -157,38 +158,59 @@ namespace ugsdr_gpu {
 			return f * 1e-3 + rec(p, e, c).phase_error * 0.25;
 		}
 
+		// One warp per channel, launched as 2-warp CTAs so the channels spread
+		// over every SM: each lane loads 8 epochs of a 256-epoch group (32
+		// apart) and the next group's 8 while the current group's 256 values are
+		// added in epoch order (every lane replays the same serial adds), so 16
+		// record loads per lane are in flight behind one dependent add chain.
+		constexpr int kSigmaWarps = 2;
 		__global__ void __launch_bounds__(kObsThreads) obs_sigma_kernel(ObsParams p) {
-			const int c = blockIdx.x * kObsWarps + (threadIdx.x >> 5);
+			const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
 			const int lane = threadIdx.x & 31;
 			if (c >= p.n_channels)
 				return;
 			const int n = p.n_epochs;
 			float q = 0.f, m = 0.f;
-			float v = lane < n ? rec(p, lane, c).taps[2][1] : 0.f;
-			for (int e0 = 0; e0 < n; e0 += 32) {
-				const int nx = e0 + 32 + lane;
-				const float v_next = nx < n ? rec(p, nx, c).taps[2][1] : 0.f;
-				const int cnt = min(32, n - e0);
-				if (cnt == 32) {
-					// all 32 shuffles issue ahead of the two serial add chains
-					float x[32];
+			float cur[8], nxt[8];
+			auto load_group = [&](int g, float (&v)[8]) {
 #pragma unroll
-					for (int j = 0; j < 32; ++j)
-						x[j] = __shfl_sync(0xffffffffu, v, j);
+				for (int j = 0; j < 8; ++j) {
+					const int e = g * 256 + j * 32 + lane;
+					v[j] = e < n ? rec(p, e, c).taps[2][1] : 0.f;
+				}
+			};
+			load_group(0, cur);
+			for (int g = 0; g * 256 < n; ++g) {
+				load_group(g + 1, nxt);
 #pragma unroll
-					for (int j = 0; j < 32; ++j) {
-						q = __fadd_rn(q, __fmul_rn(x[j], x[j]));
-						m = __fadd_rn(m, x[j]);
+				for (int j = 0; j < 8; ++j) {
+					const int e0 = g * 256 + j * 32;
+					const int cnt = min(32, n - e0);
+					if (cnt <= 0)
+						break;
+					if (cnt == 32) {
+						// all 32 shuffles issue ahead of the two serial add chains
+						float x[32];
+#pragma unroll
+						for (int k = 0; k < 32; ++k)
+							x[k] = __shfl_sync(0xffffffffu, cur[j], k);
+#pragma unroll
+						for (int k = 0; k < 32; ++k) {
+							q = __fadd_rn(q, __fmul_rn(x[k], x[k]));
+							m = __fadd_rn(m, x[k]);
+						}
+					}
+					else {
+						for (int k = 0; k < cnt; ++k) {
+							const float x = __shfl_sync(0xffffffffu, cur[j], k);
+							q = __fadd_rn(q, __fmul_rn(x, x));
+							m = __fadd_rn(m, x);
+						}
 					}
 				}
-				else {
-					for (int j = 0; j < cnt; ++j) {
-						const float x = __shfl_sync(0xffffffffu, v, j);
-						q = __fadd_rn(q, __fmul_rn(x, x));
-						m = __fadd_rn(m, x);
-					}
-				}
-				v = v_next;
+#pragma unroll
+				for (int j = 0; j < 8; ++j)
+					cur[j] = nxt[j];
 			}
 			if (lane == 0) {
 				float s = 0.f;
@@ -252,7 +274,9 @@ namespace ugsdr_gpu {
 				const ugsdr_track_output& r = rec(p, e, c);
 				// the bank keeps the phase as a 64-bit fraction of a cycle:
 				// its whole cycles come from the running sum
-				const double wrapped = r.carrier_phase / kTwoPi;
+				// (times 1 / 2 pi: the FP64 division would be this pass's costliest
+				// operation; the cycles differ from the quotient by an ulp)
+				const double wrapped = r.carrier_phase * kInvTwoPi;
 				const double cycles = rint(approx - wrapped) + wrapped;
 				ugsdr_observable o;
 				o.pseudorange = __dadd_rn(__dsub_rn(__dmul_rn(r.code_phase, ch.samples_to_ms),
@@ -363,7 +387,7 @@ int ugsdr_observables(ugsdr_ctx* ctx, const ugsdr_track_output* outputs, int out
 		ObsParams p{d_out, n_epochs, n_channels, n_segments, d_ch, d_sigma, d_seg, d_obs};
 		{
 			KernelTimer timer(ctx, "observables");
-			obs_sigma_kernel<<<blocks_for_warps(n_channels), kObsThreads, 0, ctx->stream>>>(p);
+			obs_sigma_kernel<<<(n_channels + kSigmaWarps - 1) / kSigmaWarps, 32 * kSigmaWarps, 0, ctx->stream>>>(p);
 			obs_segsum_kernel<<<blocks_for_warps(static_cast<long long>(segs)), kObsThreads, 0, ctx->stream>>>(p);
 			obs_emit_kernel<<<blocks_for_warps(static_cast<long long>(segs)), kObsThreads, 0, ctx->stream>>>(p);
 			UG_CUDA(cudaGetLastError());
