@@ -336,6 +336,9 @@ struct ugsdr_server {
 		}
 		lock.lock();
 		free_slot->enqueuing = false;
+		// the retirement thread sleeps 5 ms while nothing is in flight: wake it
+		// to poll this slot (a short search completes in well under that)
+		cv_reap.notify_one();
 		if (fail_status != UGSDR_OK) {
 			if (r->kind == 1)
 				busy_banks.erase(r->bank);
