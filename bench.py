@@ -308,7 +308,7 @@ def run_ours(args, world, rank):
         kept_ms = next((x["ms"] for x in tried if x["block_samples"] == n and all(x[k] == t[k] for k in key)), None)
         tiles[str(n)] = {"split": f"{t['n1']}x{n // t['n1']}", "cols": t["cols"], "rows": t["rows"],
                          "column_kernel": "warp-owned" if t["warp_cols"] else "tile",
-                         "row_kernel": "warp-owned" if t["warp_rows"] else "tile",
+                         "row_kernel": {0: "tile", 1: "warp-owned", 2: "warp-owned, 3 rows/warp, code via L2"}[t["warp_rows"]],
                          "shapes_timed": sum(1 for x in tried if x["block_samples"] == n),
                          "rule_ms": rule_ms, "kept_ms": kept_ms}
 

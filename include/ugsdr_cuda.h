@@ -230,7 +230,8 @@ typedef struct ugsdr_tile_shape {
 	int warp_cols;   /* 1: warp-owned column kernel where one is compiled for the split, 0: one tile of
 	                    `cols` columns per CTA, -1: rule (the warp-owned kernel where compiled) */
 	int warp_rows;   /* 1: warp-owned row kernel (with the warp-owned columns; each warp takes whole rows through
-	                    both passes), 0: rows in CTA tiles of `rows` rows, -1: rule (warp-owned where compiled) */
+	                    both passes, code rows staged), 2: the same with three rows per warp and the code rows read
+	                    through L1 / L2, 0: rows in CTA tiles of `rows` rows, -1: rule (1 where compiled) */
 	int block_samples; /* N the shape is for (filled by ugsdr_tile_get / ugsdr_autotune, ignored by ugsdr_tile_set) */
 	double ms;       /* ugsdr_autotune: device time of the tuning search with this shape */
 } ugsdr_tile_shape;

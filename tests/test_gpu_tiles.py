@@ -5,7 +5,8 @@ Every shape the autotuner may pick runs the same search: peak index and
 Doppler bin equal to the oracle's, level, mean, sigma and SNR within 1e-4
 of the FP64 oracle, on the compile-time 200 x 250 split of a 50,000-point
 block (warp-owned and natural column kernels, 8 / 4 / 2 columns, 8 / 4 / 2
-rows, warp-owned and CTA-tile row kernels) and on the runtime splits of a 16,000-point block (125 x 128, its
+rows, warp-owned row kernels with staged or L2 code rows and CTA-tile row
+kernels) and on the runtime splits of a 16,000-point block (125 x 128, its
 transpose, 100 x 160), whose code spectra were cached under another split
 and are rebuilt by the change.  The tuner keeps a shape it measured and
 the search still matches the oracle after tuning."""
@@ -20,7 +21,7 @@ from ugsdr_gb300 import signals
 pytestmark = pytest.mark.gpu
 
 SHAPES_50K = ([dict(cols=c, rows=r, warp_cols=w, warp_rows=0) for w in (1, 0) for c in (8, 4, 2) for r in (8, 4, 2)] +
-              [dict(cols=c, rows=r, warp_cols=1, warp_rows=1) for c in (8, 2) for r in (8, 2)])
+              [dict(cols=c, rows=r, warp_cols=1, warp_rows=w) for w in (1, 2) for c in (8, 2) for r in (8, 2)])
 KEY = ("n1", "cols", "rows", "warp_cols", "warp_rows")
 
 

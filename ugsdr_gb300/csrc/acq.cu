@@ -239,9 +239,11 @@ namespace ugsdr_gpu {
 		template <int N2>
 		constexpr int kRowsPerWarp = N2 <= 256 ? 3 : 1;
 		constexpr int kRowsWarps = 4;
-		bool warp_rows_on(ugsdr_ctx* ctx, int n) {
+		// 0: CTA row tiles; 1: warp-owned rows (the rule); 2: warp-owned, three
+		// rows per warp, code rows through L1 / L2
+		int warp_rows_mode(ugsdr_ctx* ctx, int n) {
 			const auto t = ctx->tiles.find(n);
-			return t == ctx->tiles.end() || t->second.warp_rows != 0;
+			return t == ctx->tiles.end() || t->second.warp_rows < 0 ? 1 : t->second.warp_rows;
 		}
 
 		// columns per column-kernel CTA of the blocked layout (0: natural layout)
@@ -479,18 +481,25 @@ namespace ugsdr_gpu {
 					constexpr int CW = P::CW;
 					// the row plan that pairs with the column plan: N = N1 x N2
 					if constexpr (F2::kHooked && ((P::N1 == 400 && F2::N == 500) || (P::N1 == 200 && F2::N == 250))) {
-						if (warp_rows_on(ctx, s.n)) {
-							// warp-owned rows: RPW rows per warp, four warps per CTA
+						const int wr = warp_rows_mode(ctx, s.n);
+						if (wr != 0) {
+							// warp-owned rows, four warps per CTA: RPW rows per warp with
+							// the code rows staged (mode 1), or three rows per warp with
+							// the code rows read through L1 / L2 (mode 2)
+							auto launch_rows = [&](auto rows_kernel, int rpw, size_t smem_r) {
+								set_smem(rows_kernel, smem_r);
+								set_smem(inv_cols_warp_kernel<P>, P::smem_bytes());
+								KernelTimer timer(ctx, "acq_inverse_large");
+								run_batches([&] {
+									rows_kernel<<<p.rows * chunks_of(p.n1, rpw * kRowsWarps), 32 * kRowsWarps, smem_r, ctx->stream>>>(p);
+									inv_cols_warp_kernel<P><<<p.rows * chunks, 32 * P::WARPS, P::smem_bytes(), ctx->stream>>>(p);
+								});
+							};
 							constexpr int RPW = kRowsPerWarp<F2::N>, W = kRowsWarps;
-							auto rows_kernel = inv_rows_warp_kernel<F2, CW, P::N1, RPW, W>;
-							constexpr size_t smem_r = rows_warp_smem<F2, RPW, W>();
-							set_smem(rows_kernel, smem_r);
-							set_smem(inv_cols_warp_kernel<P>, P::smem_bytes());
-							KernelTimer timer(ctx, "acq_inverse_large");
-							run_batches([&] {
-								rows_kernel<<<p.rows * chunks_of(p.n1, RPW * W), 32 * W, smem_r, ctx->stream>>>(p);
-								inv_cols_warp_kernel<P><<<p.rows * chunks, 32 * P::WARPS, P::smem_bytes(), ctx->stream>>>(p);
-							});
+							if (wr == 2)
+								launch_rows(inv_rows_warp_kernel<F2, CW, P::N1, 3, W, false>, 3, rows_warp_smem<F2, 3, W, false>());
+							else
+								launch_rows(inv_rows_warp_kernel<F2, CW, P::N1, RPW, W>, RPW, rows_warp_smem<F2, RPW, W>());
 							return;
 						}
 						const size_t smem_r = smem_inv_rows<F2>(p);
@@ -1024,7 +1033,7 @@ namespace ugsdr_gpu {
 			t.warp_cols = blocked_cw(ctx, n, lp.n1, lp.n2, 0) ? 1 : 0;
 			// the warp-owned row kernel runs with the warp-owned columns of the
 			// 200 x 250 and 400 x 500 splits
-			t.warp_rows = t.warp_cols && warp_rows_on(ctx, n) ? 1 : 0;
+			t.warp_rows = t.warp_cols ? warp_rows_mode(ctx, n) : 0;
 			t.block_samples = n;
 			return t;
 		}
@@ -1067,7 +1076,7 @@ namespace ugsdr_gpu {
 		void apply_tiles(ugsdr_ctx* ctx, int n, const TileChoice& t) {
 			require(!fits_single_cta(ctx, n), "block size runs on the single-CTA path (no four-step tiles)", UGSDR_E_INVALID);
 			auto pow2 = [](int v) { return v == 0 || v == 1 || v == 2 || v == 4 || v == 8; };
-			require(pow2(t.cw) && pow2(t.rw) && t.warp_cols >= -1 && t.warp_cols <= 1 && t.warp_rows >= -1 && t.warp_rows <= 1,
+			require(pow2(t.cw) && pow2(t.rw) && t.warp_cols >= -1 && t.warp_cols <= 1 && t.warp_rows >= -1 && t.warp_rows <= 2,
 				"tile shape out of range");
 			require(t.n1 == 0 || split_fits(ctx, n, t.n1, 1), "no four-step split " + std::to_string(t.n1) + " for FFT size " +
 				std::to_string(n), UGSDR_E_UNSUPPORTED);
@@ -1213,7 +1222,7 @@ namespace ugsdr_gpu {
 					consider(t);
 				}
 			const TileChoice cols = best;
-			for (const int wr : {1, 0})
+			for (const int wr : {1, 2, 0})
 				for (const int rw : {8, 4, 2}) {
 					TileChoice t = cols;
 					t.warp_rows = wr;

@@ -707,15 +707,18 @@ namespace ugsdr_gpu {
 	// (staged once) and its work tile are private to it; the pass tables and
 	// the twiddle seeds are built once per CTA.  B goes out in the blocked
 	// layout of inv_cols_warp_kernel.  grid: rows * ceil(N1 / (RPW WARPS)).
-	template <class F2, int RPW, int WARPS>
+	// CODE: the code rows staged in shared memory (else read through L1 / L2,
+	// which leaves room for more rows per warp)
+	template <class F2, int RPW, int WARPS, bool CODE = true>
 	constexpr size_t rows_warp_smem() {
-		return sizeof(float2) * (3 * static_cast<size_t>(WARPS) * RPW * F2::N + F2::N + static_cast<size_t>(WARPS) * RPW * (F2::kLastNS + 1)) + 16;
+		return sizeof(float2) * ((CODE ? 3 : 2) * static_cast<size_t>(WARPS) * RPW * F2::N + F2::N +
+			static_cast<size_t>(WARPS) * RPW * (F2::kLastNS + 1)) + 16;
 	}
-	template <class F2, int BCW, int BN1, int RPW, int WARPS>
+	template <class F2, int BCW, int BN1, int RPW, int WARPS, bool CODE = true>
 	__global__ void __launch_bounds__(32 * WARPS) inv_rows_warp_kernel(BatchedParams p) {
 		static_assert(F2::kHooked && F2::kPasses == 2, "warp-owned rows run two-pass hooked plans (one work tile)");
 		extern __shared__ float2 smem[];
-		constexpr int N2 = F2::N, NS = F2::kLastNS, RW = RPW * WARPS, WT = RPW * N2;
+		constexpr int N2 = F2::N, NS = F2::kLastNS, RW = RPW * WARPS, WT = RPW * N2, TILES = CODE ? 3 : 2;
 		const AcqParams& q = p.base;
 		const int n1 = p.n1, n = q.n;
 		const int chunks = (n1 + RW - 1) / RW;
@@ -727,10 +730,10 @@ namespace ugsdr_gpu {
 		const int row = p.row0 + lrow;
 		const int c = row % q.n_codes;
 		const int d = row / q.n_codes;
-		float2* b = smem + warp * 3 * WT;
+		float2* b = smem + warp * TILES * WT;
 		float2* xs = b + WT;
-		float2* cs = xs + WT;
-		const FftPlanDev p2 = F2::prepare(p.p2, smem + WARPS * 3 * WT);
+		float2* cs = CODE ? xs + WT : nullptr;
+		const FftPlanDev p2 = F2::prepare(p.p2, smem + WARPS * TILES * WT);
 		float2* seeds = const_cast<float2*>(p2.tw) + N2;  // after the pass tables (N2 entries)
 		build_row_seeds(seeds, min(RW, n1 - rc), NS, rc, static_cast<uint32_t>(n));
 		__syncthreads();  // pass tables and seeds: the CTA's only barrier
@@ -750,7 +753,8 @@ namespace ugsdr_gpu {
 					cp_async8(dst + e, src + e);
 			}
 		};
-		copy_rows(cs, code);
+		if constexpr (CODE)
+			copy_rows(cs, code);
 		copy_rows(xs, xg);
 		cp_async_commit();
 		const InvRowsLoadStagedN load{InvRowsLoadStaged{xs, cs, code}, N2};
