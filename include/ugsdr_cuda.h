@@ -566,9 +566,11 @@ enum ugsdr_serve_policy {
 	/* highest response ratio next: (wait + estimated service) / estimated
 	 * service, the service estimated from the request's cell-blocks (codes x
 	 * Doppler bins x block samples x blocks) and the server's measured
-	 * throughput — short searches go first, long ones age to the front; a
-	 * search estimated below 0.5 s runs on its slot's highest-priority CUDA
-	 * stream, so its blocks are dispatched ahead of running long searches */
+	 * throughput — short searches go first, long ones age to the front.  A
+	 * search estimated below 20 ms (the latency target) is short: it runs on
+	 * its slot's highest-priority CUDA stream, so its blocks are dispatched
+	 * ahead of running long searches, and one slot (with max_inflight >= 2)
+	 * admits only short searches, so long ones cannot hold every slot */
 	UGSDR_SERVE_RESPONSE_RATIO = 1
 };
 

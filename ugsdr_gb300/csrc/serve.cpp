@@ -30,8 +30,11 @@
 using namespace ugsdr_gpu;
 
 namespace {
-	// estimated service below which a search runs on a slot's high-priority stream
-	constexpr double kUrgentSeconds = 0.5;
+	// estimated service below which a search is short: it runs on a slot's
+	// high-priority stream and may take the slot kept for short requests —
+	// the served stream's latency target (p99 below 20 ms), so a request that
+	// can meet it is never queued behind longer ones
+	constexpr double kUrgentSeconds = 0.02;
 
 	// Pinned host staging that grows without freeing while the server runs
 	// (cudaFreeHost waits for the device); outgrown buffers are freed at exit.
@@ -144,20 +147,24 @@ struct ugsdr_server {
 	// measured cell-blocks per second (a first guess until work has completed)
 	double rate() const { return stats.busy_seconds > 0.05 && done_work > 0 ? done_work / stats.busy_seconds : 5e10; }
 
-	// the pending request to admit next under cfg.policy
-	std::deque<Request*>::iterator pick() {
+	// the pending request to admit next under cfg.policy (short_only: among
+	// requests estimated below kUrgentSeconds of service)
+	std::deque<Request*>::iterator pick(bool short_only) {
+		const double rate = this->rate();
+		auto admissible = [&](std::deque<Request*>::iterator it) {
+			return eligible(it) && (!short_only || (*it)->work / rate < kUrgentSeconds);
+		};
 		if (cfg.policy != UGSDR_SERVE_RESPONSE_RATIO || pending.size() < 2) {
 			for (auto it = pending.begin(); it != pending.end(); ++it)
-				if (eligible(it))
+				if (admissible(it))
 					return it;
 			return pending.end();
 		}
-		const double rate = this->rate();
 		const auto now = std::chrono::steady_clock::now();
 		auto best = pending.end();
 		double best_ratio = -1;
 		for (auto it = pending.begin(); it != pending.end(); ++it) {
-			if (!eligible(it))
+			if (!admissible(it))
 				continue;
 			const double service = std::max((*it)->work / rate, 1e-4);
 			const double wait = std::chrono::duration<double>(now - (*it)->queued).count();
@@ -236,15 +243,28 @@ struct ugsdr_server {
 	bool admit(std::unique_lock<std::mutex>& lock) {
 		if (pending.empty())
 			return false;
-		Slot* free_slot = nullptr;
-		for (auto& sl : slots)
-			if (!sl.req) {
-				free_slot = &sl;
-				break;
-			}
+		// under the response-ratio policy the last slot takes only short
+		// requests (estimated service below kUrgentSeconds), so a queue of long
+		// searches cannot hold every slot while short ones wait
+		const bool reserve = cfg.policy == UGSDR_SERVE_RESPONSE_RATIO && slots.size() >= 2;
+		Slot* free_general = nullptr;
+		Slot* free_short = nullptr;
+		for (auto& sl : slots) {
+			if (sl.req)
+				continue;
+			if (reserve && &sl == &slots.back())
+				free_short = &sl;
+			else if (!free_general)
+				free_general = &sl;
+		}
+		Slot* free_slot = free_general;
+		auto pos = free_general ? pick(false) : pending.end();
+		if (pos == pending.end() && free_short) {
+			free_slot = free_short;
+			pos = pick(true);
+		}
 		if (!free_slot)
 			return false;
-		const auto pos = pick();
 		if (pos == pending.end())
 			return false;  // only tracking requests whose bank is busy
 		Request* r = *pos;
@@ -456,6 +476,9 @@ int ugsdr_server_submit(ugsdr_server* server, const ugsdr_acq_job* job, uint64_t
 	r->ticket = server->next_ticket++;
 	r->queued = std::chrono::steady_clock::now();
 	*ticket = r->ticket;
+	if (server->trace)
+		std::fprintf(stderr, "[serve] %.1f submit ticket %llu work %.3g\n", server->since(),
+			static_cast<unsigned long long>(r->ticket), r->work);
 	server->pending.push_back(r.get());
 	server->requests[r->ticket] = std::move(r);
 	++server->stats.submitted;
