@@ -361,3 +361,25 @@ def test_iq_16_capture_search(ctx, oracle, golden_codes):
         o32 = oracle.acquire(x, n, 1, code, fs, 15000, 200, reshape=True, coherent=True)
         o64 = oracle.acquire(x, n, 1, code, fs, 15000, 200, reshape=True, coherent=True, double=True)
         check_vs_oracle(res[sv], o32, o64)
+
+
+def test_maximum_block_size_2_24(ctx, oracle, golden_codes):
+    """The largest block the engine takes (2^24 = 16,777,216 points: 1024 ms
+    of GPS L1 C/A at 16.384 MHz, the code repeated 1024 times, K = 1, 3
+    Doppler bins) on the four-step kernels with single-column tiles (the
+    4096 x 4096 split), against the FP64 oracle: Doppler bin exact, the peak
+    exact modulo the 1 ms code period (the replica repeats), levels within
+    the bar."""
+    n, fs = 1 << 24, 16.384e6
+    ca = unpack_codes(golden_codes, "gps_l1ca")
+    em = signals.Emitter(ca[5], 1.023e6, 100.25, 0.5, 45.0, data_rate=0.0)
+    raw = signals.synthesize([em], fs, n, 20.0, "ci16", seed=24)
+    x = to_complex(raw)
+    res, _ = run_engine(ctx, raw, fs, n, 1, [ca[5]], 1024, 0.5, 0.5)
+    code = oracle.upsample(np.tile(ca[5], 1024), n)
+    o64 = oracle.acquire(x, n, 1, code, fs, 0.5, 0.5, double=True)
+    r, period = res[0], 16384
+    assert r.doppler_bin == int(o64["doppler_bin"])
+    assert r.index % period == int(o64["index"]) % period
+    for f in ("level", "mean", "std", "snr", "sigma"):
+        assert abs(getattr(r, f) - o64[f]) <= RTOL * abs(o64[f]), (f, getattr(r, f), o64[f])
