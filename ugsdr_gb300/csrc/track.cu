@@ -162,7 +162,14 @@ namespace ugsdr_gpu {
 			const int n_chunks = (spm + CH - 1) / CH;
 			const double spc = p.fs / st->base;
 			const double base_freq = st->base, inv_base = 1.0 / st->base, dll_scale = st->base / 1.023e6;
+			// the loop update's constant quotients, formed once (the same values
+			// the reference's expressions give): FP64 divisions are the slowest
+			// operations of the per-epoch serial update on warp 0
+			const double fs_ms = p.fs / 1e3, half_fs_ms = p.fs / 1000 / 2;
 			const int lane = threadIdx.x & 31;
+			// epoch % period_ms of the next tap set-up, advanced by one per epoch
+			// (no 64-bit modulo on the serial path)
+			int ep_mod = static_cast<int>(st->epoch % period_ms);
 			const bool warp0 = threadIdx.x < 32;
 
 			LoopState ls{};
@@ -205,11 +212,10 @@ namespace ugsdr_gpu {
 			// of warp 0 (one tap each): split point, weight, replica offset.
 			auto tap_setup = [&]() {
 				const double code_phase = __shfl_sync(0xffffffffu, ls.code_phase, 0);
-				const long long epoch = __shfl_sync(0xffffffffu, ls.epoch, 0);
 				long long fp = 0;
 				int fl = 0;
 				if (lane < 5) {
-					const double ph = code_phase - p.fs / 1e3 * static_cast<double>(epoch % period_ms);
+					const double ph = code_phase - fs_ms * static_cast<double>(ep_mod);
 					double q = ph + spc * p.offsets[lane];
 					while (q < 0)
 						q += period;
@@ -445,18 +451,22 @@ namespace ugsdr_gpu {
 					const float ea = __shfl_sync(0xffffffffu, part, 2);
 					const float la = __shfl_sync(0xffffffffu, part, 3);
 					if (lane == 0) {
-						const double err = (p.nco_mode == 1 ? part_d : static_cast<double>(part)) / (kPi * 2.0);
-						const double ferr = static_cast<double>(ferr_f) / kPi;
+						// the reference divides by 2 pi and pi (nco_mode 1 keeps the
+						// quotients); the 64-bit NCO mode multiplies by the reciprocals
+						const double err = p.nco_mode == 1 ? part_d / (kPi * 2.0) : static_cast<double>(part) * (0.5 / kPi);
+						const double ferr = p.nco_mode == 1 ? static_cast<double>(ferr_f) / kPi : static_cast<double>(ferr_f) * (1.0 / kPi);
 						// UpdatePhase (tracking_parameters.hpp:163-165) with the pre-update frequency
 						ls.phase_fx += frac_to_fx(ls.carrier_freq * 1e-3);
-						ls.phase_rad = __dadd_rn(ls.phase_rad, __ddiv_rn(__dmul_rn(2 * kPi, ls.carrier_freq), 1000.0));
+						if (p.nco_mode == 1)  // the radian phase: the reference NCO mode's carrier phase
+							ls.phase_rad = __dadd_rn(ls.phase_rad, __ddiv_rn(__dmul_rn(2 * kPi, ls.carrier_freq), 1000.0));
 						// Pll(prompt) (tracking_parameters.hpp:495-511), loop filter in FP64
 						// in the reference's operation order, nothing contracted
 						ls.carrier_freq = __dadd_rn(ls.carrier_freq, __dsub_rn(__dsub_rn(__dmul_rn(p.k1_pll, err),
 							__dmul_rn(p.k2_pll, ls.carrier_phase_error)), __dmul_rn(p.k3_pll, ferr)));
 						ls.carrier_phase_error = err;
 						ls.phase_fx += static_cast<unsigned long long>(llrint(err * (kTwo64 / 4.0)));
-						ls.phase_rad = __dadd_rn(ls.phase_rad, __ddiv_rn(__dmul_rn(err, kPi), 2.0));
+						if (p.nco_mode == 1)
+							ls.phase_rad = __dadd_rn(ls.phase_rad, __ddiv_rn(__dmul_rn(err, kPi), 2.0));
 						ls.prev_re = pr;
 						ls.prev_im = pi;
 						// Dll(early, late) (tracking_parameters.hpp:513-528)
@@ -470,7 +480,7 @@ namespace ugsdr_gpu {
 						// code_freq / base as the reference divides it (nco_mode 1), by the
 						// reciprocal otherwise (one FP64 division less on the epoch's serial path)
 						const double ratio = p.nco_mode == 1 ? __ddiv_rn(ls.code_freq, base_freq) : __dmul_rn(ls.code_freq, inv_base);
-						ls.code_phase = __dsub_rn(ls.code_phase, __dmul_rn(p.fs / 1000 / 2, __dsub_rn(ratio, 1.0)));
+						ls.code_phase = __dsub_rn(ls.code_phase, __dmul_rn(half_fs_ms, __dsub_rn(ratio, 1.0)));
 						if (p.out) {
 							TrackOut o;
 							for (int t = 0; t < 5; ++t) {
@@ -489,6 +499,7 @@ namespace ugsdr_gpu {
 						nco_setup();
 					}
 					__syncwarp();
+					ep_mod = ep_mod + 1 == period_ms ? 0 : ep_mod + 1;
 					if (ep + 1 < p.n_epochs)
 						tap_setup();
 				}
