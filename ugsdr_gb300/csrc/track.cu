@@ -165,7 +165,7 @@ namespace ugsdr_gpu {
 			// the loop update's constant quotients, formed once (the same values
 			// the reference's expressions give): FP64 divisions are the slowest
 			// operations of the per-epoch serial update on warp 0
-			const double fs_ms = p.fs / 1e3, half_fs_ms = p.fs / 1000 / 2;
+			const double fs_ms = p.fs / 1e3, half_fs_ms = p.fs / 1000 / 2, two64_over_fs = kTwo64 / p.fs;
 			const int lane = threadIdx.x & 31;
 			// epoch % period_ms of the next tap set-up, advanced by one per epoch
 			// (no 64-bit modulo on the serial path)
@@ -179,14 +179,11 @@ namespace ugsdr_gpu {
 					st->phase_rad};
 
 			// carrier NCO of GetEpl's Translate(signal, fs, -f, -phase), lane 0
-			auto nco_setup = [&]() {
+			auto nco_setup = [&](bool first) {
 				double f = -ls.carrier_freq;
 				s_mix = fabs(f) != 0.0;
 				if (f < 0)
 					f = p.fs + f;
-				// NumericallyControlledOscillator's order (nco.hpp:17-20): a sample whose
-				// phase lands exactly on a LUT boundary (rational f / fs) then picks
-				// the same entry as the host restatement
 				if (p.nco_mode == 1) {
 					// Mixer::Translate's NCO (mixer.hpp:21-42, nco.hpp:17-20): phase
 					// reduced to [0, 2 pi), 32-bit holder and adder; carried in the
@@ -202,7 +199,13 @@ namespace ugsdr_gpu {
 					s_holder0 = h32 << 32;
 					return;
 				}
-				double av = kTwo64 * f / p.fs;
+				// the increment in NumericallyControlledOscillator's order (2^64 f) / fs
+				// (nco.hpp:17-20) for the channel's starting frequency, so a sample
+				// whose phase lands exactly on a LUT boundary (a rational f / fs, as
+				// a caller's round starting Doppler gives) picks the same entry as the
+				// host restatement; after a loop update (f from the FP64 filter) as
+				// f times the quotient 2^64 / fs formed once per launch
+				double av = first ? kTwo64 * f / p.fs : f * two64_over_fs;
 				if (av >= kTwo64)
 					av = 0.0;
 				s_adder = static_cast<unsigned long long>(av);
@@ -284,7 +287,7 @@ namespace ugsdr_gpu {
 			};
 			if (warp0) {
 				if (lane == 0)
-					nco_setup();
+					nco_setup(ls.epoch == 0);  // the channel's first epoch (not every launch: runs split differently agree)
 				tap_setup();
 			}
 			if constexpr (STAGED)
@@ -415,8 +418,9 @@ namespace ugsdr_gpu {
 						}
 						const double a = static_cast<double>(lr) * (1.0 - rel);
 						const bool plus = fabs(a + static_cast<double>(rr) * rel) > fabs(a);
-						tap_re = static_cast<float>(plus ? static_cast<double>(lr) + rr : static_cast<double>(lr) - rr);
-						tap_im = static_cast<float>(plus ? static_cast<double>(li) + ri : static_cast<double>(li) - ri);
+						// lhs +- rhs of complex<float>: float sums, as the reference adds
+						tap_re = plus ? __fadd_rn(lr, rr) : __fsub_rn(lr, rr);
+						tap_im = plus ? __fadd_rn(li, ri) : __fsub_rn(li, ri);
 					}
 					float taps_re[5], taps_im[5];
 #pragma unroll
@@ -496,7 +500,7 @@ namespace ugsdr_gpu {
 							p.out[static_cast<size_t>(ep) * p.n_channels + blockIdx.x] = o;
 						}
 						++ls.epoch;
-						nco_setup();
+						nco_setup(false);
 					}
 					__syncwarp();
 					ep_mod = ep_mod + 1 == period_ms ? 0 : ep_mod + 1;
