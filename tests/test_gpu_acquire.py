@@ -115,19 +115,22 @@ def test_odd_radix_2046_int16(ctx, oracle, golden_codes):
                         oracle.acquire(x, 2046, 6, code, 2.046e6, 5000, 1000, double=True))
 
 
-def test_large_50000_vs_oracle(ctx, oracle, golden_codes):
-    """50 MHz, 1 ms blocks: N = 50,000 (four-step path), int16 IQ."""
+@pytest.mark.parametrize("mode", [L.SPECTRUM_ONE_SIDED, L.SPECTRUM_TWO_SIDED])
+def test_large_50000_vs_oracle(ctx, oracle, golden_codes, mode):
+    """50 MHz, 1 ms blocks: N = 50,000 (four-step path), int16 IQ; one-sided
+    spectra run the row stage's pruned gather (Z's upper half is zero),
+    two-sided ones the full one."""
     ca = unpack_codes(golden_codes, "gps_l1ca")
     codes = {i: ca[i] for i in range(4)}
     raw, truth = signals.gps_l1_config(seed=9, codes=codes, fs=50e6, ms=2, visible=2, sample_type="ci16", cn0=(48, 50),
                                        max_doppler=1000)
     x = to_complex(raw)
     prns = [t["prn"] for t in truth]
-    res, _ = run_engine(ctx, raw, 50e6, 50000, 2, [ca[p] for p in prns], 1, 1000, 500)
+    res, _ = run_engine(ctx, raw, 50e6, 50000, 2, [ca[p] for p in prns], 1, 1000, 500, spectrum_mode=mode)
     for p, r, t in zip(prns, res, truth):
         code = oracle.upsample(ca[p], 50000)
-        check_vs_oracle(r, oracle.acquire(x, 50000, 2, code, 50e6, 1000, 500),
-                        oracle.acquire(x, 50000, 2, code, 50e6, 1000, 500, double=True))
+        check_vs_oracle(r, oracle.acquire(x, 50000, 2, code, 50e6, 1000, 500, spectrum_mode=mode),
+                        oracle.acquire(x, 50000, 2, code, 50e6, 1000, 500, spectrum_mode=mode, double=True))
         assert abs(r.index - t["code_phase_samples"]) <= 0.1 * 50e6 / 1.023e6  # within 0.1 chip
 
 

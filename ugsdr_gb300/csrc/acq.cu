@@ -434,13 +434,24 @@ namespace ugsdr_gpu {
 		BatchedParams p = batched_params(ctx, base, s.n);
 		const int items = nd * base.k_blocks;
 		p.out = base.spectra;
+		int cw_blocked = 0, chunks = 0;
+		size_t b_points = 0;
+		inverse_geometry(ctx, p, s.fold_mode, cw_blocked, b_points, chunks);
+		// the warp-owned row kernels' pruned gather (one-sided spectra) reads
+		// only the lower part of each signal-spectrum row: only that is stored
+		const int wr = warp_rows_mode(ctx, s.n);
+		const bool half = base.one_sided != 0 && !std::getenv("UGSDR_NO_PRUNE");
+		if (cw_blocked && wr != 0 && half)
+			with_large_ffts(p.n1, p.n2, [&](auto, auto f2) {
+				using F2 = decltype(f2);
+				if constexpr (F2::kHooked && F2::kRowsCompact)
+					p.row_keep = half_row_elems<F2>(p.n1);
+			});
 		{
 			KernelTimer timer(ctx, "acq_forward_large");
 			launch_forward(ctx, job.sample_type, p, items);
 		}
-		int cw_blocked = 0, chunks = 0;
-		size_t b_points = 0;
-		inverse_geometry(ctx, p, s.fold_mode, cw_blocked, b_points, chunks);
+		p.row_keep = 0;
 		if (cw_blocked)
 			p.n2p = static_cast<int>(b_points / p.n1);
 		const int r_max = batch_rows(s, b_points);
@@ -481,7 +492,6 @@ namespace ugsdr_gpu {
 					constexpr int CW = P::CW;
 					// the row plan that pairs with the column plan: N = N1 x N2
 					if constexpr (F2::kHooked && ((P::N1 == 400 && F2::N == 500) || (P::N1 == 200 && F2::N == 250))) {
-						const int wr = warp_rows_mode(ctx, s.n);
 						if (wr != 0) {
 							// warp-owned rows, four warps per CTA: RPW rows per warp with
 							// the code rows staged (mode 1), or three rows per warp with
@@ -495,9 +505,15 @@ namespace ugsdr_gpu {
 									inv_cols_warp_kernel<P><<<p.rows * chunks, 32 * P::WARPS, P::smem_bytes(), ctx->stream>>>(p);
 								});
 							};
+							// one-sided code spectra: the gather reads only the rows' lower
+							// halves (the rest of Z is zero) and pass 0 runs pruned DFTs
 							constexpr int RPW = kRowsPerWarp<F2::N>, W = kRowsWarps;
-							if (wr == 2)
+							if (wr == 2 && half)
+								launch_rows(inv_rows_warp_kernel<F2, CW, P::N1, 3, W, false, true>, 3, rows_warp_smem<F2, 3, W, false>());
+							else if (wr == 2)
 								launch_rows(inv_rows_warp_kernel<F2, CW, P::N1, 3, W, false>, 3, rows_warp_smem<F2, 3, W, false>());
+							else if (half)
+								launch_rows(inv_rows_warp_kernel<F2, CW, P::N1, RPW, W, true, true>, RPW, rows_warp_smem<F2, RPW, W>());
 							else
 								launch_rows(inv_rows_warp_kernel<F2, CW, P::N1, RPW, W>, RPW, rows_warp_smem<F2, RPW, W>());
 							return;
@@ -744,9 +760,16 @@ namespace ugsdr_gpu {
 			note_launch(ctx);
 			// a, b, the N-float accumulator, the pass tables (N entries)
 			const size_t smem_i = 2 * sizeof(float2) * F::N + sizeof(float) * F::N + sizeof(float2) * F::N + 16;
-			set_smem(acq_inverse_static_kernel<F>, smem_i);
 			KernelTimer timer(ctx, "acq_inverse");
-			acq_inverse_static_kernel<F><<<nd * n_codes, kThreads, smem_i, ctx->stream>>>(p);
+			auto inverse = [&](auto kernel) {
+				set_smem(kernel, smem_i);
+				kernel<<<nd * n_codes, kThreads, smem_i, ctx->stream>>>(p);
+			};
+			// one-sided spectra: pass 0 reads only the lower half of Z
+			if (p.one_sided && !std::getenv("UGSDR_NO_PRUNE"))
+				inverse(acq_inverse_static_kernel<F, true>);
+			else
+				inverse(acq_inverse_static_kernel<F>);
 			note_launch(ctx);
 		}
 	}

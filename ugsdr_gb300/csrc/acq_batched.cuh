@@ -130,6 +130,7 @@ namespace ugsdr_gpu {
 		int ld1;                // column-tile stride: N1 rounded up to odd (conflict-free smem)
 		// forward / code items
 		int code_mode;          // 1: items are codes (chips -> spectra), 0: signal (Doppler, block)
+		int row_keep;           // signal spectra: elements k2 < row_keep of each row stored (0: all)
 		const float* chips;     // code mode: chips of code `item` at chips + item * chip_stride
 		int n_chips, chip_stride, repeats, sign_segment;
 		const uint32_t* sign_masks;
@@ -212,10 +213,16 @@ namespace ugsdr_gpu {
 				acc[base + r * NS] += stat_of(cscale(cscale(v[r], inv_n), post), stat);
 		}
 	};
+	// one-sided: Z is zero above N/2, so pass 0 reads only its live inputs
+	template <int ZF>
+	struct SmallInvLoadZ : SmallInvLoad {
+		static constexpr int kZeroFrom = ZF;
+	};
 	// grid: codes x Doppler bins; unfolded rows (m == N) only.  Each thread
 	// owns the same last-pass outputs in every block, so its accumulator
-	// entries need no barrier between blocks.
-	template <class F>
+	// entries need no barrier between blocks.  HALF: one-sided spectra (the
+	// pruned pass 0 of SmallInvLoadZ)
+	template <class F, bool HALF = false>
 	__global__ void __launch_bounds__(256) acq_inverse_static_kernel(AcqParams p) {
 		extern __shared__ float2 smem[];
 		float2* a = smem;
@@ -230,8 +237,8 @@ namespace ugsdr_gpu {
 		__syncthreads();
 		const SmallInvEmit emit{acc, 1.0f / static_cast<float>(F::N), p.one_sided ? 2.0f : 1.0f, p.stat};
 		for (int blk = 0; blk < p.k_blocks; ++blk) {
-			const SmallInvLoad load{p.spectra + (static_cast<size_t>(d) * p.k_blocks + blk) * F::N, p.codes[c], F::N / 2,
-				p.one_sided};
+			const SmallInvLoadZ<HALF ? F::N / 2 + 1 : F::N> load{SmallInvLoad{p.spectra + (static_cast<size_t>(d) * p.k_blocks + blk) * F::N,
+				p.codes[c], F::N / 2, p.one_sided}};
 			F::template run_hooked<true, true>(a, b, plan, 1, F::N, load, emit);
 			__syncthreads();  // pass 0 of the next block rewrites the tiles
 		}
@@ -287,17 +294,28 @@ namespace ugsdr_gpu {
 			const int d = item / p.base.k_blocks;
 			const int blk = item - d * p.base.k_blocks;
 			const uint32_t adder = p.base.adders[p.base.d_base + d];
-			const uint64_t g0 = static_cast<uint64_t>(blk) * p.base.n + c0;
 			const int fe_on = p.base.fe_on;
 			const uint32_t fe_adder = p.base.fe_adder, phase0 = p.base.phase0;
-			for (int e = threadIdx.x; e < p.cw * n1; e += blockDim.x) {
-				const int f = e & mask, i1 = e >> p.cw_shift;
-				if (f < cw) {
-					const uint64_t g = g0 + static_cast<uint64_t>(n2) * i1 + f;
+			// a thread keeps its column f (the block is a multiple of cw) and
+			// steps its row by di: the sample index and both NCO holders
+			// advance by constants
+			const int f = threadIdx.x & mask, di = blockDim.x >> p.cw_shift;
+			if (f < cw) {
+				const int i10 = threadIdx.x >> p.cw_shift;
+				uint64_t g = static_cast<uint64_t>(blk) * p.base.n + c0 + f + static_cast<uint64_t>(n2) * i10;
+				const uint64_t dg = static_cast<uint64_t>(n2) * di;
+				uint32_t hf = static_cast<uint32_t>(g) * fe_adder, hd = phase0 + static_cast<uint32_t>(g) * adder;
+				const uint32_t dhf = static_cast<uint32_t>(dg) * fe_adder, dhd = static_cast<uint32_t>(dg) * adder;
+				float2* col = a + f * ld;
+#pragma unroll 4
+				for (int i1 = i10; i1 < n1; i1 += di) {
 					float2 v = load_sample<ST>(p.base.samples, g);
 					if (fe_on)
-						v = table_mix(v, g, fe_adder, 0u, lut);
-					a[f * ld + i1] = table_mix(v, g, adder, phase0, lut);
+						v = table_mix_holder(v, hf, lut);
+					col[i1] = table_mix_holder(v, hd, lut);
+					g += dg;
+					hf += dhf;
+					hd += dhd;
 				}
 			}
 		}
@@ -333,7 +351,7 @@ namespace ugsdr_gpu {
 	};
 	struct FwdRowsEmit {
 		float2* out;
-		int n1, n2, r0, half, one_sided, code_mode;
+		int n1, n2, r0, half, one_sided, code_mode, keep;
 		template <int R, int NS>
 		__device__ __forceinline__ void put(int f, int base, const float2 (&v)[R]) const {
 			float2* o = out + static_cast<size_t>(f) * n2 + base;
@@ -341,9 +359,14 @@ namespace ugsdr_gpu {
 			for (int r = 0; r < R; ++r) {
 				const int k2 = base + r * NS;
 				const bool zero = one_sided && (r0 + f) + static_cast<int64_t>(n1) * k2 > half;
-				// signal spectra are written whole: the inverse gather multiplies
-				// by the one-sided code spectrum, zero above N/2, with no test
-				o[r * NS] = code_mode ? (zero ? c2(0.f, 0.f) : c2(v[r].x, -v[r].y)) : v[r];
+				// signal spectra: the elements the inverse gather reads, k2 < keep
+				// (the whole row, or the lower part the pruned gather reads); it
+				// multiplies by the one-sided code spectrum, zero above N/2, with
+				// no test
+				if (code_mode)
+					o[r * NS] = zero ? c2(0.f, 0.f) : c2(v[r].x, -v[r].y);
+				else if (k2 < keep)
+					o[r * NS] = v[r];
 			}
 		}
 	};
@@ -389,7 +412,7 @@ namespace ugsdr_gpu {
 				cp_async_wait_all();
 				__syncthreads();
 				const FwdRowsEmit emit{p.out + static_cast<size_t>(item) * p.base.n + static_cast<size_t>(r0) * n2, n1, n2, r0,
-					p.base.n / 2, p.base.one_sided, p.code_mode};
+					p.base.n / 2, p.base.one_sided, p.code_mode, p.row_keep > 0 ? p.row_keep : n2};
 				auto next = [&] {
 					if (item + 1 < it1)
 						copy_rows(item + 1);
@@ -460,6 +483,26 @@ namespace ugsdr_gpu {
 		int n2;
 		__device__ __forceinline__ float2 operator()(int f, int k2) const { return g(f, k2, n2); }
 	};
+	// the same gather with Z known to be zero at k2 >= ZF in every row
+	template <int ZF>
+	struct InvRowsLoadStagedZ : InvRowsLoadStagedN {
+		static constexpr int kZeroFrom = ZF;
+	};
+	// One-sided code spectra are zero above N/2, so Z = X C is zero at
+	// k = k1 + N1 k2 > N/2, which holds in every row for k2 >= ZF =
+	// floor(N/2 / N1) + 1.  The pruned row gather reads the elements k2 < ZF
+	// rounded up to its pass-0 stride: the row elements the forward stage
+	// must store for it.
+	template <class F2>
+	constexpr int half_zero_from(int n1) {
+		return (n1 * F2::N / 2) / n1 + 1;
+	}
+	template <class F2>
+	constexpr int half_row_elems(int n1) {
+		const int zf = half_zero_from<F2>(n1), nb = F2::kFirstNB;
+		const int zl = (zf + nb - 1) / nb * nb;
+		return zl < F2::N ? zl : F2::N;
+	}
 	// Inter-step twiddle seeds of the row stage, per CTA: for each of its rows
 	// k1 = r0 + f, W_N^{-j k1} for j < NS and W_N^{-NS k1} at j = NS, where NS
 	// is the stride of the plan's last pass (whose butterflies start at base
@@ -708,17 +751,27 @@ namespace ugsdr_gpu {
 	// the twiddle seeds are built once per CTA.  B goes out in the blocked
 	// layout of inv_cols_warp_kernel.  grid: rows * ceil(N1 / (RPW WARPS)).
 	// CODE: the code rows staged in shared memory (else read through L1 / L2,
-	// which leaves room for more rows per warp)
+	// which leaves room for more rows per warp).
+	// HALF (one-sided code spectra): the code spectrum is zero above N/2, so
+	// Z = X C is zero at k = k1 + N1 k2 > N/2, which holds in every row for
+	// k2 >= ZF = floor(N/2 / N1) + 1; pass 0 reads only the elements k2 < ZL
+	// (its live inputs: ZF rounded up to its butterfly stride), and only
+	// those of the X and code rows are staged.
 	template <class F2, int RPW, int WARPS, bool CODE = true>
 	constexpr size_t rows_warp_smem() {
 		return sizeof(float2) * ((CODE ? 3 : 2) * static_cast<size_t>(WARPS) * RPW * F2::N + F2::N +
 			static_cast<size_t>(WARPS) * RPW * (F2::kLastNS + 1)) + 16;
 	}
-	template <class F2, int BCW, int BN1, int RPW, int WARPS, bool CODE = true>
+	template <class F2, int BCW, int BN1, int RPW, int WARPS, bool CODE = true, bool HALF = false>
 	__global__ void __launch_bounds__(32 * WARPS) inv_rows_warp_kernel(BatchedParams p) {
 		static_assert(F2::kHooked && F2::kPasses == 2, "warp-owned rows run two-pass hooked plans (one work tile)");
 		extern __shared__ float2 smem[];
 		constexpr int N2 = F2::N, NS = F2::kLastNS, RW = RPW * WARPS, WT = RPW * N2, TILES = CODE ? 3 : 2;
+		constexpr int ZF = HALF ? half_zero_from<F2>(BN1) : N2;
+		using Load = InvRowsLoadStagedZ<ZF>;
+		constexpr int ZL = HALF ? half_row_elems<F2>(BN1) : N2;  // staged elements per row
+		static_assert(ZL == live_inputs<Load, N2, N2 / F2::kFirstNB>() * F2::kFirstNB && ZL >= ZF,
+			"pass 0 reads the staged elements only");
 		const AcqParams& q = p.base;
 		const int n1 = p.n1, n = q.n;
 		const int chunks = (n1 + RW - 1) / RW;
@@ -744,20 +797,38 @@ namespace ugsdr_gpu {
 		const int elems = rw * N2;
 		const bool wide = (N2 % 2 == 0) && (n % 2 == 0);  // every row start 16-byte aligned
 		auto copy_rows = [&](float2* dst, const float2* src) {
-			if (wide) {
-				for (int e = 2 * lane; e < elems; e += 64)
-					cp_async16(dst + e, src + e);
+			if constexpr (ZL == N2) {
+				if (wide) {
+					for (int e = 2 * lane; e < elems; e += 64)
+						cp_async16(dst + e, src + e);
+				}
+				else {
+					for (int e = lane; e < elems; e += 32)
+						cp_async8(dst + e, src + e);
+				}
 			}
 			else {
-				for (int e = lane; e < elems; e += 32)
-					cp_async8(dst + e, src + e);
+				// the first ZL elements of each of the warp's rows
+				if (ZL % 2 == 0 && wide) {
+					constexpr int HP = ZL / 2;
+					for (int e = lane; e < rw * HP; e += 32) {
+						const int ri = e / HP, c = ri * N2 + 2 * (e - ri * HP);
+						cp_async16(dst + c, src + c);
+					}
+				}
+				else {
+					for (int e = lane; e < rw * ZL; e += 32) {
+						const int ri = e / ZL, c = ri * N2 + (e - ri * ZL);
+						cp_async8(dst + c, src + c);
+					}
+				}
 			}
 		};
 		if constexpr (CODE)
 			copy_rows(cs, code);
 		copy_rows(xs, xg);
 		cp_async_commit();
-		const InvRowsLoadStagedN load{InvRowsLoadStaged{xs, cs, code}, N2};
+		const Load load{InvRowsLoadStagedN{InvRowsLoadStaged{xs, cs, code}, N2}};
 		const float2* wseeds = seeds + warp * RPW * (NS + 1);
 		for (int blk = 0; blk < q.k_blocks; ++blk) {
 			cp_async_wait_all();

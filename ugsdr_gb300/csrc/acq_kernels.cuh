@@ -62,11 +62,15 @@ namespace ugsdr_gpu {
 	// (phase0 + i * adder mod 2^32, i.e. i additions of the adder), then the
 	// complex<float> product evaluated without contraction, as the reference's
 	// std::complex<float> multiply (table_mixer.hpp:86-97).
-	__device__ __forceinline__ float2 table_mix(float2 x, uint64_t i, uint32_t adder, uint32_t phase0, const float* lut) {
-		const uint32_t holder = phase0 + static_cast<uint32_t>(i * static_cast<uint64_t>(adder));
+	// The same product from the holder itself (callers that step it: sample
+	// i + d has holder + d * adder mod 2^32)
+	__device__ __forceinline__ float2 table_mix_holder(float2 x, uint32_t holder, const float* lut) {
 		const uint32_t idx = holder >> 26;
 		const float c = lut[idx + 16], s = lut[idx];
 		return c2(__fsub_rn(__fmul_rn(x.x, c), __fmul_rn(x.y, s)), __fadd_rn(__fmul_rn(x.x, s), __fmul_rn(x.y, c)));
+	}
+	__device__ __forceinline__ float2 table_mix(float2 x, uint64_t i, uint32_t adder, uint32_t phase0, const float* lut) {
+		return table_mix_holder(x, phase0 + static_cast<uint32_t>(i * static_cast<uint64_t>(adder)), lut);
 	}
 
 	// ------------------------------------------------------------- passes

@@ -260,6 +260,133 @@ namespace ugsdr_gpu {
 	}
 
 	// ---------------------------------------------------------------------
+	// R-point DFT whose inputs v[NZ..R) are zero and are not read: Dft<R>'s
+	// operations with the terms of those inputs left out.  Dropping x + 0,
+	// x - 0 and the c * 0 terms of the FMA chains changes no value but the
+	// sign of an exact zero, so the outputs equal Dft<R>'s on the
+	// zero-filled input in magnitude, bit for bit.
+	template <int R, bool INV, int NZ>
+	struct DftPruned {
+		UG_HD static void run(float2* v);
+	};
+
+	template <int P, bool INV, int NZ>
+	struct DftPrimePruned {
+		UG_HD static void run(float2* v) {
+			constexpr int H = (P - 1) / 2;
+			// j <= H < P - j: input P - j is zero whenever j is; sp / sm of a
+			// zero input j are zero and their terms are left out (j < NZ live)
+			constexpr int JL = NZ - 1 < H ? NZ - 1 : H;  // live pairs j = 1..JL
+			float2 sp[H + 1], sm[H + 1];
+			static_for<1, JL + 1>([&](auto jc) {
+				constexpr int j = decltype(jc)::value;
+				if constexpr (P - j < NZ) {
+					sp[j] = cadd(v[j], v[P - j]);
+					sm[j] = csub(v[j], v[P - j]);
+				}
+				else {
+					sp[j] = v[j];
+					sm[j] = v[j];
+				}
+			});
+			float2 out[P];
+			float2 dc = v[0];
+			static_for<1, JL + 1>([&](auto jc) {
+				constexpr int j = decltype(jc)::value;
+				dc = cadd(dc, sp[j]);
+			});
+			out[0] = dc;
+			static_for<1, H + 1>([&](auto kc) {
+				constexpr int k = decltype(kc)::value;
+				float2 re = v[0];
+				float2 im = c2(0.f, 0.f);
+				static_for<1, JL + 1>([&](auto jc) {
+					constexpr int j = decltype(jc)::value;
+					constexpr float c = static_cast<float>(ct::cos2pi(static_cast<long>(j) * k, P));
+					constexpr float s = static_cast<float>(ct::sin2pi(static_cast<long>(j) * k, P));
+					re = c2(re.x + c * sp[j].x, re.y + c * sp[j].y);
+					im = c2(im.x + s * sm[j].x, im.y + s * sm[j].y);
+				});
+				if constexpr (!INV) {
+					out[k] = c2(re.x + im.y, re.y - im.x);
+					out[P - k] = c2(re.x - im.y, re.y + im.x);
+				}
+				else {
+					out[k] = c2(re.x - im.y, re.y + im.x);
+					out[P - k] = c2(re.x + im.y, re.y - im.x);
+				}
+			});
+			static_for<0, P>([&](auto kc) {
+				constexpr int k = decltype(kc)::value;
+				v[k] = out[k];
+			});
+		}
+	};
+
+	template <int R, bool INV, int NZ>
+	struct DftCompositePruned {
+		UG_HD static void run(float2* v) {
+			constexpr int A = smallest_factor(R);
+			constexpr int B = R / A;
+			constexpr int AL = NZ < A ? NZ : A;  // rows a < AL hold a live input
+			float2 t[A][B];
+			static_for<0, AL>([&](auto ac) {
+				constexpr int a = decltype(ac)::value;
+				constexpr int live = (NZ - a + A - 1) / A;  // b with a + A b < NZ
+				static_for<0, live>([&](auto bc) {
+					constexpr int b = decltype(bc)::value;
+					t[a][b] = v[a + A * b];
+				});
+				DftPruned<B, INV, live>::run(t[a]);
+			});
+			static_for<0, B>([&](auto kc) {
+				constexpr int k = decltype(kc)::value;
+				float2 col[A];
+				static_for<0, AL>([&](auto ac) {
+					constexpr int a = decltype(ac)::value;
+					col[a] = twiddle_mul<static_cast<long>(a) * k, R, INV>(t[a][k]);
+				});
+				DftPruned<A, INV, AL>::run(col);
+				static_for<0, A>([&](auto rc) {
+					constexpr int r = decltype(rc)::value;
+					v[k + B * r] = col[r];
+				});
+			});
+		}
+	};
+
+	template <int R, bool INV, int NZ>
+	UG_HD void DftPruned<R, INV, NZ>::run(float2* v) {
+		static_assert(NZ >= 1, "a pruned DFT keeps input 0");
+		if constexpr (NZ >= R) {
+			Dft<R, INV>::run(v);
+		}
+		else if constexpr (NZ == 1) {
+			// a lone input: every output is v[0]
+			static_for<1, R>([&](auto kc) { v[decltype(kc)::value] = v[0]; });
+		}
+		else if constexpr (is_prime(R)) {
+			DftPrimePruned<R, INV, NZ>::run(v);
+		}
+		else if constexpr (R == 4) {
+			// Dft<4, INV> with v[3] (NZ == 3) or v[2], v[3] (NZ == 2) zero
+			float2 a0 = v[0], a1 = v[0];
+			if constexpr (NZ == 3) {
+				a0 = cadd(v[0], v[2]);
+				a1 = csub(v[0], v[2]);
+			}
+			const float2 b0 = v[1], b1 = twiddle_mul<1, 4, INV>(v[1]);
+			v[0] = cadd(a0, b0);
+			v[2] = csub(a0, b0);
+			v[1] = cadd(a1, b1);
+			v[3] = csub(a1, b1);
+		}
+		else {
+			DftCompositePruned<R, INV, NZ>::run(v);
+		}
+	}
+
+	// ---------------------------------------------------------------------
 	// One butterfly (index j < N/R) of a radix-R Stockham pass:
 	//   v[r] = in[j + r N/R] * W_{Ns R}^{r (j mod Ns)},  DFT_R(v),
 	//   out[(j / Ns) Ns R + (j mod Ns) + r Ns] = v[r].

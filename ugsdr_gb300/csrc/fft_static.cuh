@@ -88,10 +88,32 @@ namespace ugsdr_gpu {
 		__device__ static void sync() { __syncwarp(); }
 	};
 
+	// A load hook may declare kZeroFrom: its elements i >= kZeroFrom are zero
+	// in every transform (a one-sided spectrum's upper half).  Pass 0 then
+	// reads only the inputs r < live_inputs() of each butterfly and runs the
+	// pruned DFT (the same values but for the sign of exact zeros).
+	template <class L, class = void>
+	struct ZeroFrom {
+		static constexpr int value = 1 << 30;
+	};
+	template <class L>
+	struct ZeroFrom<L, std::void_t<decltype(L::kZeroFrom)>> {
+		static constexpr int value = L::kZeroFrom;
+	};
+	// inputs r of a pass-0 butterfly (element j + r N / R, j < N / R) that
+	// may be non-zero: r < ceil(kZeroFrom / (N / R))
+	template <class L, int N, int R>
+	constexpr int live_inputs() {
+		constexpr long zf = ZeroFrom<L>::value, nb = N / R;
+		return zf >= N ? R : static_cast<int>((zf + nb - 1) / nb);
+	}
+
 	template <int N, int R, int NS, bool INV, bool FIRST, bool LAST, class Load, class Emit, class G = CtaGroup>
 	__device__ __forceinline__ void hooked_pass(const float2* __restrict__ in, float2* __restrict__ out,
 		const float2* __restrict__ tw, int batch, int ld, Load& load, Emit& emit) {
 		constexpr int NB = N / R;
+		constexpr int RL = FIRST ? live_inputs<Load, N, R>() : R;
+		static_assert(RL >= 1 && RL <= R, "pass 0 reads at least its first input");
 		const int total = NB * batch;
 		for (int u = G::rank(); u < total; u += G::size()) {
 			const int f = u / NB;
@@ -100,7 +122,7 @@ namespace ugsdr_gpu {
 			float2 v[R];
 			if constexpr (FIRST) {
 #pragma unroll
-				for (int r = 0; r < R; ++r)
+				for (int r = 0; r < RL; ++r)
 					v[r] = load(f, j + r * NB);
 			}
 			else {
@@ -117,7 +139,10 @@ namespace ugsdr_gpu {
 					v[r] = INV ? cmulc(v[r], w) : cmul(v[r], w);
 				}
 			}
-			Dft<R, INV>::run(v);
+			if constexpr (RL < R)
+				DftPruned<R, INV, RL>::run(v);
+			else
+				Dft<R, INV>::run(v);
 			if constexpr (LAST) {
 				emit.template put<R, NS>(f, (j - k) * R + k, v);
 			}
@@ -190,6 +215,11 @@ namespace ugsdr_gpu {
 		return l;
 	}
 
+	template <int R, int... Rest>
+	constexpr int radix_first() {
+		return R;
+	}
+
 	template <int... Rs>
 	constexpr int radix_min() {
 		int m = 1 << 30;
@@ -207,6 +237,8 @@ namespace ugsdr_gpu {
 		static constexpr int kPasses = sizeof...(Rs);
 		// stride of the last pass (its butterflies start at base = j < kLastNS)
 		static constexpr int kLastNS = N_ / radix_last<Rs...>();
+		// butterflies of pass 0 per transform (its inputs j + r kFirstNB)
+		static constexpr int kFirstNB = N_ / radix_first<Rs...>();
 		// inverse row kernel launch bounds: a hooked two-pass plan whose widest
 		// pass over 8 rows fits 224 threads runs one shared tile and four CTAs
 		// per SM (72 registers), other plans two tiles and three CTAs
