@@ -509,13 +509,17 @@ namespace ugsdr_gpu {
 							// halves (the rest of Z is zero) and pass 0 runs pruned DFTs
 							constexpr int RPW = kRowsPerWarp<F2::N>, W = kRowsWarps;
 							if (wr == 2 && half)
-								launch_rows(inv_rows_warp_kernel<F2, CW, P::N1, 3, W, false, true>, 3, rows_warp_smem<F2, 3, W, false>());
+								launch_rows(inv_rows_warp_kernel<F2, CW, P::N1, 3, W, false, true>, 3,
+									rows_warp_smem<F2, P::N1, 3, W, false, true>());
 							else if (wr == 2)
-								launch_rows(inv_rows_warp_kernel<F2, CW, P::N1, 3, W, false>, 3, rows_warp_smem<F2, 3, W, false>());
+								launch_rows(inv_rows_warp_kernel<F2, CW, P::N1, 3, W, false, false>, 3,
+									rows_warp_smem<F2, P::N1, 3, W, false, false>());
 							else if (half)
-								launch_rows(inv_rows_warp_kernel<F2, CW, P::N1, RPW, W, true, true>, RPW, rows_warp_smem<F2, RPW, W>());
+								launch_rows(inv_rows_warp_kernel<F2, CW, P::N1, RPW, W, true, true>, RPW,
+									rows_warp_smem<F2, P::N1, RPW, W, true, true>());
 							else
-								launch_rows(inv_rows_warp_kernel<F2, CW, P::N1, RPW, W>, RPW, rows_warp_smem<F2, RPW, W>());
+								launch_rows(inv_rows_warp_kernel<F2, CW, P::N1, RPW, W, true, false>, RPW,
+									rows_warp_smem<F2, P::N1, RPW, W, true, false>());
 							return;
 						}
 						const size_t smem_r = smem_inv_rows<F2>(p);

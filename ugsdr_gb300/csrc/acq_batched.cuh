@@ -757,21 +757,47 @@ namespace ugsdr_gpu {
 	// k2 >= ZF = floor(N/2 / N1) + 1; pass 0 reads only the elements k2 < ZL
 	// (its live inputs: ZF rounded up to its butterfly stride), and only
 	// those of the X and code rows are staged.
-	template <class F2, int RPW, int WARPS, bool CODE = true>
+	// staged elements per row: the pruned gather's part, or the whole row
+	template <class F2, int BN1, bool HALF>
+	constexpr int rows_warp_staged() {
+		return HALF ? half_row_elems<F2>(BN1) : F2::N;
+	}
+	// per warp: the work tile (RPW rows of N2), the staged X rows and (CODE)
+	// code rows (RPW rows of SL each); per CTA: pass tables (N2) and seeds
+	template <class F2, int BN1, int RPW, int WARPS, bool CODE, bool HALF>
 	constexpr size_t rows_warp_smem() {
-		return sizeof(float2) * ((CODE ? 3 : 2) * static_cast<size_t>(WARPS) * RPW * F2::N + F2::N +
+		constexpr size_t SL = rows_warp_staged<F2, BN1, HALF>();
+		return sizeof(float2) * (static_cast<size_t>(WARPS) * RPW * (F2::N + (CODE ? 2 : 1) * SL) + F2::N +
 			static_cast<size_t>(WARPS) * RPW * (F2::kLastNS + 1)) + 16;
 	}
+	// the gather of the warp kernel: staged X (and code) rows at stride SL,
+	// or code rows from global memory at stride N2; Z zero at k2 >= ZF
+	template <int ZF, int SL, int N2, bool CODE>
+	struct InvRowsLoadWarp {
+		const float2* xs;
+		const float2* cs;
+		const float2* code_g;
+		static constexpr int kZeroFrom = ZF;
+		__device__ __forceinline__ float2 operator()(int f, int k2) const {
+			const int off = f * SL + k2;
+			if constexpr (CODE)
+				return cmul(xs[off], cs[off]);
+			else
+				return cmul(xs[off], __ldg(code_g + f * N2 + k2));
+		}
+	};
 	template <class F2, int BCW, int BN1, int RPW, int WARPS, bool CODE = true, bool HALF = false>
 	__global__ void __launch_bounds__(32 * WARPS) inv_rows_warp_kernel(BatchedParams p) {
 		static_assert(F2::kHooked && F2::kPasses == 2, "warp-owned rows run two-pass hooked plans (one work tile)");
 		extern __shared__ float2 smem[];
-		constexpr int N2 = F2::N, NS = F2::kLastNS, RW = RPW * WARPS, WT = RPW * N2, TILES = CODE ? 3 : 2;
+		constexpr int N2 = F2::N, NS = F2::kLastNS, RW = RPW * WARPS;
 		constexpr int ZF = HALF ? half_zero_from<F2>(BN1) : N2;
-		using Load = InvRowsLoadStagedZ<ZF>;
-		constexpr int ZL = HALF ? half_row_elems<F2>(BN1) : N2;  // staged elements per row
-		static_assert(ZL == live_inputs<Load, N2, N2 / F2::kFirstNB>() * F2::kFirstNB && ZL >= ZF,
+		constexpr int SL = rows_warp_staged<F2, BN1, HALF>();  // staged elements per row
+		using Load = InvRowsLoadWarp<ZF, SL, N2, CODE>;
+		static_assert(SL == live_inputs<Load, N2, N2 / F2::kFirstNB>() * F2::kFirstNB && SL >= ZF,
 			"pass 0 reads the staged elements only");
+		static_assert((N2 * sizeof(float2)) % 16 == 0 && (SL * sizeof(float2)) % 16 == 0, "16-byte aligned tiles");
+		constexpr int WT = RPW * (N2 + (CODE ? 2 : 1) * SL);  // a warp's region
 		const AcqParams& q = p.base;
 		const int n1 = p.n1, n = q.n;
 		const int chunks = (n1 + RW - 1) / RW;
@@ -783,10 +809,10 @@ namespace ugsdr_gpu {
 		const int row = p.row0 + lrow;
 		const int c = row % q.n_codes;
 		const int d = row / q.n_codes;
-		float2* b = smem + warp * TILES * WT;
-		float2* xs = b + WT;
-		float2* cs = CODE ? xs + WT : nullptr;
-		const FftPlanDev p2 = F2::prepare(p.p2, smem + WARPS * TILES * WT);
+		float2* b = smem + warp * WT;
+		float2* xs = b + RPW * N2;
+		float2* cs = CODE ? xs + RPW * SL : nullptr;
+		const FftPlanDev p2 = F2::prepare(p.p2, smem + WARPS * WT);
 		float2* seeds = const_cast<float2*>(p2.tw) + N2;  // after the pass tables (N2 entries)
 		build_row_seeds(seeds, min(RW, n1 - rc), NS, rc, static_cast<uint32_t>(n));
 		__syncthreads();  // pass tables and seeds: the CTA's only barrier
@@ -794,33 +820,20 @@ namespace ugsdr_gpu {
 			return;
 		const float2* code = q.codes[c] + static_cast<size_t>(r0) * N2;
 		const float2* xg = q.spectra + static_cast<size_t>(d) * q.k_blocks * n + static_cast<size_t>(r0) * N2;
-		const int elems = rw * N2;
-		const bool wide = (N2 % 2 == 0) && (n % 2 == 0);  // every row start 16-byte aligned
+		const bool wide = (n % 2 == 0);  // every row start 16-byte aligned (N2 even)
+		// the first SL elements of each of the warp's rows: src stride N2, dst stride SL
 		auto copy_rows = [&](float2* dst, const float2* src) {
-			if constexpr (ZL == N2) {
-				if (wide) {
-					for (int e = 2 * lane; e < elems; e += 64)
-						cp_async16(dst + e, src + e);
-				}
-				else {
-					for (int e = lane; e < elems; e += 32)
-						cp_async8(dst + e, src + e);
+			if (wide) {
+				constexpr int HP = SL / 2;
+				for (int e = lane; e < rw * HP; e += 32) {
+					const int ri = e / HP, h = 2 * (e - ri * HP);
+					cp_async16(dst + ri * SL + h, src + ri * N2 + h);
 				}
 			}
 			else {
-				// the first ZL elements of each of the warp's rows
-				if (ZL % 2 == 0 && wide) {
-					constexpr int HP = ZL / 2;
-					for (int e = lane; e < rw * HP; e += 32) {
-						const int ri = e / HP, c = ri * N2 + 2 * (e - ri * HP);
-						cp_async16(dst + c, src + c);
-					}
-				}
-				else {
-					for (int e = lane; e < rw * ZL; e += 32) {
-						const int ri = e / ZL, c = ri * N2 + (e - ri * ZL);
-						cp_async8(dst + c, src + c);
-					}
+				for (int e = lane; e < rw * SL; e += 32) {
+					const int ri = e / SL, h = e - ri * SL;
+					cp_async8(dst + ri * SL + h, src + ri * N2 + h);
 				}
 			}
 		};
@@ -828,7 +841,7 @@ namespace ugsdr_gpu {
 			copy_rows(cs, code);
 		copy_rows(xs, xg);
 		cp_async_commit();
-		const Load load{InvRowsLoadStagedN{InvRowsLoadStaged{xs, cs, code}, N2}};
+		const Load load{xs, cs, code};
 		const float2* wseeds = seeds + warp * RPW * (NS + 1);
 		for (int blk = 0; blk < q.k_blocks; ++blk) {
 			cp_async_wait_all();
