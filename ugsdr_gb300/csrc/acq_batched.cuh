@@ -76,6 +76,7 @@ namespace ugsdr_gpu {
 		static constexpr bool kColsCompact = false;
 		static constexpr int kColsMaxThreads = 256;
 		static constexpr int kColsMinBlocks = 2;
+		static constexpr int kFwdColsMinBlocks = 3;
 		__device__ static FftPlanDev prepare(const FftPlanDev& plan, void* dst) { return plan_in_smem(plan, dst, plan.n); }
 		template <bool INV>
 		__device__ static float2* run(float2* a, float2* b, const FftPlanDev& plan, int batch, int ld) {
@@ -264,7 +265,7 @@ namespace ugsdr_gpu {
 
 	// grid: items * ceil(N2 / cw)
 	template <int ST, class F1>
-	__global__ void __launch_bounds__(256, 3) fwd_cols_kernel(BatchedParams p) {
+	__global__ void __launch_bounds__(F1::kColsMaxThreads, F1::kFwdColsMinBlocks) fwd_cols_kernel(BatchedParams p) {
 		extern __shared__ float2 smem[];
 		__shared__ float lut[80];
 		// the 80-entry table whatever the block size (64-thread CTAs for 2-column tiles)

@@ -30,8 +30,35 @@ namespace ugsdr_gpu {
 		r.y = y;
 		return r;
 	}
-	UG_HD float2 cadd(float2 a, float2 b) { return c2(a.x + b.x, a.y + b.y); }
-	UG_HD float2 csub(float2 a, float2 b) { return c2(a.x - b.x, a.y - b.y); }
+	// Complex sums and the real-scalar multiply-add of the DFT kernels as
+	// packed FP32 pair instructions on the device (sm_100 and later: one
+	// instruction for both halves, each half rounded as the scalar form)
+#if defined(__CUDA_ARCH__) && (__CUDA_ARCH__ >= 1000)
+#define UG_PACKED_F32 1
+#endif
+	UG_HD float2 cadd(float2 a, float2 b) {
+#ifdef UG_PACKED_F32
+		return __fadd2_rn(a, b);
+#else
+		return c2(a.x + b.x, a.y + b.y);
+#endif
+	}
+	UG_HD float2 csub(float2 a, float2 b) {
+#ifdef UG_PACKED_F32
+		return __fadd2_rn(a, c2(-b.x, -b.y));
+#else
+		return c2(a.x - b.x, a.y - b.y);
+#endif
+	}
+	// acc + s a per half, the product fused into the sum (the contraction the
+	// compiler forms for the scalar expression on the device)
+	UG_HD float2 cfma_s(float s, float2 a, float2 acc) {
+#ifdef UG_PACKED_F32
+		return __ffma2_rn(c2(s, s), a, acc);
+#else
+		return c2(acc.x + s * a.x, acc.y + s * a.y);
+#endif
+	}
 	UG_HD float2 cmul(float2 a, float2 b) { return c2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
 	// a * conj(b)
 	UG_HD float2 cmulc(float2 a, float2 b) { return c2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y); }
@@ -200,8 +227,8 @@ namespace ugsdr_gpu {
 					constexpr int j = decltype(jc)::value;
 					constexpr float c = static_cast<float>(ct::cos2pi(static_cast<long>(j) * k, P));
 					constexpr float s = static_cast<float>(ct::sin2pi(static_cast<long>(j) * k, P));
-					re = c2(re.x + c * sp[j].x, re.y + c * sp[j].y);
-					im = c2(im.x + s * sm[j].x, im.y + s * sm[j].y);
+					re = cfma_s(c, sp[j], re);
+					im = cfma_s(s, sm[j], im);
 				});
 				// forward: exp(-i t) -> term = re - i*im ; inverse: re + i*im
 				if constexpr (!INV) {
@@ -304,8 +331,8 @@ namespace ugsdr_gpu {
 					constexpr int j = decltype(jc)::value;
 					constexpr float c = static_cast<float>(ct::cos2pi(static_cast<long>(j) * k, P));
 					constexpr float s = static_cast<float>(ct::sin2pi(static_cast<long>(j) * k, P));
-					re = c2(re.x + c * sp[j].x, re.y + c * sp[j].y);
-					im = c2(im.x + s * sm[j].x, im.y + s * sm[j].y);
+					re = cfma_s(c, sp[j], re);
+					im = cfma_s(s, sm[j], im);
 				});
 				if constexpr (!INV) {
 					out[k] = c2(re.x + im.y, re.y - im.x);

@@ -252,6 +252,9 @@ namespace ugsdr_gpu {
 		static constexpr bool kColsCompact = kRowsCompact;
 		static constexpr int kColsMaxThreads = kColsCompact ? 224 : 256;
 		static constexpr int kColsMinBlocks = kColsCompact ? (N_ <= 256 ? 4 : 3) : 2;
+		// forward column kernel (one item per CTA, two tiles): four CTAs per SM
+		// for a compact plan
+		static constexpr int kFwdColsMinBlocks = kColsCompact ? 4 : 3;
 		// most butterflies of one pass over `batch` transforms
 		static constexpr int most_butterflies(int batch) { return batch * (N_ / radix_min<Rs...>()); }
 		static_assert(tables_size<1, Rs...>() <= N_, "pass tables fit the N-entry table space");
@@ -302,6 +305,7 @@ namespace ugsdr_gpu {
 		static constexpr bool kColsCompact = false;
 		static constexpr int kColsMaxThreads = 256;
 		static constexpr int kColsMinBlocks = 2;
+		static constexpr int kFwdColsMinBlocks = 3;
 	};
 
 	// a load hook for plans that read their first pass from shared memory
