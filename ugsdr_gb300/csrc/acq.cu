@@ -492,17 +492,18 @@ namespace ugsdr_gpu {
 					constexpr int CW = P::CW;
 					// the row plan that pairs with the column plan: N = N1 x N2
 					if constexpr (F2::kHooked && ((P::N1 == 400 && F2::N == 500) || (P::N1 == 200 && F2::N == 250))) {
+						void (*const cols_kernel)(BatchedParams) = p.base.stat ? inv_cols_warp_kernel<P, 1> : inv_cols_warp_kernel<P, 0>;
 						if (wr != 0) {
 							// warp-owned rows, four warps per CTA: RPW rows per warp with
 							// the code rows staged (mode 1), or three rows per warp with
 							// the code rows read through L1 / L2 (mode 2)
 							auto launch_rows = [&](auto rows_kernel, int rpw, size_t smem_r) {
 								set_smem(rows_kernel, smem_r);
-								set_smem(inv_cols_warp_kernel<P>, P::smem_bytes());
+								set_smem(cols_kernel, P::smem_bytes());
 								KernelTimer timer(ctx, "acq_inverse_large");
 								run_batches([&] {
 									rows_kernel<<<p.rows * chunks_of(p.n1, rpw * kRowsWarps), 32 * kRowsWarps, smem_r, ctx->stream>>>(p);
-									inv_cols_warp_kernel<P><<<p.rows * chunks, 32 * P::WARPS, P::smem_bytes(), ctx->stream>>>(p);
+									cols_kernel<<<p.rows * chunks, 32 * P::WARPS, P::smem_bytes(), ctx->stream>>>(p);
 								});
 							};
 							// one-sided code spectra: the gather reads only the rows' lower
@@ -524,13 +525,13 @@ namespace ugsdr_gpu {
 						}
 						const size_t smem_r = smem_inv_rows<F2>(p);
 						set_smem(inv_rows_kernel<F2, CW, P::N1>, smem_r);
-						set_smem(inv_cols_warp_kernel<P>, P::smem_bytes());
+						set_smem(cols_kernel, P::smem_bytes());
 						const int t_rows = threads_of<F2>(p.p2, p.rw);
 						require(t_rows <= F2::kRowsMaxThreads, "row kernel needs more threads than its launch bound");
 						KernelTimer timer(ctx, "acq_inverse_large");
 						run_batches([&] {
 							inv_rows_kernel<F2, CW, P::N1><<<p.rows * chunks_of(p.n1, p.rw), t_rows, smem_r, ctx->stream>>>(p);
-							inv_cols_warp_kernel<P><<<p.rows * chunks, 32 * P::WARPS, P::smem_bytes(), ctx->stream>>>(p);
+							cols_kernel<<<p.rows * chunks, 32 * P::WARPS, P::smem_bytes(), ctx->stream>>>(p);
 						});
 					}
 				});

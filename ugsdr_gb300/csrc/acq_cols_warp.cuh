@@ -41,8 +41,9 @@ namespace ugsdr_gpu {
 		__device__ static __forceinline__ int prow(int k1) { return k1 + k1 / R0; }
 	};
 
-	// grid: rows x (N2 padded / CW); one CTA per (row, column chunk) over the K blocks
-	template <class P>
+	// grid: rows x (N2 padded / CW); one CTA per (row, column chunk) over the K
+	// blocks.  STAT: the job's statistic (UGSDR_STAT_ABS2 non-zero: |y|^2)
+	template <class P, int STAT>
 	__global__ void __launch_bounds__(32 * P::WARPS, P::MINB) inv_cols_warp_kernel(BatchedParams p) {
 		extern __shared__ float2 smem[];
 		__shared__ MaxIdx s_max[P::WARPS];
@@ -114,13 +115,13 @@ namespace ugsdr_gpu {
 #pragma unroll
 				for (int r = 0; r < P::R1; ++r) {
 					const float m2 = v[r].x * v[r].x + v[r].y * v[r].y;
-					acc[r] += q.stat ? m2 : m2 * rsqrtf(fmaxf(m2, 1e-30f));
+					acc[r] += STAT ? m2 : sqrt_approx(m2);
 				}
 			}
 		}
 		// scale once: |s y| = s |y| with s = 2 / N one-sided (1 / N two-sided)
 		const float s = (q.one_sided ? 2.0f : 1.0f) / static_cast<float>(q.n);
-		const float sc = q.stat ? s * s : s;
+		const float sc = STAT ? s * s : s;
 		const int n2g = chunk * P::CW + warp * P::CPW + c1;
 		MaxIdx best{-1.0f, 0xFFFFFFFFu};
 		float sum = 0.f, sq = 0.f;

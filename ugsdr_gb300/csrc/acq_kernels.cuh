@@ -188,9 +188,17 @@ namespace ugsdr_gpu {
 			dst[i] = y[i];
 	}
 
+	// |v| of a correlation sample: the hardware square-root approximation
+	// (PTX sqrt.approx.f32, one instruction; exact at 0), whose relative error
+	// is a few float ulps, far inside the search's 1e-4 tolerance
+	__device__ __forceinline__ float sqrt_approx(float x) {
+		float r;
+		asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+		return r;
+	}
 	__device__ __forceinline__ float stat_of(float2 v, int stat) {
 		const float q = v.x * v.x + v.y * v.y;
-		return stat ? q : sqrtf(q);
+		return stat ? q : sqrt_approx(q);
 	}
 
 	// block-wide first-max / sum reduction helpers
