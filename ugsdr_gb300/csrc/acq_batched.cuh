@@ -308,15 +308,26 @@ namespace ugsdr_gpu {
 				uint32_t hf = static_cast<uint32_t>(g) * fe_adder, hd = phase0 + static_cast<uint32_t>(g) * adder;
 				const uint32_t dhf = static_cast<uint32_t>(dg) * fe_adder, dhd = static_cast<uint32_t>(dg) * adder;
 				float2* col = a + f * ld;
-#pragma unroll 4
-				for (int i1 = i10; i1 < n1; i1 += di) {
-					float2 v = load_sample<ST>(p.base.samples, g);
-					if (fe_on)
-						v = table_mix_holder(v, hf, lut);
-					col[i1] = table_mix_holder(v, hd, lut);
-					g += dg;
-					hf += dhf;
-					hd += dhd;
+				// eight rows' samples in flight per thread, then their mixes
+				constexpr int U = 8;
+				for (int i1 = i10; i1 < n1; i1 += U * di) {
+					float2 v[U];
+#pragma unroll
+					for (int u = 0; u < U; ++u)
+						if (i1 + u * di < n1)
+							v[u] = load_sample<ST>(p.base.samples, g + static_cast<uint64_t>(u) * dg);
+#pragma unroll
+					for (int u = 0; u < U; ++u) {
+						if (i1 + u * di < n1) {
+							float2 w = v[u];
+							if (fe_on)
+								w = table_mix_holder(w, hf, lut);
+							col[i1 + u * di] = table_mix_holder(w, hd, lut);
+							hf += dhf;
+							hd += dhd;
+						}
+					}
+					g += U * dg;
 				}
 			}
 		}
