@@ -197,9 +197,9 @@ def inverse_flops(j):
 
 
 # DRAM bytes per inverse-transform point of the four-step kernels (inv_rows +
-# inv_cols), measured with ncu on the 200,000-point profiling case (17.5: the
+# inv_cols), measured with ncu on the 200,000-point profiling case (16.1: the
 # intermediate B buffer is 16 of it); see profiles/.
-TRAFFIC_BYTES_PER_INVERSE_POINT = 17.5
+TRAFFIC_BYTES_PER_INVERSE_POINT = 16.1
 
 
 def inverse_points(j):
@@ -396,8 +396,8 @@ def run_ours(args, world, rank):
         "gpu_launches": launches,
         "roofline": {"bound": "fp32", "kernel": inv_name, "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": achieved / fp32_peak if achieved else None, "traffic": traffic,
-                     "traffic_source": "ncu dram__bytes_read+write per inverse point (17.5 B, 200k profiling "
-                                       "cases) x points per launch" if traffic else None,
+                     "traffic_source": "ncu dram__bytes_read+write per inverse point (16.1 B, 200k profiling "
+                                       "case) x points per launch" if traffic else None,
                      "algorithmic_bytes_per_launch": bytes_inv / max(n_inv, 1),
                      "peak_source": f"{n_sm} SMs x 128 FP32 lanes x 2 x sm_max_mhz {sm_max} (MEASURED_PEAKS.json)",
                      "launches": n_inv, "avg_launch_ms": ms_inv / max(n_inv, 1),
