@@ -327,6 +327,17 @@ namespace ugsdr_gpu {
 				case UGSDR_SAMPLES_CI16: launch_fwd_cols(ctx, fwd_cols_kernel<UGSDR_SAMPLES_CI16, F1>, p, items, t1); break;
 				default: launch_fwd_cols(ctx, fwd_cols_kernel<UGSDR_SAMPLES_RI8, F1>, p, items, t1); break;
 				}
+				// signal items of the two-pass 250- / 500-point row plans: warp-owned rows
+				if constexpr (F2::kHooked && F2::kPasses == 2 && (F2::N == 250 || F2::N == 500)) {
+					if (!p.code_mode && !std::getenv("UGSDR_NO_WARP_FWD_ROWS")) {
+						constexpr int RPW = kRowsPerWarp<F2::N>, W = kRowsWarps;
+						constexpr size_t smem = fwd_rows_warp_smem<F2, RPW, W>();
+						set_smem(fwd_rows_warp_kernel<F2, RPW, W>, smem);
+						const int groups = (items + kFwdRowItems - 1) / kFwdRowItems;
+						fwd_rows_warp_kernel<F2, RPW, W><<<groups * chunks_of(p.n1, RPW * W), 32 * W, smem, ctx->stream>>>(p, items);
+						return;
+					}
+				}
 				const size_t smem = smem_rows(p, false);
 				set_smem(fwd_rows_kernel<F2>, smem);
 				const int groups = F2::kRowsCompact ? (items + kFwdRowItems - 1) / kFwdRowItems : items;

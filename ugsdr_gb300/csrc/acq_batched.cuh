@@ -460,6 +460,68 @@ namespace ugsdr_gpu {
 		}
 	}
 
+	// Warp-owned forward rows (signal items of the two-pass row plans): each
+	// warp of the CTA takes RPW of its RPW x WARPS rows through both passes
+	// for up to kFwdRowItems items, the next item's rows copied into its
+	// private tile by cp.async once pass 0 has read the current ones, with
+	// only __syncwarp between its passes; the pass tables are built once per
+	// CTA, its only barrier.  grid: ceil(items / kFwdRowItems) x
+	// ceil(N1 / (RPW WARPS)).
+	template <class F2, int RPW, int WARPS>
+	constexpr size_t fwd_rows_warp_smem() {
+		return sizeof(float2) * (static_cast<size_t>(WARPS) * RPW * 2 * F2::N + F2::N) + 16;
+	}
+	template <class F2, int RPW, int WARPS>
+	__global__ void __launch_bounds__(32 * WARPS) fwd_rows_warp_kernel(BatchedParams p, int items) {
+		static_assert(F2::kHooked && F2::kPasses == 2, "warp-owned rows run two-pass hooked plans (one work tile)");
+		static_assert((F2::N * sizeof(float2)) % 16 == 0, "16-byte aligned rows");
+		extern __shared__ float2 smem[];
+		constexpr int N2 = F2::N, RW = RPW * WARPS, WT = RPW * N2;
+		const int n1 = p.n1, n = p.base.n;
+		const int chunks = (n1 + RW - 1) / RW;
+		const int group = blockIdx.x / chunks;
+		const int rc = (blockIdx.x - group * chunks) * RW;  // the CTA's first row
+		const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+		const int r0 = rc + warp * RPW;                   // the warp's first row
+		const int rw = max(0, min(RPW, n1 - r0));         // its rows (0: idle)
+		float2* b = smem + warp * 2 * WT;
+		float2* xs = b + WT;
+		const FftPlanDev p2 = F2::prepare(p.p2, smem + WARPS * 2 * WT);
+		__syncthreads();  // pass tables: the CTA's only barrier
+		if (rw == 0)
+			return;
+		const int it0 = group * kFwdRowItems;
+		const int it1 = min(items, it0 + kFwdRowItems);
+		const int elems = rw * N2;
+		const bool wide = (n % 2 == 0);  // every row start 16-byte aligned
+		auto copy_rows = [&](int item) {
+			const float2* src = p.out + static_cast<size_t>(item) * n + static_cast<size_t>(r0) * N2;
+			if (wide) {
+				for (int e = 2 * lane; e < elems; e += 64)
+					cp_async16(xs + e, src + e);
+			}
+			else {
+				for (int e = lane; e < elems; e += 32)
+					cp_async8(xs + e, src + e);
+			}
+			cp_async_commit();
+		};
+		copy_rows(it0);
+		const FwdRowsLoad load{xs, N2};
+		const int keep = p.row_keep > 0 ? p.row_keep : N2;
+		for (int item = it0; item < it1; ++item) {
+			cp_async_wait_all();
+			__syncwarp();  // this item's rows; the previous item's last pass is done with `b`
+			const FwdRowsEmit emit{p.out + static_cast<size_t>(item) * n + static_cast<size_t>(r0) * N2, n1, N2, r0, n / 2,
+				p.base.one_sided, 0, keep};
+			auto next = [&] {  // pass 0 has read xs: the next item's rows go there
+				if (item + 1 < it1)
+					copy_rows(item + 1);
+			};
+			F2::template run_hooked_warp<false, true>(b, b, p2, rw, N2, load, emit, next);
+		}
+	}
+
 	// ------------------------------------------------------------- inverse
 	// Hooks of the static inverse plans.  Row stage: pass 0 gathers Z = X * C
 	// straight from the spectra (bins above N/2 are zero one-sided), the last
